@@ -1,0 +1,2 @@
+/* Header-only GSL stand-in for compiling the reference KDTree sources as an oracle: nothing from this header is used on the KDTree path. */
+#pragma once

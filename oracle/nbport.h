@@ -1,0 +1,65 @@
+/*
+ * Test infrastructure only. C restatement of the reference NBodylib KDTree hot path
+ * (src/KDTree/), used as the CPU checker by tests/ and as the CPU baseline by bench.py.
+ * It is never linked into the product library. Parity of this restatement is pinned
+ * against the reference itself (oracle/_ref/libnbref.so) by tests/test_oracle_port.py
+ * and against the committed golden fixtures in tests/golden/.
+ *
+ * Indices: every neighbour list and every per-particle output is in input order ("ID"
+ * in the reference, set to the input index at KDTree.cxx:1291).
+ */
+#ifndef NBPORT_H
+#define NBPORT_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct PTree PTree;
+
+/* treetype: 0 physical (TPHYS), 2 velocity (TVEL), 3 phase space (TPHS).
+   kerntype: 0 M4 spline (KSPH), 1 Gaussian, 2 Epanechnikov, 3 top-hat. period may be NULL. */
+PTree* pt_create(const double* pos, const double* vel, const double* mass, int n, int b,
+                 int treetype, int kerntype, int kernres, const double* period, int nthreads);
+void pt_destroy(PTree* t);
+int pt_num_nodes(const PTree* t);
+int pt_num_leaves(const PTree* t);
+double pt_kernnorm(const PTree* t);
+void pt_kernel_table(const PTree* t, double* table);
+void pt_ids(const PTree* t, int* ids);
+void pt_leaf_start(const PTree* t, int* leaf_start);
+double pt_build_seconds(const PTree* t);
+
+/* method 0: FindNearest(tt), 1: FindNearestPos(tt). Row i belongs to the particle with ID i. */
+int pt_knn(PTree* t, int method, int k, int nthreads, int* nn_ids, double* d2);
+/* FindNearestPos(x) for nq coordinates. */
+int pt_knn_pos(PTree* t, const double* x, int nq, int k, int nthreads, int* nn_ids, double* d2);
+/* CalcDensity(k) (KDCalcSmoothQuantities.cxx:203-305). rho in ID order. If nn_ids is not
+   NULL it receives the k neighbours of each particle (ID rows, descending d2 as the heap
+   pops them) so that tests can freeze them for the adjoint. */
+int pt_density(PTree* t, int k, double* rho, int* nn_ids);
+int pt_veldensity(PTree* t, int nsmooth, int nsearch, double* out);
+double pt_density_particle(PTree* t, int id, int k);
+double pt_veldensity_particle(PTree* t, int id, int nsmooth, int nsearch);
+int pt_fof(PTree* t, double ll, int minnum, int order, int* group, int* ngroup);
+/* cmp: 0 FOF3d, 1 FOFVel, 2 FOF6d (src/KDTree/FOFFunc.h:30-55). params as the reference. */
+int pt_fof_criterion(PTree* t, int cmp, const double* params, int minnum, int order, int* group,
+                     int* ngroup);
+int pt_ball_tagged(PTree* t, int id, double fdist2, int* out_ids);
+int pt_ball_tagged_pos(PTree* t, const double* x, double fdist2, int* out_ids);
+int pt_ball_mark(PTree* t, int id, double fdist2, int imark, int* mark, double* dist2);
+
+/* Density adjoint (no reference counterpart): L = sum_i w_i log rho_i with rho from
+   CalcDensity(k), neighbour lists nn_ids (ID rows of k, any order) and kernel-table cells
+   frozen. Inputs/outputs in ID order; pos is (n,3) row-major. */
+int pt_density_adjoint(PTree* t, int k, const int* nn_ids, const double* pos,
+                       const double* mass, const double* w, double* rho_out,
+                       double* grad_pos, double* grad_mass);
+/* Density from frozen neighbour lists and frozen table cells (cells taken from pos0),
+   evaluated at positions pos; used by the finite-difference check. */
+int pt_density_frozen(PTree* t, int k, const int* nn_ids, const double* pos0,
+                      const double* pos, const double* mass, double* rho_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
