@@ -1,0 +1,380 @@
+"""Benchmark of the KDTree hot path on GB300.
+
+Default workload (the FOF configuration): 2^20 particles, 70% in 500 Plummer spheres
++ 30% uniform background, periodic box L=100, linking length 0.2 x mean spacing,
+minnum 20. One step = GPU tree build (bucket 16) + FOF, i.e. the reference's
+KDTree(...) + FOF(ll, ngroup, 20). The line also reports the kNN-density workloads
+(32768 uniform particles in the periodic unit box with k=32 FindNearest + CalcDensity,
+and 2^20 clustered particles with CalcDensity(32)) under "components".
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+value  = particles per second with inputs already in HBM (device pointers);
+e2e    = the same through the C ABI with host buffers (H2D of positions and masses and
+         D2H of the group array inside each step);
+impl reference = the CPU restatement of the reference (oracle/) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "kNN-density queries/s & FOF particles/s, batched vs per-tree, 1 GB300"
+N_FOF = 1 << 20
+BOX = 100.0
+MINNUM = 20
+BUCKET = 16
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- workloads
+def fof_inputs():
+    from nbodylib_gb300 import synthetic as syn
+    pos, mass = syn.clustered_box(N_FOF, BOX, seed=2)
+    return pos, mass, syn.linking_length(N_FOF, BOX)
+
+
+def run_gpu(args, world, rank, local):
+    import torch
+
+    from nbodylib_gb300 import KDTree, _build, _capi
+    _build.build()
+    lib = _capi.load()
+    torch.cuda.set_device(local)
+    pos, mass, ll = fof_inputs()
+    per = [BOX] * 3
+    dpos = torch.from_numpy(pos).cuda()
+    dmass = torch.from_numpy(mass).cuda()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    def step_device():
+        t = KDTree(dpos, None, dmass, BUCKET, kerntype=0, period=per, device=True)
+        g, ng = t.FOF(ll, MINNUM)
+        t.close()
+        return ng
+
+    for _ in range(args.warmup):
+        ng = step_device()
+    torch.cuda.synchronize()
+    lib.nbk_trace_reset()
+    lib.nbk_trace_enable(1)
+    l0 = lib.nbk_launch_count()
+    times = []
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            ng = step_device()
+            e.record()
+            times.append((s, e))
+        torch.cuda.synchronize()
+    barrier(world)
+    launches = (lib.nbk_launch_count() - l0) // max(args.steps, 1)
+    lib.nbk_trace_enable(0)
+    buf = ctypes.create_string_buffer(1 << 16)
+    lib.nbk_trace_json(buf, len(buf))
+    trace = json.loads(buf.value.decode())
+    ms = [s.elapsed_time(e) for s, e in times]
+    tot_s = max_over_ranks(sum(ms) / 1e3, world)
+    value = world * N_FOF * args.steps / tot_s
+    clocks = clk.summary()
+
+    # end to end through the C ABI with host (pinned) buffers
+    hpos = torch.from_numpy(pos).pin_memory().numpy()
+    hmass = torch.from_numpy(mass).pin_memory().numpy()
+
+    def step_host():
+        t = KDTree(hpos, None, hmass, BUCKET, kerntype=0, period=per)
+        g, ng = t.FOF(ll, MINNUM)
+        t.close()
+        return g
+
+    for _ in range(max(1, args.warmup)):
+        step_host()
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        g = step_host()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e = world * N_FOF * args.steps / e2e_s
+
+    # roofline of the dominant kernel (FOF link): algorithmic bytes = 24 (position) +
+    # 4 (group id) per particle
+    link = trace.get("fof_link", {"count": 0, "ms": 0.0})
+    hbm, which = peaks()
+    achieved = None
+    if link["count"]:
+        per_launch_s = link["ms"] / link["count"] / 1e3
+        achieved = 28.0 * N_FOF / per_launch_s / 1e9
+    phases = {k: round(v["ms"] / max(v["count"], 1), 4) for k, v in trace.items()}
+    comps = knn_density_components(args, lib)
+    result = {
+        "metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot_s * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded clustered Plummer spheres + background)",
+        "config": {"workload": "FOF, 2^20 clustered particles, periodic L=100, ll=0.2 mean "
+                               "spacing, minnum 20; step = GPU tree build (b=16) + FOF",
+                   "n": N_FOF, "bucket": BUCKET, "minnum": MINNUM, "linking_length": ll,
+                   "groups": ng, "l2": "flushed (512 MB write) before every timed step",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e, "unit": "particles/s",
+                "h2d_bytes_per_step": int(pos.nbytes + mass.nbytes),
+                "d2h_bytes_per_step": int(g.nbytes + 4)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                     "kernel": "fof_link (k_link)", "peak_source": which,
+                     "algorithmic_bytes_per_launch": 28 * N_FOF},
+        "phase_ms_per_step": phases,
+        "clocks": clocks,
+        "components": comps,
+    }
+    if rank == 0 and not args.no_cpu:
+        result["cpu_baseline"] = cpu_baseline_fof(pos, mass, ll)
+    return result
+
+
+def knn_density_components(args, lib):
+    """kNN-density on the plain 32768-particle box and on 2^20 clustered particles."""
+    import torch
+
+    from nbodylib_gb300 import KDTree
+    from nbodylib_gb300 import synthetic as syn
+    out = {}
+    cases = [("uniform_32768_periodic_k32", syn.uniform_box(32768, 1.0, seed=1), [1.0] * 3, 32),
+             ("clustered_2pow20_k32", syn.clustered_box(N_FOF, BOX, seed=2), None, 32)]
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    for name, (pos, mass), per, k in cases:
+        dpos = torch.from_numpy(pos).cuda()
+        dmass = torch.from_numpy(mass).cuda()
+        n = len(mass)
+
+        def step():
+            t = KDTree(dpos, None, dmass, BUCKET, kerntype=0, period=per, device=True)
+            nn, d2 = t.FindNearest(k)
+            rho = t.CalcDensity(k)
+            t.sync()
+            t.close()
+            return rho
+
+        for _ in range(3):
+            step()
+        lib.nbk_trace_reset()
+        lib.nbk_trace_enable(1)
+        ms = []
+        for _ in range(max(3, args.steps)):
+            flush.zero_()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            step()
+            e.record()
+            torch.cuda.synchronize()
+            ms.append(s.elapsed_time(e))
+        lib.nbk_trace_enable(0)
+        buf = ctypes.create_string_buffer(1 << 16)
+        lib.nbk_trace_json(buf, len(buf))
+        tr = json.loads(buf.value.decode())
+        dens = tr.get("knn_density", {"count": 1, "ms": float("nan")})
+        kd_ms = dens["ms"] / max(dens["count"], 1)
+        out[name] = {
+            "n": n, "k": k,
+            "step_ms": float(np.mean(ms)),
+            "queries_per_s_step": n / (np.mean(ms) / 1e3),
+            "density_kernel_ms": kd_ms,
+            "density_queries_per_s": n / (kd_ms / 1e3),
+            "fp64_flop_per_query": 20 * k,
+            "algorithmic_bytes_per_query": 40,
+            "phase_ms": {kk: round(v["ms"] / max(v["count"], 1), 4) for kk, v in tr.items()},
+        }
+    return out
+
+
+def cpu_baseline_fof(pos, mass, ll):
+    import oracle
+    oracle.build(ref=False)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    reps = 0
+    while reps < 2:
+        o = oracle.OracleTree(pos, None, mass, BUCKET, 0, 0, 1000, [BOX] * 3, backend="port",
+                              nthreads=threads)
+        o.fof(ll, MINNUM)
+        o.close()
+        reps += 1
+    dt = (time.perf_counter() - t0) / reps
+    return {"value": N_FOF / dt, "unit": "particles/s", "cores": threads, "kind": "port",
+            "sample": f"{reps} full steps (tree build with {threads} OpenMP threads + serial "
+                      "FOF, as the reference ships them) on the 2^20 FOF workload"}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return None
+    import oracle
+    oracle.build(ref=False)
+    pos, mass, ll = fof_inputs()
+    threads = os.cpu_count() or 1
+    for _ in range(min(args.warmup, 1)):
+        o = oracle.OracleTree(pos, None, mass, BUCKET, 0, 0, 1000, [BOX] * 3, backend="port",
+                              nthreads=threads)
+        o.fof(ll, MINNUM)
+        o.close()
+    steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o = oracle.OracleTree(pos, None, mass, BUCKET, 0, 0, 1000, [BOX] * 3, backend="port",
+                              nthreads=threads)
+        o.fof(ll, MINNUM)
+        o.close()
+    dt = (time.perf_counter() - t0) / steps
+    v = N_FOF / dt
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "particles/s",
+            "n_gpus": world, "steps": steps, "warmup": min(args.warmup, 1),
+            "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "FOF, 2^20 clustered particles, periodic L=100, ll=0.2 mean "
+                                   "spacing, minnum 20; step = tree build (b=16) + FOF",
+                       "n": N_FOF},
+            "cpu_baseline": {"value": v, "unit": "particles/s", "cores": threads, "kind": "port",
+                             "sample": f"{steps} full steps on the host cores (build with "
+                                       f"{threads} OpenMP threads, FOF serial as shipped)"},
+            "e2e": {"value": v, "unit": "particles/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+    if args.impl == "reference":
+        # only rank 0 times the CPU path; no process group is needed
+        world = int(os.environ.get("WORLD_SIZE", "1"))
+        res = run_reference(args, world, int(os.environ.get("RANK", "0")))
+        if res is not None:
+            print(json.dumps(res), flush=True)
+        return
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        res = run_reference(args, world, rank)
+    else:
+        res = run_gpu(args, world, rank, local)
+    if rank == 0 and res is not None:
+        print(json.dumps(res), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,267 @@
+/*
+ * nbkdt.h -- C ABI of the GB300-native KDTree hot path (tree build, kNN, SPH density,
+ * ball search, friends-of-friends), implemented by hand-written sm_103a CUDA kernels in
+ * libnbkdt.so.
+ *
+ * Each entry point replaces one method of the reference C++ class NBody::KDTree
+ * (pelahi/NBodylib, src/KDTree/KDTree.h); the comment above each declaration names the
+ * reference interface it stands in for. The C++ drop-in class in include/nbkdt/KDTree.hpp
+ * and the Python binding in nbodylib_gb300/ are thin layers over these calls.
+ *
+ * Conventions
+ *  - Every call returns an int status (NBK_OK = 0); nbk_last_error() returns a message
+ *    for the calling thread's most recent failure. Nothing aborts the process: where the
+ *    reference prints and calls exit(1) (e.g. CalcDensity with fewer than k neighbours,
+ *    KDCalcSmoothQuantities.cxx:273-276) the call returns NBK_ERR_TOO_FEW.
+ *  - Tree order: the tree reorders particles into its own leaf order (the reference
+ *    permutes the caller's Particle array, KDTree.h:12-15). "Tree index" means a position
+ *    in that order; nbk_get_perm maps tree index -> input index (the reference's ID,
+ *    KDTree.cxx:1291). Neighbour lists hold tree indices, as the reference's do
+ *    (KDTree.h:295); per-particle quantities (density, FOF groups) are returned in input
+ *    order, as the reference's ID-indexed arrays are (KDTree.h:399, :474).
+ *  - Memory: by default every pointer argument is host memory and calls are synchronous.
+ *    A tree created with NBK_DEVICE_PTRS takes device pointers for all inputs and outputs
+ *    on all its calls, runs on its stream (nbk_set_stream) and does not synchronise.
+ *  - Arithmetic is FP64 throughout: distances are computed as ((dx*dx + dy*dy) + dz*dz)
+ *    with separately rounded operations, as the reference computes them
+ *    (DistFunc.h:14-19), so neighbour selection and linking decisions are bit-exact.
+ */
+#ifndef NBKDT_H
+#define NBKDT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define NBK_OK 0
+#define NBK_ERR_INVALID 1      /* bad argument (null pointer, k out of range, NaN input) */
+#define NBK_ERR_UNSUPPORTED 2  /* a reference option this build does not run on the GPU */
+#define NBK_ERR_CUDA 3         /* a CUDA runtime call failed */
+#define NBK_ERR_NOMEM 4        /* device or host allocation failed */
+#define NBK_ERR_TOO_FEW 5      /* fewer than k neighbours exist (reference: exit(1)) */
+#define NBK_ERR_DEVICE 6       /* a device-side bound (iteration cap, capacity) was hit */
+
+/* ---- tree types (KDTree.h:90) and kernel types (KDTree.h:97) ---- */
+#define NBK_TPHYS 0
+#define NBK_TPROJ 1
+#define NBK_TVEL 2
+#define NBK_TPHS 3
+#define NBK_TMETRIC 4
+#define NBK_KSPH 0
+#define NBK_KGAUSS 1
+#define NBK_KEPAN 2
+#define NBK_KTH 3
+
+/* ---- creation flags ---- */
+#define NBK_DEVICE_PTRS 1u /* all pointer arguments of this tree's calls are device pointers */
+
+/* ---- kNN variants ---- */
+#define NBK_FINDNEAREST 0    /* KDTree::FindNearest(tt, ...)    (KDFindNearest.cxx:247-318) */
+#define NBK_FINDNEARESTPOS 1 /* KDTree::FindNearestPos(tt, ...) (KDFindNearest.cxx:320-334) */
+
+/* ---- periodic image modes ---- */
+/* Reproduce the reference's image gates exactly, including its comparison of a squared
+   distance with a distance for the 2-D and 3-D images (KDSplitNode.cxx:1129-1146). */
+#define NBK_PERIODIC_REF 0
+/* Gate every image by sqrt(top) > wall distance: the exact minimum-image kNN. */
+#define NBK_PERIODIC_MIN_IMAGE 1
+
+/* ---- FOF comparators (FOFFunc.h:30-55) ---- */
+#define NBK_FOF3D 0
+#define NBK_FOFVEL 1
+#define NBK_FOF6D 2
+
+typedef struct nbk_tree nbk_tree;
+typedef struct nbk_batch nbk_batch;
+
+/* Message for the calling thread's most recent failed call ("" if none). */
+const char* nbk_last_error(void);
+
+/* Library version string and the device it runs on. (No reference counterpart.) */
+const char* nbk_version(void);
+
+/* Number of CUDA kernels this library has launched since it was loaded; lets a caller
+   count the device work of a call sequence. (No reference counterpart.) */
+long long nbk_launch_count(void);
+
+/* Phase trace (no reference counterpart; the reference has only ad-hoc std::chrono
+   timing macros in src/tests/test_kdtree.cxx:19-22). While enabled, each named phase
+   (tree build, kNN search, FOF link, ...) is bracketed by a CUDA event pair on the
+   stream it runs on, without synchronising; nbk_trace_json resolves the pending events
+   and writes {"phase": {"count": c, "ms": total}, ...} into buf (NUL-terminated) and
+   returns the length it needs. */
+int nbk_trace_enable(int on);
+int nbk_trace_reset(void);
+int64_t nbk_trace_json(char* buf, int64_t cap);
+
+/*
+ * Build a tree. Replaces KDTree::KDTree(Particle*, Int_t numparts, Int_t bucket_size,
+ * int TreeType, int KernType, int KernRes, int SplittingCriterion, int Aniso,
+ * int ScaleSpace, Double_t* Period, ...)  (KDTree.h:229-245, KDTree.cxx:1238-1306).
+ *  pos  : n x 3 positions, row-major (x, y, z)
+ *  vel  : n x 3 velocities or NULL (needed by nbk_veldensity, nbk_fof_criterion)
+ *  mass : n masses or NULL (unit masses)
+ *  period: 3 box lengths or NULL (non-periodic)
+ * Supported: treetype NBK_TPHYS; kernel types all four; splitting 0, aniso 0,
+ * scale_space 0. Anything else returns NBK_ERR_UNSUPPORTED. The tree is built on the
+ * GPU with the reference's rules (split dimension of largest spread, median split with
+ * the left child taking ceil(size/2), leaf when size <= bucket_size), so its leaves hold
+ * the same particle sets as the reference's.
+ */
+int nbk_create(const double* pos, const double* vel, const double* mass, int64_t n,
+               int bucket_size, int treetype, int kerntype, int kernres,
+               int splitting_criterion, int aniso, int scale_space, const double* period,
+               unsigned flags, nbk_tree** out);
+
+/* Free the tree. Replaces KDTree::~KDTree (KDTree.cxx:1340-1356); the caller restores
+   its own particle order with the permutation (see nbk_get_perm). */
+int nbk_destroy(nbk_tree* tree);
+
+/* Set the CUDA stream (a cudaStream_t) the tree's kernels run on; NULL = default. */
+int nbk_set_stream(nbk_tree* tree, void* stream);
+/* Wait for all work queued on the tree's stream. */
+int nbk_sync(nbk_tree* tree);
+
+/* KDTree::GetNumNodes / GetNumLeafNodes / GetBucketSize (KDTree.h:282-284). */
+int nbk_get_counts(const nbk_tree* tree, int64_t* numparts, int64_t* numnodes,
+                   int64_t* numleafnodes, int32_t* bucket_size);
+/* perm[t] = input index of the particle at tree index t (the reference's
+   bucket[t].GetID(), KDTree.cxx:1291). */
+int nbk_get_perm(const nbk_tree* tree, int32_t* perm);
+/* The kernel table (kernres doubles) and its normalisation, as
+   KDTree::KernelConstruction builds them (KDTree.cxx:1144-1183). */
+int nbk_get_kernel(const nbk_tree* tree, double* table, double* kernnorm);
+
+/*
+ * k nearest neighbours of every particle. Replaces KDTree::FindNearest(Int_t** nn,
+ * Double_t** dist2, Int_t Nsearch) and FindNearestPos(Int_t**, Double_t**, Int_t)
+ * (KDFindNearest.cxx:444-456), i.e. FindNearest(tt)/FindNearestPos(tt) for every tt.
+ * variant: NBK_FINDNEAREST or NBK_FINDNEARESTPOS; periodic_mode as above.
+ * nn, d2: n x k, row t = the particle at tree index t; neighbours are tree indices in
+ * ascending squared distance. Non-periodic trees exclude the particle itself and any
+ * particle at distance 0 (KDLeafNode.cxx:19-21); periodic FindNearest drops the nearest
+ * entry (normally the particle itself) and periodic FindNearestPos keeps it
+ * (KDFindNearest.cxx:250,315-331).
+ */
+int nbk_knn(nbk_tree* tree, int k, int variant, int periodic_mode, int32_t* nn, double* d2);
+
+/* k nearest neighbours of nq coordinates (nq x 3). Replaces
+   KDTree::FindNearestPos(Double_t* x, Int_t* nn, Double_t* dist2, Int_t Nsearch)
+   (KDFindNearest.cxx:509-520); nothing is excluded. */
+int nbk_knn_points(nbk_tree* tree, const double* x, int64_t nq, int k, int periodic_mode,
+                   int32_t* nn, double* d2);
+
+/*
+ * SPH density of every particle. Replaces KDTree::CalcDensity(Int_t Nsmooth)
+ * (KDCalcSmoothQuantities.cxx:203-305): non-periodic kNN excluding the particle,
+ * h = 0.5 sqrt(d2 of the k-th), w = 0.5 Wsm(r/h) h^-3, rho_i += w m_j and rho_j += w m_i.
+ * rho: n values in input order (the reference writes Particle::rho). Like the
+ * reference, the period is ignored.
+ */
+int nbk_density(nbk_tree* tree, int k, double* rho);
+
+/* Gather-only density of selected particles. Replaces KDTree::CalcDensityParticle
+   (KDCalcSmoothQuantities.cxx:768-843): no 0.5 factor, no scatter.
+   targets: tree indices. out: one value per target. */
+int nbk_density_particles(nbk_tree* tree, const int32_t* targets, int64_t ntargets, int k,
+                          double* out);
+
+/* Velocity-space density. Replaces KDTree::CalcVelDensity(Int_t Nsmooth, Int_t Nsearch)
+   (KDCalcSmoothQuantities.cxx:309-389): physical kNN (Nsearch), then the Nsmooth nearest
+   in velocity, h = 0.5 max |dv|, sum of Wsm(|dv|/h) h^-3 with unit weights. out: input
+   order. Requires velocities. */
+int nbk_veldensity(nbk_tree* tree, int nsmooth, int nsearch, double* out);
+
+/* One traversal computing both nbk_density(k) and nbk_veldensity(nsmooth, k): the
+   reference's CalcDensity(k) followed by CalcVelDensity(nsmooth, k) use the same
+   neighbour search. rho and veldens: input order. */
+int nbk_density_veldensity(nbk_tree* tree, int k, int nsmooth, double* rho, double* veldens);
+
+/* Velocity density of selected particles. Replaces KDTree::CalcVelDensityParticle
+   (KDCalcSmoothQuantities.cxx:845-920). targets: tree indices. */
+int nbk_veldensity_particles(nbk_tree* tree, const int32_t* targets, int64_t ntargets,
+                             int nsmooth, int nsearch, double* out);
+
+/*
+ * Fixed-radius search around particles. Replaces KDTree::SearchBallPosTagged(Int_t tt,
+ * Double_t fdist2) (KDFindNearest.cxx:618-626, 664-672) for a batch of targets (tree
+ * indices): every particle with d2 < fdist2, excluding the target itself; periodic trees
+ * search the direct position and every mirror image whose wall distance is below the
+ * radius (KDSplitNode.cxx:1389-1414) and then include the target, as the reference does.
+ * Results are CSR: offsets[ntargets+1], out = tree indices. If out_capacity is too small
+ * the call fills offsets, sets *total and returns NBK_ERR_INVALID without writing out.
+ */
+int nbk_ball_tagged(nbk_tree* tree, const int32_t* targets, int64_t ntargets, double fdist2,
+                    int64_t* offsets, int32_t* out, int64_t out_capacity, int64_t* total);
+
+/* As nbk_ball_tagged for arbitrary coordinates (nq x 3). Replaces
+   KDTree::SearchBallPosTagged(Double_t* x, Double_t fdist2) (KDFindNearest.cxx:628-636). */
+int nbk_ball_tagged_points(nbk_tree* tree, const double* x, int64_t nq, double fdist2,
+                           int64_t* offsets, int32_t* out, int64_t out_capacity,
+                           int64_t* total);
+
+/* Replaces KDTree::SearchBallPos(Int_t tt, Double_t fdist2, Int_t imark, Int_t* nn,
+   Double_t* dist2) (KDFindNearest.cxx:567-573): nn[ID] = imark and dist2[ID] = d2 for
+   every particle found; arrays are input-order and caller-owned, entries not found are
+   left untouched. The target is included exactly when the reference includes it (when a
+   node on its root-to-leaf path lies wholly inside the radius,
+   KDSplitNode.cxx:457-467, KDLeafNode.cxx:250-263). target: tree index. */
+int nbk_ball_mark(nbk_tree* tree, int32_t target, double fdist2, int32_t imark, int32_t* nn,
+                  double* dist2);
+
+/*
+ * Friends-of-friends. Replaces KDTree::FOF(Double_t fdist, Int_t& numgroup, Int_t minnum,
+ * int order) (KDFOF.cxx:29-153): particles are linked when d2 < fdist^2 (periodic
+ * images as KDSplitNode.cxx:1602-1646). group: input order, 0 = no group; groups are
+ * numbered 1..ngroup by their first member in tree order, groups smaller than minnum
+ * are dropped; order = 1 renumbers by decreasing size (ties by first member).
+ */
+int nbk_fof(nbk_tree* tree, double fdist, int32_t minnum, int order, int32_t* group,
+            int32_t* ngroup);
+
+/* Replaces KDTree::FOFCriterion(FOFcompfunc cmp, Double_t* params, Int_t& numgroup,
+   Int_t minnum, int order) (KDFOF.cxx:157-265) for the comparators FOF3d, FOFVel and
+   FOF6d (FOFFunc.h:30-55), selected by `comparator`. params: at least 8 doubles, laid
+   out as the reference's (params[0] tree type, [1]/[2] search distance^2, [6]/[7]
+   linking lengths^2). An arbitrary host FOFcompfunc cannot run on the GPU: the C++
+   drop-in maps the three known functions to this call and reports any other as
+   NBK_ERR_UNSUPPORTED. */
+int nbk_fof_criterion(nbk_tree* tree, int comparator, const double* params, int32_t minnum,
+                      int order, int32_t* group, int32_t* ngroup);
+
+/*
+ * Density adjoint (no reference counterpart; the reference has no gradients).
+ * Forward: rho = nbk_density(k). Loss L = sum_i w_i log rho_i. With the neighbour sets
+ * and the kernel-table cells frozen at the forward pass, returns dL/dpos (n x 3) and
+ * dL/dmass (n), all in input order. Kernel weights are recomputed in the backward
+ * kernel, not stored.
+ */
+int nbk_density_adjoint(nbk_tree* tree, int k, const double* w, double* rho,
+                        double* grad_pos, double* grad_mass);
+
+/*
+ * Batched path: many independent trees (one per group, e.g. per FOF halo) built and
+ * searched together. offsets: ngroups+1 CSR offsets into pos/mass. bucket_size <= 0
+ * selects the autotuned leaf size. Replaces a caller loop of
+ * KDTree(group particles) + CalcDensity(min(k, n_g - 1)) per group.
+ */
+int nbk_batch_create(const double* pos, const double* mass, const int64_t* offsets,
+                     int64_t ngroups, int bucket_size, int kerntype, int kernres,
+                     unsigned flags, nbk_batch** out);
+int nbk_batch_destroy(nbk_batch* batch);
+int nbk_batch_set_stream(nbk_batch* batch, void* stream);
+/* Density of every particle of every group, k clamped per group to n_g - 1. rho: input
+   order. use_graph != 0 replays the search as a captured CUDA graph. */
+int nbk_batch_density(nbk_batch* batch, int k, double* rho, int use_graph);
+/* The plain comparator: the same density computed by one build + one kNN-density
+   launch sequence per group, looping over groups on the host. */
+int nbk_batch_density_pertree(nbk_batch* batch, int k, double* rho);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NBKDT_H */

@@ -1,0 +1,786 @@
+// GPU kd-tree build (replaces KDTree::BuildNodes + MedianPos + DetermineSplitDim,
+// src/KDTree/KDTree.cxx:970-1055, 328-370, 459-504).
+//
+// The reference builds recursively: split dimension = largest spread (ties to the lowest
+// dimension), split at index start + (size-1)/2 with the left child [start, split+1),
+// leaf when size <= b. Because the median partition of a node is unique (up to ties in
+// the coordinate), building level by level with the same rules yields nodes holding the
+// same particle sets as the reference's, hence the same node counts and bounding boxes.
+//
+// Phase 1 (levels whose nodes hold more than kLocalMax particles): for all nodes of a
+// level at once, over chunks of kChunk particles:
+//   bbox      segmented min/max of x, y, z (order-preserving uint64 keys, atomics)
+//   split     per node: spread, split dimension, target rank
+//   select    8 radix passes of 8 bits find the key of the median particle exactly
+//   partition stable 3-way (less / equal / greater) scatter into the other buffer
+// Phase 2: one CTA per subtree of <= kLocalMax particles finishes it in shared memory,
+// level by level, sorting each node by its split key with a bitonic network, and writes
+// the final tree-order arrays.
+#include <algorithm>
+#include <vector>
+
+#include "nbk_build.h"
+
+namespace nbk {
+
+namespace {
+
+constexpr int kChunk = 4096;
+constexpr int kThreads = 256;
+constexpr int kRounds = kChunk / kThreads;
+constexpr int kSortCap = 4 * kLocalMax;
+constexpr int kLevelCap = kLocalMax;  // level lists hold up to 2*size/(b+1) nodes
+
+struct GNode {
+  int start, size;  // absolute tree-index range
+  int node;         // absolute node index
+  int dim;
+  int k;            // rank still to find inside the current prefix class
+  int n_less;       // particles with key below the current prefix class
+  int need_eq;      // after selection: equal-key particles that go left
+  int total_eq;
+  int first_chunk, nchunks;
+  int first_diff;   // highest bit where the keys of the split dimension can differ
+  int pad;
+  unsigned long long prefix, mask;
+  unsigned long long kmin[3], kmax[3];
+};
+
+struct Chunk {
+  int g;      // gnode index within the level
+  int start;  // absolute start
+  int len;
+  int off;    // offset of the chunk inside its node
+};
+
+struct LRoot {
+  int start, size;  // absolute range
+  int nbase;        // node index of the tree's root
+  int h;            // heap index of this subtree root within its tree
+  int buf;          // which ping-pong buffer holds its particles
+  int pad;
+};
+
+__device__ __forceinline__ double coord_of(const double* X, const double* Y, const double* Z,
+                                           int d, int i) {
+  return d == 0 ? X[i] : (d == 1 ? Y[i] : Z[i]);
+}
+
+__global__ void k_init_soa(const double* __restrict__ pos_in, double* X, double* Y, double* Z,
+                           int* ID, int64_t n, int* err) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x = pos_in[3 * i], y = pos_in[3 * i + 1], z = pos_in[3 * i + 2];
+  if (!(x == x) || !(y == y) || !(z == z) || isinf(x) || isinf(y) || isinf(z))
+    atomicExch(err, 1);
+  X[i] = x;
+  Y[i] = y;
+  Z[i] = z;
+  ID[i] = (int)i;
+}
+
+__global__ void k_gnode_reset(GNode* g, int ng) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ng) return;
+  for (int d = 0; d < 3; d++) {
+    g[i].kmin[d] = ~0ull;
+    g[i].kmax[d] = 0ull;
+  }
+}
+
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w < v ? w : v;
+  }
+  return v;
+}
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w > v ? w : v;
+  }
+  return v;
+}
+
+__global__ void __launch_bounds__(kThreads) k_bbox(const Chunk* __restrict__ chunks, GNode* g,
+                                                   const double* X, const double* Y,
+                                                   const double* Z) {
+  Chunk c = chunks[blockIdx.x];
+  unsigned long long mn[3] = {~0ull, ~0ull, ~0ull}, mx[3] = {0ull, 0ull, 0ull};
+  for (int i = threadIdx.x; i < c.len; i += kThreads) {
+    int p = c.start + i;
+    unsigned long long k0 = okey(X[p]), k1 = okey(Y[p]), k2 = okey(Z[p]);
+    mn[0] = min(mn[0], k0);
+    mx[0] = max(mx[0], k0);
+    mn[1] = min(mn[1], k1);
+    mx[1] = max(mx[1], k1);
+    mn[2] = min(mn[2], k2);
+    mx[2] = max(mx[2], k2);
+  }
+  __shared__ unsigned long long s[6][kThreads / 32];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int d = 0; d < 3; d++) {
+    unsigned long long a = warp_min_u64(mn[d]), b = warp_max_u64(mx[d]);
+    if (lane == 0) {
+      s[d][w] = a;
+      s[3 + d][w] = b;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    int d = threadIdx.x;
+    unsigned long long a = ~0ull, b = 0ull;
+    for (int i = 0; i < kThreads / 32; i++) {
+      a = min(a, s[d][i]);
+      b = max(b, s[3 + d][i]);
+    }
+    atomicMin(&g[c.g].kmin[d], a);
+    atomicMax(&g[c.g].kmax[d], b);
+  }
+}
+
+__device__ void write_node(NodeRec* node, NodeX* nodex, int idx, const double lo[3],
+                           const double hi[3], int start, int count, int dim, double split_val) {
+  NodeRec r;
+  NodeX x;
+  for (int d = 0; d < 3; d++) {
+    r.lo[d] = __double2float_rd(lo[d]);
+    r.hi[d] = __double2float_ru(hi[d]);
+    x.lo[d] = lo[d];
+    x.hi[d] = hi[d];
+  }
+  r.start = start;
+  r.count = count;
+  x.split_dim = dim;
+  x.split_val = split_val;
+  x.pad = 0;
+  node[idx] = r;
+  nodex[idx] = x;
+}
+
+// DetermineSplitDim (KDTree.cxx:459-504): spread = max - min per dimension in FP64, the
+// first strictly larger spread wins.
+__global__ void k_gnode_split(GNode* g, int ng, NodeRec* node, NodeX* nodex) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ng) return;
+  GNode s = g[i];
+  double lo[3], hi[3];
+  for (int d = 0; d < 3; d++) {
+    lo[d] = okey_inv(s.kmin[d]);
+    hi[d] = okey_inv(s.kmax[d]);
+  }
+  int dim = 0;
+  double cur = dsub(hi[0], lo[0]);
+  for (int d = 1; d < 3; d++) {
+    double sp = dsub(hi[d], lo[d]);
+    if (sp > cur) {
+      dim = d;
+      cur = sp;
+    }
+  }
+  s.dim = dim;
+  s.k = (s.size - 1) / 2;
+  s.n_less = 0;
+  s.prefix = 0;
+  s.mask = 0;
+  unsigned long long x = s.kmin[dim] ^ s.kmax[dim];
+  s.first_diff = x ? 63 - __clzll((long long)x) : -1;
+  g[i] = s;
+  // the split value is written once the median key is known (k_chunk_scan)
+  write_node(node, nodex, s.node, lo, hi, s.start, s.size, dim, 0.0);
+}
+
+__global__ void __launch_bounds__(kThreads) k_hist(const Chunk* __restrict__ chunks,
+                                                   const GNode* __restrict__ g, const double* X,
+                                                   const double* Y, const double* Z,
+                                                   unsigned* hist, int shift) {
+  Chunk c = chunks[blockIdx.x];
+  const GNode& s = g[c.g];
+  if (s.first_diff < shift) return;  // this byte is shared by every key of the node
+  __shared__ unsigned h[256];
+  for (int i = threadIdx.x; i < 256; i += kThreads) h[i] = 0;
+  __syncthreads();
+  int d = s.dim;
+  unsigned long long mask = s.mask, prefix = s.prefix;
+  for (int i = threadIdx.x; i < c.len; i += kThreads) {
+    unsigned long long key = okey(coord_of(X, Y, Z, d, c.start + i));
+    if ((key & mask) == prefix) atomicAdd(&h[(key >> shift) & 255], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 256; i += kThreads)
+    if (h[i]) atomicAdd(&hist[(size_t)c.g * 256 + i], h[i]);
+}
+
+// One warp per node: find the digit bucket that holds rank k.
+__global__ void k_select(GNode* g, int ng, unsigned* hist, int shift) {
+  int gi = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  int lane = threadIdx.x & 31;
+  if (gi >= ng) return;
+  GNode s = g[gi];
+  unsigned long long byte_mask = 255ull << shift;
+  if (s.first_diff < shift) {
+    if (lane == 0) {
+      g[gi].prefix = s.prefix | (s.kmin[s.dim] & byte_mask);
+      g[gi].mask = s.mask | byte_mask;
+    }
+    return;
+  }
+  unsigned* hh = hist + (size_t)gi * 256;
+  unsigned c[8];
+  unsigned sum = 0;
+  for (int j = 0; j < 8; j++) {
+    c[j] = hh[lane * 8 + j];
+    sum += c[j];
+  }
+  unsigned incl = sum;
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  unsigned excl = incl - sum;
+  unsigned kk = (unsigned)s.k;
+  bool mine = (excl <= kk) && (kk < incl);
+  unsigned ballot = __ballot_sync(0xffffffffu, mine);
+  int owner = __ffs(ballot) - 1;
+  if (lane == owner) {
+    unsigned before = excl;
+    int digit = lane * 8;
+    for (int j = 0; j < 8; j++) {
+      if (kk < before + c[j]) {
+        digit = lane * 8 + j;
+        break;
+      }
+      before += c[j];
+    }
+    s.k = (int)(kk - before);
+    s.n_less += (int)before;
+    s.prefix |= ((unsigned long long)digit) << shift;
+    s.mask |= byte_mask;
+    g[gi].k = s.k;
+    g[gi].n_less = s.n_less;
+    g[gi].prefix = s.prefix;
+    g[gi].mask = s.mask;
+  }
+  __syncwarp();
+  for (int j = 0; j < 8; j++) hh[lane * 8 + j] = 0;
+}
+
+__device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned* tot, unsigned* wsum) {
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned incl = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) wsum[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    unsigned x = lane < kThreads / 32 ? wsum[lane] : 0;
+    unsigned xi = x;
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned t = __shfl_up_sync(0xffffffffu, xi, o);
+      if (lane >= o) xi += t;
+    }
+    if (lane < kThreads / 32) wsum[lane] = xi - x;
+    if (lane == kThreads / 32 - 1) *tot = xi;
+  }
+  __syncthreads();
+  unsigned r = incl - v + wsum[w];
+  __syncthreads();
+  return r;
+}
+
+// Per chunk: how many keys are below / equal to the median key.
+__global__ void __launch_bounds__(kThreads) k_count(const Chunk* __restrict__ chunks,
+                                                    const GNode* __restrict__ g, const double* X,
+                                                    const double* Y, const double* Z,
+                                                    unsigned* cnt_less, unsigned* cnt_eq) {
+  Chunk c = chunks[blockIdx.x];
+  const GNode& s = g[c.g];
+  unsigned long long piv = s.prefix;
+  unsigned a = 0, e = 0;
+  for (int i = threadIdx.x; i < c.len; i += kThreads) {
+    unsigned long long key = okey(coord_of(X, Y, Z, s.dim, c.start + i));
+    a += key < piv;
+    e += key == piv;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    e += __shfl_xor_sync(0xffffffffu, e, o);
+  }
+  __shared__ unsigned sa[kThreads / 32], se[kThreads / 32];
+  if ((threadIdx.x & 31) == 0) {
+    sa[threadIdx.x >> 5] = a;
+    se[threadIdx.x >> 5] = e;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned ta = 0, te = 0;
+    for (int i = 0; i < kThreads / 32; i++) {
+      ta += sa[i];
+      te += se[i];
+    }
+    cnt_less[blockIdx.x] = ta;
+    cnt_eq[blockIdx.x] = te;
+  }
+}
+
+// One block per node: exclusive scan of the chunk counts (chunk order), the split value,
+// and the number of equal keys that go left.
+__global__ void __launch_bounds__(kThreads) k_chunk_scan(GNode* g, const unsigned* cnt_less,
+                                                         const unsigned* cnt_eq,
+                                                         unsigned* base_less, unsigned* base_eq,
+                                                         NodeX* nodex) {
+  __shared__ unsigned wsum[32];
+  __shared__ unsigned tot;
+  GNode s = g[blockIdx.x];
+  unsigned run_l = 0, run_e = 0;
+  for (int c0 = 0; c0 < s.nchunks; c0 += kThreads) {
+    int c = c0 + threadIdx.x;
+    unsigned vl = c < s.nchunks ? cnt_less[s.first_chunk + c] : 0;
+    unsigned ve = c < s.nchunks ? cnt_eq[s.first_chunk + c] : 0;
+    unsigned el = block_excl_scan(vl, &tot, wsum);
+    unsigned tl = tot;
+    unsigned ee = block_excl_scan(ve, &tot, wsum);
+    unsigned te = tot;
+    if (c < s.nchunks) {
+      base_less[s.first_chunk + c] = run_l + el;
+      base_eq[s.first_chunk + c] = run_e + ee;
+    }
+    run_l += tl;
+    run_e += te;
+  }
+  if (threadIdx.x == 0) {
+    // after selection n_less counts every key below the median key; rank k + 1 particles
+    // go left: all of those plus (k_total + 1 - n_less) equal keys.
+    int ktot = (s.size - 1) / 2;
+    g[blockIdx.x].need_eq = ktot + 1 - (int)run_l;
+    g[blockIdx.x].total_eq = (int)run_e;
+    g[blockIdx.x].n_less = (int)run_l;
+    nodex[s.node].split_val = okey_inv(s.prefix);
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_scatter(const Chunk* __restrict__ chunks,
+                                                      const GNode* __restrict__ g,
+                                                      const double* X, const double* Y,
+                                                      const double* Z, const int* ID, double* X2,
+                                                      double* Y2, double* Z2, int* ID2,
+                                                      const unsigned* base_less,
+                                                      const unsigned* base_eq, int* err) {
+  __shared__ unsigned wsum[32];
+  __shared__ unsigned tot;
+  Chunk c = chunks[blockIdx.x];
+  const GNode s = g[c.g];
+  unsigned long long piv = s.prefix;
+  unsigned bl = base_less[blockIdx.x], be = base_eq[blockIdx.x];
+  unsigned bg = (unsigned)c.off - bl - be;  // greater keys before this chunk
+  int kleft = (s.size - 1) / 2 + 1;
+  int right0 = s.start + kleft;
+  int excess = s.total_eq - s.need_eq;
+  unsigned run_l = 0, run_e = 0, run_g = 0;
+  for (int r = 0; r < kRounds; r++) {
+    int i = r * kThreads + threadIdx.x;
+    bool valid = i < c.len;
+    unsigned long long key = 0;
+    int p = c.start + i;
+    if (valid) key = okey(coord_of(X, Y, Z, s.dim, p));
+    unsigned fl = valid && key < piv, fe = valid && key == piv, fg = valid && key > piv;
+    unsigned el = block_excl_scan(fl, &tot, wsum);
+    unsigned tl = tot;
+    unsigned ee = block_excl_scan(fe, &tot, wsum);
+    unsigned te = tot;
+    unsigned eg = block_excl_scan(fg, &tot, wsum);
+    unsigned tg = tot;
+    if (valid) {
+      int dst;
+      if (fl) {
+        dst = s.start + (int)(bl + run_l + el);
+      } else if (fe) {
+        int e = (int)(be + run_e + ee);
+        dst = e < s.need_eq ? s.start + s.n_less + e : right0 + (e - s.need_eq);
+      } else {
+        dst = right0 + excess + (int)(bg + run_g + eg);
+      }
+      if (dst < s.start || dst >= s.start + s.size) {  // selection inconsistent: report
+        atomicExch(err, 2);
+        dst = p;
+      }
+      X2[dst] = X[p];
+      Y2[dst] = Y[p];
+      Z2[dst] = Z[p];
+      ID2[dst] = ID[p];
+    }
+    run_l += tl;
+    run_e += te;
+    run_g += tg;
+  }
+}
+
+// ---- phase 2: one CTA per subtree of at most kLocalMax particles
+struct LNode {
+  int start;  // local start
+  int size;
+  int h;      // heap index within the tree
+  int dim;    // -1 leaf
+};
+
+__global__ void __launch_bounds__(kThreads) k_local_build(
+    const LRoot* __restrict__ roots, const double* Xa, const double* Ya, const double* Za,
+    const int* IDa, const double* Xb, const double* Yb, const double* Zb, const int* IDb,
+    const double* __restrict__ mass_in, const double* __restrict__ vel_in, int b,
+    NodeRec* node, NodeX* nodex, P4* pos, float4* posf, V4* vel, int* perm) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  double* cx = (double*)smem;
+  double* cy = cx + kLocalMax;
+  double* cz = cy + kLocalMax;
+  unsigned long long* skey = (unsigned long long*)(cz + kLocalMax);
+  int* id = (int*)(skey + kSortCap);
+  unsigned short* sidx = (unsigned short*)(id + kLocalMax);
+  unsigned short* src = sidx + kSortCap;
+  LNode* lv = (LNode*)(src + kLocalMax);
+  LNode* lv2 = lv + kLevelCap;
+  __shared__ int n_cur, n_split, max_split;
+
+  const LRoot R = roots[blockIdx.x];
+  const double* X = R.buf ? Xb : Xa;
+  const double* Y = R.buf ? Yb : Ya;
+  const double* Z = R.buf ? Zb : Za;
+  const int* I = R.buf ? IDb : IDa;
+  for (int e = threadIdx.x; e < R.size; e += kThreads) {
+    cx[e] = X[R.start + e];
+    cy[e] = Y[R.start + e];
+    cz[e] = Z[R.start + e];
+    id[e] = I[R.start + e];
+  }
+  if (threadIdx.x == 0) {
+    lv[0].start = 0;
+    lv[0].size = R.size;
+    lv[0].h = R.h;
+    lv[0].dim = -1;
+    n_cur = 1;
+  }
+  __syncthreads();
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  while (true) {
+    // A: bounding box and split dimension of every node of this level (warp per node)
+    for (int j = warp; j < n_cur; j += kThreads / 32) {
+      LNode nd = lv[j];
+      double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
+      for (int e = nd.start + lane; e < nd.start + nd.size; e += 32) {
+        lo[0] = fmin(lo[0], cx[e]);
+        hi[0] = fmax(hi[0], cx[e]);
+        lo[1] = fmin(lo[1], cy[e]);
+        hi[1] = fmax(hi[1], cy[e]);
+        lo[2] = fmin(lo[2], cz[e]);
+        hi[2] = fmax(hi[2], cz[e]);
+      }
+      for (int d = 0; d < 3; d++) {
+        for (int o = 16; o > 0; o >>= 1) {
+          lo[d] = fmin(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+          hi[d] = fmax(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+        }
+      }
+      if (lane == 0) {
+        int dim = -1;
+        if (nd.size > b) {
+          dim = 0;
+          double cur = dsub(hi[0], lo[0]);
+          for (int d = 1; d < 3; d++) {
+            double sp = dsub(hi[d], lo[d]);
+            if (sp > cur) {
+              dim = d;
+              cur = sp;
+            }
+          }
+        }
+        lv[j].dim = dim;
+        write_node(node, nodex, R.nbase + nd.h, lo, hi, R.start + nd.start, nd.size, dim, 0.0);
+      }
+    }
+    if (threadIdx.x == 0) {
+      n_split = 0;
+      max_split = 0;
+    }
+    __syncthreads();
+    // compact the split nodes to the front of lv2 (order preserved) and size the network
+    if (threadIdx.x == 0) {
+      int ns = 0, mx = 0;
+      for (int j = 0; j < n_cur; j++)
+        if (lv[j].dim >= 0) {
+          lv2[ns++] = lv[j];
+          mx = max(mx, lv[j].size);
+        }
+      n_split = ns;
+      max_split = mx;
+    }
+    __syncthreads();
+    if (n_split == 0) break;
+    int P = 1;
+    while (P < max_split) P <<= 1;
+    int total = n_split * P;
+    // B: fill sort keys (split-dimension key, local index); pad with +inf
+    for (int t = threadIdx.x; t < total; t += kThreads) {
+      int j = t / P, r = t - j * P;
+      LNode nd = lv2[j];
+      if (r < nd.size) {
+        int e = nd.start + r;
+        double v = nd.dim == 0 ? cx[e] : (nd.dim == 1 ? cy[e] : cz[e]);
+        skey[t] = okey(v);
+        sidx[t] = (unsigned short)e;
+      } else {
+        skey[t] = ~0ull;
+        sidx[t] = 0xffff;
+      }
+    }
+    for (int e = threadIdx.x; e < R.size; e += kThreads) src[e] = (unsigned short)e;
+    __syncthreads();
+    for (int kk = 2; kk <= P; kk <<= 1) {
+      for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+        for (int t = threadIdx.x; t < total; t += kThreads) {
+          int u = t ^ jj;
+          if (u > t) {
+            bool up = (t & kk) == 0;
+            unsigned long long a = skey[t], c = skey[u];
+            unsigned short ia = sidx[t], ic = sidx[u];
+            bool gt = (a > c) || (a == c && ia > ic);
+            if (gt == up) {
+              skey[t] = c;
+              skey[u] = a;
+              sidx[t] = ic;
+              sidx[u] = ia;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    }
+    // C: new order inside each split node = sorted order
+    for (int t = threadIdx.x; t < total; t += kThreads) {
+      int j = t / P, r = t - j * P;
+      LNode nd = lv2[j];
+      if (r < nd.size) src[nd.start + r] = sidx[t];
+    }
+    __syncthreads();
+    double* tmp = (double*)skey;  // keys are no longer needed
+    for (int a = 0; a < 3; a++) {
+      double* arr = a == 0 ? cx : (a == 1 ? cy : cz);
+      for (int e = threadIdx.x; e < R.size; e += kThreads) tmp[e] = arr[src[e]];
+      __syncthreads();
+      for (int e = threadIdx.x; e < R.size; e += kThreads) arr[e] = tmp[e];
+      __syncthreads();
+    }
+    {
+      int* itmp = (int*)skey;
+      for (int e = threadIdx.x; e < R.size; e += kThreads) itmp[e] = id[src[e]];
+      __syncthreads();
+      for (int e = threadIdx.x; e < R.size; e += kThreads) id[e] = itmp[e];
+      __syncthreads();
+    }
+    // D: split values and the next level
+    if (threadIdx.x == 0) {
+      int nn = 0;
+      for (int j = 0; j < n_split; j++) {
+        LNode nd = lv2[j];
+        int kl = (nd.size - 1) / 2 + 1;
+        int m = nd.start + kl - 1;
+        double v = nd.dim == 0 ? cx[m] : (nd.dim == 1 ? cy[m] : cz[m]);
+        nodex[R.nbase + nd.h].split_val = v;
+        LNode l = {nd.start, kl, 2 * nd.h + 1, -1};
+        LNode r = {nd.start + kl, nd.size - kl, 2 * nd.h + 2, -1};
+        lv[nn++] = l;
+        lv[nn++] = r;
+      }
+      n_cur = nn;
+    }
+    __syncthreads();
+  }
+  // final tree-order arrays
+  for (int e = threadIdx.x; e < R.size; e += kThreads) {
+    int t = R.start + e;
+    int ii = id[e];
+    double m = mass_in ? mass_in[ii] : 1.0;
+    P4 p;
+    p.x = cx[e];
+    p.y = cy[e];
+    p.z = cz[e];
+    p.m = m;
+    pos[t] = p;
+    posf[t] = make_float4(__double2float_rn(cx[e]), __double2float_rn(cy[e]),
+                          __double2float_rn(cz[e]), 0.f);
+    perm[t] = ii;
+    if (vel && vel_in) vel[t] = make_v4(vel_in[3 * ii], vel_in[3 * ii + 1], vel_in[3 * ii + 2], 0.0);
+  }
+}
+
+int depth_of(int64_t n, int b) {
+  int d = 0;
+  while (n > b) {
+    n = (n - 1) / 2 + 1;
+    d++;
+  }
+  return d;
+}
+
+}  // namespace
+
+size_t local_build_smem() {
+  return sizeof(double) * 3 * kLocalMax + sizeof(unsigned long long) * kSortCap +
+         sizeof(int) * kLocalMax + sizeof(unsigned short) * (kSortCap + kLocalMax) +
+         sizeof(LNode) * 2 * kLevelCap;
+}
+
+int64_t heap_slots(int64_t n, int b) {
+  int d = depth_of(n, b);
+  return (int64_t(1) << (d + 1)) - 1;
+}
+
+int64_t count_nodes(int64_t n, int b) {
+  if (n <= b) return 1;
+  int64_t l = (n - 1) / 2 + 1;
+  return 1 + count_nodes(l, b) + count_nodes(n - l, b);
+}
+
+// Build every tree of the forest. All arrays live on `st`. Returns NBK status.
+int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_in,
+                 const double* d_mass_in, const double* d_vel_in, BuiltArrays& out,
+                 DevAlloc& alloc, cudaStream_t st) {
+  Phase ph("build", st);
+  int64_t ntot = 0;
+  for (auto& t : trees) ntot = std::max<int64_t>(ntot, t.pstart + t.n);
+  if (ntot == 0) return NBK_OK;
+  double *Xa, *Ya, *Za, *Xb, *Yb, *Zb;
+  int *IDa, *IDb, *d_err;
+  NBK_TRY(alloc.get((void**)&Xa, sizeof(double) * ntot));
+  NBK_TRY(alloc.get((void**)&Ya, sizeof(double) * ntot));
+  NBK_TRY(alloc.get((void**)&Za, sizeof(double) * ntot));
+  NBK_TRY(alloc.get((void**)&Xb, sizeof(double) * ntot));
+  NBK_TRY(alloc.get((void**)&Yb, sizeof(double) * ntot));
+  NBK_TRY(alloc.get((void**)&Zb, sizeof(double) * ntot));
+  NBK_TRY(alloc.get((void**)&IDa, sizeof(int) * ntot));
+  NBK_TRY(alloc.get((void**)&IDb, sizeof(int) * ntot));
+  NBK_TRY(alloc.get((void**)&d_err, sizeof(int)));
+  NBK_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+  k_init_soa<<<(unsigned)((ntot + 255) / 256), 256, 0, st>>>(d_pos_in, Xa, Ya, Za, IDa, ntot, d_err); note_launch();
+  NBK_CUDA_TRY(cudaGetLastError());
+
+  // host plan of the global levels and of the local subtree roots
+  std::vector<LRoot> lroots;
+  struct HN {
+    int64_t start, size;
+    int h, nbase;
+  };
+  std::vector<HN> cur, nxt;
+  for (auto& t : trees) {
+    if (t.n <= 0) continue;
+    if (t.n <= kLocalMax) lroots.push_back({(int)t.pstart, (int)t.n, t.nbase, 0, 0, 0});
+    else cur.push_back({t.pstart, t.n, 0, t.nbase});
+  }
+  int buf = 0;  // buffer holding the current level's particles
+  std::vector<GNode> gn;
+  std::vector<Chunk> ch;
+  GNode* d_g = nullptr;
+  Chunk* d_c = nullptr;
+  unsigned *d_hist = nullptr, *d_cl = nullptr, *d_ce = nullptr, *d_bl = nullptr, *d_be = nullptr;
+  size_t cap_g = 0, cap_c = 0;
+  while (!cur.empty()) {
+    gn.clear();
+    ch.clear();
+    for (size_t i = 0; i < cur.size(); i++) {
+      GNode g{};
+      g.start = (int)cur[i].start;
+      g.size = (int)cur[i].size;
+      g.node = cur[i].nbase + cur[i].h;
+      g.first_chunk = (int)ch.size();
+      int nc = (int)((cur[i].size + kChunk - 1) / kChunk);
+      g.nchunks = nc;
+      for (int c = 0; c < nc; c++) {
+        int off = c * kChunk;
+        int len = (int)std::min<int64_t>(kChunk, cur[i].size - off);
+        ch.push_back({(int)i, (int)(cur[i].start + off), len, off});
+      }
+      gn.push_back(g);
+    }
+    int ng = (int)gn.size(), nc = (int)ch.size();
+    if ((size_t)ng > cap_g) {
+      cap_g = std::max<size_t>(ng, 2 * cap_g);
+      NBK_TRY(alloc.get((void**)&d_g, sizeof(GNode) * cap_g));
+      NBK_TRY(alloc.get((void**)&d_hist, sizeof(unsigned) * 256 * cap_g));
+      NBK_CUDA_TRY(cudaMemsetAsync(d_hist, 0, sizeof(unsigned) * 256 * cap_g, st));
+    }
+    if ((size_t)nc > cap_c) {
+      cap_c = std::max<size_t>(nc, 2 * cap_c);
+      NBK_TRY(alloc.get((void**)&d_c, sizeof(Chunk) * cap_c));
+      NBK_TRY(alloc.get((void**)&d_cl, sizeof(unsigned) * cap_c));
+      NBK_TRY(alloc.get((void**)&d_ce, sizeof(unsigned) * cap_c));
+      NBK_TRY(alloc.get((void**)&d_bl, sizeof(unsigned) * cap_c));
+      NBK_TRY(alloc.get((void**)&d_be, sizeof(unsigned) * cap_c));
+    }
+    NBK_TRY(alloc.upload(d_g, gn.data(), sizeof(GNode) * ng, st));
+    NBK_TRY(alloc.upload(d_c, ch.data(), sizeof(Chunk) * nc, st));
+    const double* X = buf ? Xb : Xa;
+    const double* Y = buf ? Yb : Ya;
+    const double* Z = buf ? Zb : Za;
+    const int* I = buf ? IDb : IDa;
+    double* X2 = buf ? Xa : Xb;
+    double* Y2 = buf ? Ya : Yb;
+    double* Z2 = buf ? Za : Zb;
+    int* I2 = buf ? IDa : IDb;
+    k_gnode_reset<<<(ng + 127) / 128, 128, 0, st>>>(d_g, ng); note_launch();
+    k_bbox<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z); note_launch();
+    k_gnode_split<<<(ng + 127) / 128, 128, 0, st>>>(d_g, ng, out.node, out.nodex); note_launch();
+    for (int pass = 0; pass < 8; pass++) {
+      int shift = 56 - 8 * pass;
+      k_hist<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, d_hist, shift); note_launch();
+      k_select<<<(ng + 3) / 4, 128, 0, st>>>(d_g, ng, d_hist, shift); note_launch();
+    }
+    k_count<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, d_cl, d_ce); note_launch();
+    k_chunk_scan<<<ng, kThreads, 0, st>>>(d_g, d_cl, d_ce, d_bl, d_be, out.nodex); note_launch();
+    k_scatter<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, I, X2, Y2, Z2, I2, d_bl, d_be, d_err); note_launch();
+    NBK_CUDA_TRY(cudaGetLastError());
+    buf ^= 1;
+    nxt.clear();
+    for (auto& c : cur) {
+      int64_t l = (c.size - 1) / 2 + 1;
+      HN L = {c.start, l, 2 * c.h + 1, c.nbase};
+      HN Rr = {c.start + l, c.size - l, 2 * c.h + 2, c.nbase};
+      for (HN x : {L, Rr}) {
+        if (x.size <= kLocalMax) lroots.push_back({(int)x.start, (int)x.size, x.nbase, x.h, buf, 0});
+        else nxt.push_back(x);
+      }
+    }
+    cur.swap(nxt);
+  }
+  if (!lroots.empty()) {
+    LRoot* d_r;
+    NBK_TRY(alloc.get((void**)&d_r, sizeof(LRoot) * lroots.size()));
+    NBK_TRY(alloc.upload(d_r, lroots.data(), sizeof(LRoot) * lroots.size(), st));
+    size_t sm = local_build_smem();
+    static bool attr_set = false;
+    if (!attr_set) {
+      NBK_CUDA_TRY(cudaFuncSetAttribute(k_local_build, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)sm));
+      attr_set = true;
+    }
+    k_local_build<<<(unsigned)lroots.size(), kThreads, sm, st>>>(
+        d_r, Xa, Ya, Za, IDa, Xb, Yb, Zb, IDb, d_mass_in, d_vel_in, b, out.node, out.nodex,
+        out.pos, out.posf, out.vel, out.perm); note_launch();
+    NBK_CUDA_TRY(cudaGetLastError());
+  }
+  int h_err = 0;
+  NBK_CUDA_TRY(cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  NBK_CUDA_TRY(cudaStreamSynchronize(st));
+  alloc.release_all_scratch(st);
+  if (h_err == 1) {
+    set_error("input positions contain NaN or infinity");
+    return NBK_ERR_INVALID;
+  }
+  if (h_err) {
+    set_error("tree build: median partition inconsistent (device check)");
+    return NBK_ERR_DEVICE;
+  }
+  return NBK_OK;
+}
+
+}  // namespace nbk

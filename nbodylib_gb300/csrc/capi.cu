@@ -1,0 +1,887 @@
+// extern "C" entry points of libnbkdt (declared in include/nbkdt.h).
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+
+#include "nbk_build.h"
+
+namespace nbk {
+
+namespace {
+thread_local std::string g_err;
+
+bool g_pool_ready = false;
+void ensure_pool() {
+  if (g_pool_ready) return;
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t thr = ~0ull;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+  }
+  g_pool_ready = true;
+}
+
+// The smoothing kernels of src/KDTree/SmoothingKernels.h:32-56 (evaluated on the host
+// once, to build the table the GPU interpolates).
+double w_sph(double r, double h) {
+  double rh = r / h;
+  if (rh <= 1.0) return (1.0 - 0.75 * (2.0 - rh) * (rh * rh));
+  else if (rh > 1.0 && rh <= 2.0) return 0.25 * (2.0 - rh) * (2.0 - rh) * (2.0 - rh);
+  return 0;
+}
+double w_th(double r, double h) { return (r / h * 0.5 <= 1.0); }
+double w_gauss(double r, double h) {
+  double rh = r / h * 2.0;
+  return std::exp(-0.5 * std::pow(rh, 2.0));
+}
+double w_epan(double r, double h) {
+  double rh = r / h * 0.5;
+  return rh <= 1.0 ? (1.0 - rh * rh) : 0.;
+}
+
+// KDTree::KernelConstruction (KDTree.cxx:1144-1183) for ND dimensions; Gamma(ND/2+1)
+// from std::tgamma.
+void kernel_table(int kerntype, int kernres, int nd, std::vector<double>& T, double& norm) {
+  double kn = 1.0 / nd * std::pow(M_1_PI, nd / 2.) * std::tgamma(nd / 2. + 1.);
+  double (*f)(double, double) = w_sph;
+  if (kerntype == NBK_KGAUSS) {
+    f = w_gauss;
+    kn *= std::pow(0.5 * M_1_PI, nd / 2.);
+  } else if (kerntype == NBK_KEPAN) {
+    f = w_epan;
+    kn *= nd * (nd + 2.) * std::pow(0.5, nd + 1.);
+  } else if (kerntype == NBK_KTH) {
+    f = w_th;
+  } else {
+    f = w_sph;
+    kn *= nd * (nd + 1.) * (nd + 2.) * (nd + 3.) / (6 * (std::pow(2., nd + 1) - 1.));
+  }
+  norm = kn;
+  double delta = 2.0 / (double)(kernres - 1);
+  T.resize(kernres);
+  for (int i = 0; i < kernres; i++) T[i] = kn * f(i * delta, 1.0);
+}
+
+__global__ void k_scatter_d(const double* tv, const int* perm, double* out, int64_t n,
+                            int stride) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int64_t o = perm[i];
+  for (int s = 0; s < stride; s++) out[o * stride + s] = tv[i * stride + s];
+}
+__global__ void k_scatter_i(const int* tv, const int* perm, int* out, int64_t n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[perm[i]] = tv[i];
+}
+}  // namespace
+
+void set_error(const std::string& msg) { g_err = msg; }
+const char* get_error() { return g_err.c_str(); }
+
+static std::atomic<long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+namespace {
+struct PendingPhase {
+  std::string name;
+  cudaEvent_t a, b;
+};
+struct TraceAcc {
+  long long count = 0;
+  double ms = 0;
+};
+std::mutex g_trace_mu;
+std::atomic<bool> g_trace_on{false};
+std::vector<PendingPhase> g_pending;
+std::map<std::string, TraceAcc> g_trace;
+
+void resolve_pending() {
+  std::lock_guard<std::mutex> lk(g_trace_mu);
+  for (auto& p : g_pending) {
+    cudaEventSynchronize(p.b);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    auto& acc = g_trace[p.name];
+    acc.count++;
+    acc.ms += ms;
+    cudaEventDestroy(p.a);
+    cudaEventDestroy(p.b);
+  }
+  g_pending.clear();
+}
+}  // namespace
+
+Phase::Phase(const char* n, cudaStream_t s) : name(n), st(s) {
+  if (!g_trace_on.load(std::memory_order_relaxed)) return;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  cudaEventRecord(a, st);
+}
+Phase::~Phase() {
+  if (!a) return;
+  cudaEventRecord(b, st);
+  std::lock_guard<std::mutex> lk(g_trace_mu);
+  g_pending.push_back({name, a, b});
+}
+
+int dev_malloc(void** p, size_t bytes, cudaStream_t st) {
+  ensure_pool();
+  cudaError_t e = cudaMallocAsync(p, std::max<size_t>(bytes, 16), st);
+  if (e != cudaSuccess) {
+    set_error(std::string("device allocation of ") + std::to_string(bytes) +
+              " bytes failed: " + cudaGetErrorString(e));
+    *p = nullptr;
+    return NBK_ERR_NOMEM;
+  }
+  return NBK_OK;
+}
+void dev_free(void* p, cudaStream_t st) {
+  if (p) cudaFreeAsync(p, st);
+}
+int DevAlloc::get(void** p, size_t bytes) {
+  NBK_TRY(dev_malloc(p, bytes, st));
+  scratch.push_back(*p);
+  return NBK_OK;
+}
+int DevAlloc::upload(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  NBK_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+  return NBK_OK;
+}
+void DevAlloc::release_all_scratch(cudaStream_t s) {
+  for (void* p : scratch) dev_free(p, s);
+  scratch.clear();
+}
+DevAlloc::~DevAlloc() { release_all_scratch(st); }
+
+int scatter_to_input_order(const double* tree_vals, const int* perm, double* out, int64_t n,
+                           int stride, cudaStream_t st) {
+  if (n == 0) return NBK_OK;
+  k_scatter_d<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(tree_vals, perm, out, n, stride); note_launch();
+  NBK_CUDA_TRY(cudaGetLastError());
+  return NBK_OK;
+}
+
+}  // namespace nbk
+
+using namespace nbk;
+
+struct nbk_tree {
+  int64_t n = 0;
+  int b = 16, treetype = 0, kerntype = 0, kernres = 1000;
+  bool periodic = false;
+  double period[3] = {0, 0, 0};
+  unsigned flags = 0;
+  cudaStream_t st = nullptr;
+  bool has_vel = false;
+  BuiltArrays arr;
+  int64_t nslots = 0, numnodes = 0, numleaves = 0;
+  std::vector<double> h_kernel;
+  double kernnorm = 0;
+  double* d_kernel = nullptr;
+  float eps = 0;
+  int* d_err = nullptr;
+  bool dev() const { return flags & NBK_DEVICE_PTRS; }
+  TreeView view() const {
+    TreeView v{};
+    v.pos = arr.pos;
+    v.posf = arr.posf;
+    v.vel = arr.vel;
+    v.perm = arr.perm;
+    v.node = arr.node;
+    v.nodex = arr.nodex;
+    v.n = (int)n;
+    v.pstart = 0;
+    v.nbase = 0;
+    v.b = b;
+    // a tree that is a single leaf searches without images (KDLeafNode.cxx:658-661)
+    v.periodic = (periodic && n > b) ? 1 : 0;
+    for (int d = 0; d < 3; d++) v.period[d] = period[d];
+    v.eps = eps;
+    return v;
+  }
+};
+
+#define API_BEGIN try {
+#define API_END                                          \
+  }                                                      \
+  catch (const std::exception& e) {                      \
+    set_error(std::string("exception: ") + e.what());    \
+    return NBK_ERR_INVALID;                              \
+  }
+
+namespace {
+
+// Device staging for one call: host pointers are copied in/out, device pointers used as
+// they are.
+struct Stage {
+  nbk_tree* t;
+  DevAlloc alloc;
+  std::vector<std::pair<void*, std::pair<void*, size_t>>> outs;  // (host, (dev, bytes))
+  explicit Stage(nbk_tree* tt) : t(tt) { alloc.st = tt->st; }
+  template <class T>
+  int in(const T* host_or_dev, size_t count, const T** dev) {
+    if (t->dev() || host_or_dev == nullptr) {
+      *dev = host_or_dev;
+      return NBK_OK;
+    }
+    T* d;
+    NBK_TRY(alloc.get((void**)&d, sizeof(T) * count));
+    NBK_CUDA_TRY(cudaMemcpyAsync(d, host_or_dev, sizeof(T) * count, cudaMemcpyHostToDevice, t->st));
+    *dev = d;
+    return NBK_OK;
+  }
+  template <class T>
+  int out(T* host_or_dev, size_t count, T** dev, bool copy_existing = false) {
+    if (t->dev()) {
+      *dev = host_or_dev;
+      return NBK_OK;
+    }
+    T* d;
+    NBK_TRY(alloc.get((void**)&d, sizeof(T) * count));
+    if (copy_existing)
+      NBK_CUDA_TRY(cudaMemcpyAsync(d, host_or_dev, sizeof(T) * count, cudaMemcpyHostToDevice, t->st));
+    outs.push_back({(void*)host_or_dev, {(void*)d, sizeof(T) * count}});
+    *dev = d;
+    return NBK_OK;
+  }
+  int finish() {
+    for (auto& o : outs)
+      NBK_CUDA_TRY(cudaMemcpyAsync(o.first, o.second.first, o.second.second,
+                                   cudaMemcpyDeviceToHost, t->st));
+    if (!t->dev()) NBK_CUDA_TRY(cudaStreamSynchronize(t->st));
+    return NBK_OK;
+  }
+};
+
+int check_err(nbk_tree* t, const char* what) {
+  int h = 0;
+  NBK_CUDA_TRY(cudaMemcpyAsync(&h, t->d_err, sizeof(int), cudaMemcpyDeviceToHost, t->st));
+  NBK_CUDA_TRY(cudaStreamSynchronize(t->st));
+  if (h == kErrTooFew) {
+    set_error(std::string(what) + ": fewer than k neighbours were found for some particle");
+    return NBK_ERR_TOO_FEW;
+  }
+  if (h) {
+    set_error(std::string(what) + ": device bound exceeded (code " + std::to_string(h) + ")");
+    return NBK_ERR_DEVICE;
+  }
+  return NBK_OK;
+}
+
+int clear_err(nbk_tree* t) {
+  NBK_CUDA_TRY(cudaMemsetAsync(t->d_err, 0, sizeof(int), t->st));
+  return NBK_OK;
+}
+
+KnnArgs base_args(nbk_tree* t) {
+  KnnArgs a{};
+  a.tv = t->view();
+  a.kernel = t->d_kernel;
+  a.kernres = t->kernres;
+  a.err = t->d_err;
+  return a;
+}
+
+int check_tree(const nbk_tree* t) {
+  if (!t) {
+    set_error("null tree handle");
+    return NBK_ERR_INVALID;
+  }
+  return NBK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* nbk_last_error(void) { return get_error(); }
+
+long long nbk_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int nbk_trace_enable(int on) {
+  g_trace_on.store(on != 0);
+  return NBK_OK;
+}
+
+int nbk_trace_reset(void) {
+  resolve_pending();
+  std::lock_guard<std::mutex> lk(g_trace_mu);
+  g_trace.clear();
+  return NBK_OK;
+}
+
+int64_t nbk_trace_json(char* buf, int64_t cap) {
+  resolve_pending();
+  std::string s = "{";
+  {
+    std::lock_guard<std::mutex> lk(g_trace_mu);
+    bool first = true;
+    for (auto& kv : g_trace) {
+      char tmp[256];
+      snprintf(tmp, sizeof(tmp), "%s\"%s\": {\"count\": %lld, \"ms\": %.6f}", first ? "" : ", ",
+               kv.first.c_str(), kv.second.count, kv.second.ms);
+      s += tmp;
+      first = false;
+    }
+  }
+  s += "}";
+  if (buf && cap > 0) {
+    int64_t m = std::min<int64_t>(cap - 1, (int64_t)s.size());
+    memcpy(buf, s.data(), m);
+    buf[m] = 0;
+  }
+  return (int64_t)s.size() + 1;
+}
+
+const char* nbk_version(void) {
+  static std::string v;
+  int dev = 0;
+  cudaDeviceProp p{};
+  if (cudaGetDevice(&dev) == cudaSuccess && cudaGetDeviceProperties(&p, dev) == cudaSuccess)
+    v = std::string("nbkdt 0.1 sm_103a; device ") + p.name;
+  else
+    v = "nbkdt 0.1 sm_103a; no device";
+  return v.c_str();
+}
+
+int nbk_create(const double* pos, const double* vel, const double* mass, int64_t n,
+               int bucket_size, int treetype, int kerntype, int kernres,
+               int splitting_criterion, int aniso, int scale_space, const double* period,
+               unsigned flags, nbk_tree** out) {
+  API_BEGIN
+  if (!out || !pos) {
+    set_error("nbk_create: null pointer argument");
+    return NBK_ERR_INVALID;
+  }
+  *out = nullptr;
+  if (n < 1 || n > (int64_t)0x7fffff00) {
+    set_error("nbk_create: particle count must be in [1, 2^31)");
+    return NBK_ERR_INVALID;
+  }
+  if (bucket_size < 1) {
+    set_error("nbk_create: bucket size must be >= 1");
+    return NBK_ERR_INVALID;
+  }
+  if (bucket_size >= kLocalMax) {
+    set_error("nbk_create: bucket sizes >= 1024 are not supported on the GPU");
+    return NBK_ERR_UNSUPPORTED;
+  }
+  if (treetype != NBK_TPHYS) {
+    set_error("nbk_create: only the physical tree (TPHYS) runs on the GPU");
+    return NBK_ERR_UNSUPPORTED;
+  }
+  if (splitting_criterion != 0 || aniso != 0 || scale_space != 0) {
+    set_error("nbk_create: splitting criterion, anisotropic metric and space scaling other than 0 are not supported");
+    return NBK_ERR_UNSUPPORTED;
+  }
+  std::unique_ptr<nbk_tree> t(new nbk_tree);
+  t->n = n;
+  t->b = bucket_size;
+  t->treetype = treetype;
+  t->kerntype = (kerntype >= NBK_KSPH && kerntype <= NBK_KTH) ? kerntype : NBK_KSPH;
+  t->kernres = kernres < 100 ? 100 : kernres;  // KDTree.cxx:1145-1148
+  t->flags = flags;
+  if (period) {
+    double per[3];
+    if (flags & NBK_DEVICE_PTRS) {
+      NBK_CUDA_TRY(cudaMemcpy(per, period, sizeof(per), cudaMemcpyDeviceToHost));
+    } else {
+      memcpy(per, period, sizeof(per));
+    }
+    for (int d = 0; d < 3; d++) {
+      if (!(per[d] > 0)) {
+        set_error("nbk_create: period entries must be positive");
+        return NBK_ERR_INVALID;
+      }
+      t->period[d] = per[d];
+    }
+    t->periodic = true;
+  }
+  t->has_vel = vel != nullptr;
+  cudaStream_t st = t->st;
+  kernel_table(t->kerntype, t->kernres, 3, t->h_kernel, t->kernnorm);
+  NBK_TRY(dev_malloc((void**)&t->d_kernel, sizeof(double) * t->kernres, st));
+  NBK_CUDA_TRY(cudaMemcpyAsync(t->d_kernel, t->h_kernel.data(), sizeof(double) * t->kernres,
+                               cudaMemcpyHostToDevice, st));
+  NBK_TRY(dev_malloc((void**)&t->d_err, sizeof(int), st));
+  NBK_CUDA_TRY(cudaMemsetAsync(t->d_err, 0, sizeof(int), st));
+  t->nslots = heap_slots(n, bucket_size);
+  t->numnodes = count_nodes(n, bucket_size);
+  {
+    int64_t nl = 0;
+    // leaves = nodes - internal nodes; a binary tree has internal = leaves - 1
+    nl = (t->numnodes + 1) / 2;
+    t->numleaves = nl;
+  }
+  BuiltArrays& A = t->arr;
+  NBK_TRY(dev_malloc((void**)&A.pos, sizeof(P4) * n, st));
+  NBK_TRY(dev_malloc((void**)&A.posf, sizeof(float4) * n, st));
+  NBK_TRY(dev_malloc((void**)&A.perm, sizeof(int) * n, st));
+  if (vel) NBK_TRY(dev_malloc((void**)&A.vel, sizeof(V4) * n, st));
+  NBK_TRY(dev_malloc((void**)&A.node, sizeof(NodeRec) * t->nslots, st));
+  NBK_TRY(dev_malloc((void**)&A.nodex, sizeof(NodeX) * t->nslots, st));
+  NBK_CUDA_TRY(cudaMemsetAsync(A.node, 0, sizeof(NodeRec) * t->nslots, st));
+  NBK_CUDA_TRY(cudaMemsetAsync(A.nodex, 0, sizeof(NodeX) * t->nslots, st));
+  DevAlloc alloc;
+  alloc.st = st;
+  const double *d_pos = pos, *d_vel = vel, *d_mass = mass;
+  if (!(flags & NBK_DEVICE_PTRS)) {
+    double *a, *v = nullptr, *m = nullptr;
+    NBK_TRY(alloc.get((void**)&a, sizeof(double) * 3 * n));
+    NBK_CUDA_TRY(cudaMemcpyAsync(a, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+    if (vel) {
+      NBK_TRY(alloc.get((void**)&v, sizeof(double) * 3 * n));
+      NBK_CUDA_TRY(cudaMemcpyAsync(v, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
+    }
+    if (mass) {
+      NBK_TRY(alloc.get((void**)&m, sizeof(double) * n));
+      NBK_CUDA_TRY(cudaMemcpyAsync(m, mass, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    }
+    d_pos = a;
+    d_vel = v;
+    d_mass = m;
+  }
+  std::vector<TreeSpec> trees{{0, n, 0}};
+  NBK_TRY(build_forest(trees, bucket_size, d_pos, d_mass, d_vel, A, alloc, st));
+  // FP32 rounding bound for coordinates and image coordinates
+  NodeX root;
+  NBK_CUDA_TRY(cudaMemcpyAsync(&root, A.nodex, sizeof(NodeX), cudaMemcpyDeviceToHost, st));
+  NBK_CUDA_TRY(cudaStreamSynchronize(st));
+  double maxabs = 0;
+  for (int d = 0; d < 3; d++)
+    maxabs = std::max(maxabs, std::max(std::fabs(root.lo[d]), std::fabs(root.hi[d])));
+  double maxper = std::max(t->period[0], std::max(t->period[1], t->period[2]));
+  t->eps = (float)std::ldexp(maxabs + maxper, -23) * 1.0001f + 1e-38f;
+  alloc.release_all_scratch(st);
+  *out = t.release();
+  return NBK_OK;
+  API_END
+}
+
+int nbk_destroy(nbk_tree* t) {
+  if (!t) return NBK_OK;
+  cudaStream_t st = t->st;
+  dev_free(t->arr.pos, st);
+  dev_free(t->arr.posf, st);
+  dev_free(t->arr.vel, st);
+  dev_free(t->arr.perm, st);
+  dev_free(t->arr.node, st);
+  dev_free(t->arr.nodex, st);
+  dev_free(t->d_kernel, st);
+  dev_free(t->d_err, st);
+  cudaStreamSynchronize(st);
+  delete t;
+  return NBK_OK;
+}
+
+int nbk_set_stream(nbk_tree* t, void* stream) {
+  NBK_TRY(check_tree(t));
+  t->st = (cudaStream_t)stream;
+  return NBK_OK;
+}
+
+int nbk_sync(nbk_tree* t) {
+  NBK_TRY(check_tree(t));
+  NBK_CUDA_TRY(cudaStreamSynchronize(t->st));
+  return NBK_OK;
+}
+
+int nbk_get_counts(const nbk_tree* t, int64_t* numparts, int64_t* numnodes,
+                   int64_t* numleafnodes, int32_t* bucket_size) {
+  NBK_TRY(check_tree(t));
+  if (numparts) *numparts = t->n;
+  if (numnodes) *numnodes = t->numnodes;
+  if (numleafnodes) *numleafnodes = t->numleaves;
+  if (bucket_size) *bucket_size = t->b;
+  return NBK_OK;
+}
+
+int nbk_get_perm(const nbk_tree* t, int32_t* perm) {
+  NBK_TRY(check_tree(t));
+  if (!perm) {
+    set_error("nbk_get_perm: null output");
+    return NBK_ERR_INVALID;
+  }
+  NBK_CUDA_TRY(cudaMemcpyAsync(perm, t->arr.perm, sizeof(int) * t->n,
+                               t->dev() ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, t->st));
+  if (!t->dev()) NBK_CUDA_TRY(cudaStreamSynchronize(t->st));
+  return NBK_OK;
+}
+
+int nbk_get_kernel(const nbk_tree* t, double* table, double* kernnorm) {
+  NBK_TRY(check_tree(t));
+  if (table) memcpy(table, t->h_kernel.data(), sizeof(double) * t->kernres);
+  if (kernnorm) *kernnorm = t->kernnorm;
+  return NBK_OK;
+}
+
+int nbk_knn(nbk_tree* t, int k, int variant, int periodic_mode, int32_t* nn, double* d2) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  if (k < 1 || !nn || !d2) {
+    set_error("nbk_knn: k must be >= 1 and outputs non-null");
+    return NBK_ERR_INVALID;
+  }
+  if (variant != NBK_FINDNEAREST && variant != NBK_FINDNEARESTPOS) {
+    set_error("nbk_knn: unknown variant");
+    return NBK_ERR_INVALID;
+  }
+  Stage S(t);
+  int *dnn;
+  double* dd2;
+  NBK_TRY(S.out(nn, (size_t)t->n * k, &dnn));
+  NBK_TRY(S.out(d2, (size_t)t->n * k, &dd2));
+  NBK_TRY(clear_err(t));
+  KnnArgs a = base_args(t);
+  bool per = t->periodic;  // the heap grows by one whenever a period is set
+  a.kheap = per ? k + 1 : k;
+  a.kout = k;
+  a.drop_largest = (per && variant == NBK_FINDNEARESTPOS) ? 1 : 0;
+  a.periodic = a.tv.periodic;
+  a.exclude_self = a.tv.periodic ? 0 : 1;
+  a.min_image = periodic_mode == NBK_PERIODIC_MIN_IMAGE;
+  a.qmode = 0;
+  a.q0 = 0;
+  a.nq = (int)t->n;
+  a.nn = dnn;
+  a.d2 = dd2;
+  NBK_TRY(launch_knn(a, kEpiNN, t->st));
+  NBK_TRY(S.finish());
+  if (!t->dev()) NBK_TRY(check_err(t, "nbk_knn"));
+  return NBK_OK;
+  API_END
+}
+
+int nbk_knn_points(nbk_tree* t, const double* x, int64_t nq, int k, int periodic_mode,
+                   int32_t* nn, double* d2) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  if (k < 1 || !x || !nn || !d2 || nq < 0) {
+    set_error("nbk_knn_points: invalid argument");
+    return NBK_ERR_INVALID;
+  }
+  if (nq == 0) return NBK_OK;
+  Stage S(t);
+  const double* dx;
+  int* dnn;
+  double* dd2;
+  NBK_TRY(S.in(x, (size_t)nq * 3, &dx));
+  NBK_TRY(S.out(nn, (size_t)nq * k, &dnn));
+  NBK_TRY(S.out(d2, (size_t)nq * k, &dd2));
+  NBK_TRY(clear_err(t));
+  KnnArgs a = base_args(t);
+  a.kheap = k;
+  a.kout = k;
+  a.periodic = a.tv.periodic;
+  a.exclude_self = 0;
+  a.min_image = periodic_mode == NBK_PERIODIC_MIN_IMAGE;
+  a.qmode = 1;
+  a.qx = dx;
+  a.nq = (int)nq;
+  a.nn = dnn;
+  a.d2 = dd2;
+  NBK_TRY(launch_knn(a, kEpiNN, t->st));
+  NBK_TRY(S.finish());
+  if (!t->dev()) NBK_TRY(check_err(t, "nbk_knn_points"));
+  return NBK_OK;
+  API_END
+}
+
+static int density_common(nbk_tree* t, int k, int nsmooth, double* rho, double* vden, int epi) {
+  if (k < 1) {
+    set_error("density: k must be >= 1");
+    return NBK_ERR_INVALID;
+  }
+  if (k > t->n - 1) {
+    set_error("density: k = " + std::to_string(k) + " exceeds the " +
+              std::to_string(t->n - 1) + " other particles (the reference exits here)");
+    return NBK_ERR_TOO_FEW;
+  }
+  if ((epi == kEpiVel || epi == kEpiDensVel) && !t->has_vel) {
+    set_error("velocity density needs velocities at nbk_create");
+    return NBK_ERR_INVALID;
+  }
+  Stage S(t);
+  double *drho = nullptr, *dv = nullptr, *trho = nullptr, *tv = nullptr;
+  if (rho) NBK_TRY(S.out(rho, t->n, &drho));
+  if (vden) NBK_TRY(S.out(vden, t->n, &dv));
+  if (rho) {
+    NBK_TRY(S.alloc.get((void**)&trho, sizeof(double) * t->n));
+    NBK_CUDA_TRY(cudaMemsetAsync(trho, 0, sizeof(double) * t->n, t->st));
+  }
+  if (vden) NBK_TRY(S.alloc.get((void**)&tv, sizeof(double) * t->n));
+  NBK_TRY(clear_err(t));
+  KnnArgs a = base_args(t);
+  a.tv.periodic = 0;  // CalcDensity ignores the period (KDCalcSmoothQuantities.cxx:227)
+  a.kheap = k;
+  a.kout = k;
+  a.exclude_self = 1;
+  a.qmode = 0;
+  a.nq = (int)t->n;
+  a.nsmooth = nsmooth;
+  a.rho = trho;
+  a.vden = tv;
+  NBK_TRY(launch_knn(a, epi, t->st));
+  if (rho) NBK_TRY(scatter_to_input_order(trho, t->arr.perm, drho, t->n, 1, t->st));
+  if (vden) NBK_TRY(scatter_to_input_order(tv, t->arr.perm, dv, t->n, 1, t->st));
+  NBK_TRY(S.finish());
+  if (!t->dev()) NBK_TRY(check_err(t, "density"));
+  return NBK_OK;
+}
+
+int nbk_density(nbk_tree* t, int k, double* rho) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  if (!rho) {
+    set_error("nbk_density: null output");
+    return NBK_ERR_INVALID;
+  }
+  return density_common(t, k, k, rho, nullptr, kEpiDensity);
+  API_END
+}
+
+int nbk_veldensity(nbk_tree* t, int nsmooth, int nsearch, double* out) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  if (!out || nsmooth < 1) {
+    set_error("nbk_veldensity: invalid argument");
+    return NBK_ERR_INVALID;
+  }
+  if (nsmooth > nsearch) nsmooth = nsearch;  // KDCalcSmoothQuantities.cxx:319-322
+  return density_common(t, nsearch, nsmooth, nullptr, out, kEpiVel);
+  API_END
+}
+
+int nbk_density_veldensity(nbk_tree* t, int k, int nsmooth, double* rho, double* veldens) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  if (!rho || !veldens || nsmooth < 1) {
+    set_error("nbk_density_veldensity: invalid argument");
+    return NBK_ERR_INVALID;
+  }
+  if (nsmooth > k) nsmooth = k;
+  return density_common(t, k, nsmooth, rho, veldens, kEpiDensVel);
+  API_END
+}
+
+static int particles_common(nbk_tree* t, const int32_t* targets, int64_t nt, int k, int nsmooth,
+                            double* out, int epi) {
+  if (!targets || !out || nt < 0 || k < 1) {
+    set_error("invalid argument");
+    return NBK_ERR_INVALID;
+  }
+  if (k > t->n - 1) {
+    set_error("k exceeds the number of other particles");
+    return NBK_ERR_TOO_FEW;
+  }
+  if (epi == kEpiVelPart && !t->has_vel) {
+    set_error("velocity density needs velocities at nbk_create");
+    return NBK_ERR_INVALID;
+  }
+  if (nt == 0) return NBK_OK;
+  if (!t->dev()) {
+    for (int64_t i = 0; i < nt; i++)
+      if (targets[i] < 0 || targets[i] >= t->n) {
+        set_error("target index out of range");
+        return NBK_ERR_INVALID;
+      }
+  }
+  Stage S(t);
+  const int* dt;
+  double* dout;
+  NBK_TRY(S.in(targets, nt, &dt));
+  NBK_TRY(S.out(out, nt, &dout));
+  NBK_TRY(clear_err(t));
+  KnnArgs a = base_args(t);
+  a.tv.periodic = 0;
+  a.kheap = k;
+  a.kout = k;
+  a.exclude_self = 1;
+  a.qmode = 2;
+  a.qidx = dt;
+  a.nq = (int)nt;
+  a.nsmooth = nsmooth;
+  a.rho = dout;
+  a.vden = dout;
+  NBK_TRY(launch_knn(a, epi, t->st));
+  NBK_TRY(S.finish());
+  if (!t->dev()) NBK_TRY(check_err(t, "particle density"));
+  return NBK_OK;
+}
+
+int nbk_density_particles(nbk_tree* t, const int32_t* targets, int64_t nt, int k, double* out) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return particles_common(t, targets, nt, k, k, out, kEpiDensPart);
+  API_END
+}
+
+int nbk_veldensity_particles(nbk_tree* t, const int32_t* targets, int64_t nt, int nsmooth,
+                             int nsearch, double* out) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  if (nsmooth > nsearch) nsmooth = nsearch;
+  return particles_common(t, targets, nt, nsearch, nsmooth, out, kEpiVelPart);
+  API_END
+}
+
+static int ball_common(nbk_tree* t, int qmode, const int32_t* targets, const double* x,
+                       int64_t nq, double fdist2, int64_t* offsets, int32_t* out,
+                       int64_t out_capacity, int64_t* total) {
+  if (nq < 0 || !offsets || !total) {
+    set_error("ball search: invalid argument");
+    return NBK_ERR_INVALID;
+  }
+  Stage S(t);
+  const int* dt = nullptr;
+  const double* dx = nullptr;
+  if (qmode == 0) NBK_TRY(S.in(targets, nq, &dt));
+  else NBK_TRY(S.in(x, nq * 3, &dx));
+  int64_t* doff;
+  NBK_TRY(S.out(offsets, nq + 1, &doff));
+  int* dout = nullptr;
+  if (t->dev()) dout = out;
+  TreeView tv = t->view();
+  // the target version excludes the target (KDLeafNode.cxx:369-382); periodic trees use
+  // the coordinate version, which keeps it (KDSplitNode.cxx:1382-1387)
+  int excl = (qmode == 0 && !tv.periodic && !t->periodic) ? 1 : 0;
+  int64_t tot = 0;
+  if (!t->dev()) {
+    // count first, then size the device output
+    int s = run_ball(tv, qmode, dt, dx, (int)nq, fdist2, excl, doff, nullptr, 0, &tot, S.alloc, t->st);
+    *total = tot;
+    if (s != NBK_OK && s != NBK_ERR_INVALID) return s;
+    if (tot > out_capacity || !out) {
+      NBK_TRY(S.finish());
+      set_error("ball search: output capacity " + std::to_string(out_capacity) + " < " +
+                std::to_string(tot) + " results");
+      return NBK_ERR_INVALID;
+    }
+    NBK_TRY(S.out(out, std::max<int64_t>(tot, 1), &dout));
+    NBK_TRY(run_ball(tv, qmode, dt, dx, (int)nq, fdist2, excl, doff, dout, tot, &tot, S.alloc, t->st));
+    NBK_TRY(S.finish());
+    return NBK_OK;
+  }
+  int s = run_ball(tv, qmode, dt, dx, (int)nq, fdist2, excl, doff, dout, out_capacity, &tot, S.alloc, t->st);
+  *total = tot;
+  return s;
+}
+
+int nbk_ball_tagged(nbk_tree* t, const int32_t* targets, int64_t ntargets, double fdist2,
+                    int64_t* offsets, int32_t* out, int64_t out_capacity, int64_t* total) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return ball_common(t, 0, targets, nullptr, ntargets, fdist2, offsets, out, out_capacity, total);
+  API_END
+}
+
+int nbk_ball_tagged_points(nbk_tree* t, const double* x, int64_t nq, double fdist2,
+                           int64_t* offsets, int32_t* out, int64_t out_capacity,
+                           int64_t* total) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return ball_common(t, 1, nullptr, x, nq, fdist2, offsets, out, out_capacity, total);
+  API_END
+}
+
+int nbk_ball_mark(nbk_tree* t, int32_t target, double fdist2, int32_t imark, int32_t* nn,
+                  double* dist2) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  if (!nn || !dist2 || target < 0 || target >= t->n) {
+    set_error("nbk_ball_mark: invalid argument");
+    return NBK_ERR_INVALID;
+  }
+  Stage S(t);
+  int* dnn;
+  double* dd2;
+  NBK_TRY(S.out(nn, t->n, &dnn, true));
+  NBK_TRY(S.out(dist2, t->n, &dd2, true));
+  TreeView tv = t->view();
+  int target_search = (!t->periodic) ? 1 : 0;
+  NBK_TRY(run_ball_mark(tv, target, fdist2, imark, dnn, dd2, t->arr.perm, target_search, t->st));
+  NBK_TRY(S.finish());
+  return NBK_OK;
+  API_END
+}
+
+int nbk_fof(nbk_tree* t, double fdist, int32_t minnum, int order, int32_t* group,
+            int32_t* ngroup) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  if (!group || !ngroup || !(fdist >= 0)) {
+    set_error("nbk_fof: invalid argument");
+    return NBK_ERR_INVALID;
+  }
+  Stage S(t);
+  int* dg;
+  NBK_TRY(S.out(group, t->n, &dg));
+  int *parent, *gtree;
+  NBK_TRY(S.alloc.get((void**)&parent, sizeof(int) * t->n));
+  NBK_TRY(S.alloc.get((void**)&gtree, sizeof(int) * t->n));
+  NBK_TRY(clear_err(t));
+  FofArgs a{};
+  a.tv = t->view();
+  a.ll2 = fdist * fdist;
+  a.parent = parent;
+  a.err = t->d_err;
+  int ng = 0;
+  NBK_TRY(run_fof(a, (int)t->nslots, minnum, order, gtree, &ng, S.alloc, t->st));
+  if (t->n > 0) {
+    k_scatter_i<<<(unsigned)((t->n + 255) / 256), 256, 0, t->st>>>(gtree, t->arr.perm, dg, t->n); note_launch();
+    NBK_CUDA_TRY(cudaGetLastError());
+  }
+  NBK_TRY(S.finish());
+  NBK_TRY(check_err(t, "nbk_fof"));
+  *ngroup = ng;
+  return NBK_OK;
+  API_END
+}
+
+int nbk_fof_criterion(nbk_tree* t, int comparator, const double* params, int32_t minnum,
+                      int order, int32_t* group, int32_t* ngroup) {
+  (void)comparator;
+  (void)params;
+  (void)minnum;
+  (void)order;
+  (void)group;
+  (void)ngroup;
+  NBK_TRY(check_tree(t));
+  set_error("nbk_fof_criterion: not yet available");
+  return NBK_ERR_UNSUPPORTED;
+}
+
+int nbk_density_adjoint(nbk_tree* t, int k, const double* w, double* rho, double* grad_pos,
+                        double* grad_mass) {
+  (void)k;
+  (void)w;
+  (void)rho;
+  (void)grad_pos;
+  (void)grad_mass;
+  NBK_TRY(check_tree(t));
+  set_error("nbk_density_adjoint: not yet available");
+  return NBK_ERR_UNSUPPORTED;
+}
+
+int nbk_batch_create(const double*, const double*, const int64_t*, int64_t, int, int, int,
+                     unsigned, nbk_batch** out) {
+  if (out) *out = nullptr;
+  set_error("batched path not yet available");
+  return NBK_ERR_UNSUPPORTED;
+}
+int nbk_batch_destroy(nbk_batch*) { return NBK_OK; }
+int nbk_batch_set_stream(nbk_batch*, void*) { return NBK_ERR_UNSUPPORTED; }
+int nbk_batch_density(nbk_batch*, int, double*, int) { return NBK_ERR_UNSUPPORTED; }
+int nbk_batch_density_pertree(nbk_batch*, int, double*) { return NBK_ERR_UNSUPPORTED; }
+
+}  // extern "C"

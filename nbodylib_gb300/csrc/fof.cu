@@ -1,0 +1,360 @@
+// Friends-of-friends on the GPU (replaces KDTree::FOF, src/KDTree/KDFOF.cxx:29-153, and
+// the node searches it drives: SplitNode/LeafNode::FOFSearchBall[Periodic],
+// KDSplitNode.cxx:921-988, 1602-1646, KDLeafNode.cxx:527-589).
+//
+// The reference grows one group at a time by breadth-first search; its result is the
+// set of connected components of the graph "d2 < ll^2" (with periodic images), numbered
+// by the first member met in tree order, groups below minnum dropped. Here:
+//  1. prelink: every particle is united with the first particle of its largest
+//     "compact" ancestor node (box diagonal certainly below ll, so every pair inside is
+//     linked);
+//  2. link: one warp per 32 consecutive particles walks the tree with radius ll. A
+//     compact node that lies wholly inside a lane's ball is united with that lane's
+//     particle in one step; otherwise leaves are tested pair by pair in FP64 with the
+//     reference's arithmetic and linked pairs are united. Union-find links the larger
+//     root under the smaller (atomicCAS), so every root ends as its component's minimum
+//     tree index.
+//  3. label: roots of components with at least minnum members get 1..G in increasing
+//     root order -- the reference's numbering (discovery order in tree order).
+// All FP32 shortcuts are conservative (directed rounding), so the linked pairs are
+// exactly those the FP64 test links.
+#include "nbk_build.h"
+
+namespace nbk {
+
+namespace {
+
+constexpr int kCap = 1 << 24;  // iteration cap for union-find loops
+
+__device__ __forceinline__ int ld_parent(const int* p, int x) {
+  return *((volatile const int*)p + x);
+}
+
+__device__ int find_root(int* parent, int x, int* err) {
+  for (int it = 0; it < kCap; it++) {
+    int p = ld_parent(parent, x);
+    if (p == x) return x;
+    int gp = ld_parent(parent, p);
+    if (gp != p) atomicCAS(&parent[x], p, gp);
+    x = gp;
+  }
+  atomicExch(err, kErrIterCap);
+  return x;
+}
+
+__device__ void unite(int* parent, int a, int b, int* err) {
+  for (int it = 0; it < 1 << 20; it++) {
+    a = find_root(parent, a, err);
+    b = find_root(parent, b, err);
+    if (a == b) return;
+    if (a < b) {
+      int t = a;
+      a = b;
+      b = t;
+    }
+    int old = atomicCAS(&parent[a], a, b);
+    if (old == a) return;
+    a = old;
+  }
+  atomicExch(err, kErrIterCap);
+}
+
+__device__ __forceinline__ bool node_compact(const NodeRec& r, float ll2_lo) {
+  float ex = __fsub_ru(r.hi[0], r.lo[0]), ey = __fsub_ru(r.hi[1], r.lo[1]),
+        ez = __fsub_ru(r.hi[2], r.lo[2]);
+  float d = __fadd_ru(__fadd_ru(__fmul_ru(ex, ex), __fmul_ru(ey, ey)), __fmul_ru(ez, ez));
+  return d < ll2_lo;
+}
+
+__global__ void k_iota(int* p, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = i;
+}
+
+// 1. unite each particle with the first particle of its highest compact ancestor
+__global__ void k_prelink(FofArgs a) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const TreeView& tv = a.tv;
+  if (t >= tv.n) return;
+  int ti = tv.pstart + t;
+  float ll2_lo = thresh_lo(a.ll2);
+  int h = 0;
+  for (int depth = 0; depth < 64; depth++) {
+    NodeRec r = tv.node[tv.nbase + h];
+    if (node_compact(r, ll2_lo)) {
+      if (r.start != ti) unite(a.parent, ti, r.start, a.err);
+      return;
+    }
+    if (r.count <= tv.b) return;
+    NodeRec l = tv.node[tv.nbase + 2 * h + 1];
+    h = (ti < l.start + l.count) ? 2 * h + 1 : 2 * h + 2;
+  }
+}
+
+constexpr int kStack = 64;
+constexpr int kWpb = 8;
+
+struct FofSmem {
+  float4 sf[32];
+  P4 sp[32];
+  int stk[kStack];
+};
+
+__global__ void __launch_bounds__(32 * kWpb) k_link(FofArgs a) {
+  __shared__ FofSmem sm[kWpb];
+  const unsigned FULL = 0xffffffffu;
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  FofSmem& w = sm[warp];
+  const TreeView& tv = a.tv;
+  int q = (blockIdx.x * kWpb + warp) * 32 + lane;
+  if ((blockIdx.x * kWpb + warp) * 32 >= tv.n) return;
+  bool valid = q < tv.n;
+  int self = tv.pstart + (valid ? q : 0);
+  P4 me = tv.pos[self];
+  double x0[3] = {me.x, me.y, me.z};
+  float thr = thresh_hi(a.ll2), ll2_lo = thresh_lo(a.ll2);
+  float eps = tv.eps, two_eps = __fmul_ru(2.f, tv.eps);
+  int npass = tv.periodic ? 8 : 1;
+  for (int pass = 0; pass < npass; pass++) {
+    double xq[3] = {x0[0], x0[1], x0[2]};
+    bool active = valid;
+    if (pass > 0) {
+      double sval = reflect(x0, xq, tv.period, kImageMask[pass]);
+      active = active && (a.ll2 > dmul(sval, sval));  // KDSplitNode.cxx:1611
+    }
+    if (!__any_sync(FULL, active)) continue;
+    float qx = __double2float_rn(xq[0]), qy = __double2float_rn(xq[1]),
+          qz = __double2float_rn(xq[2]);
+    int sp = 1;
+    if (lane == 0) w.stk[0] = 0;
+    __syncwarp();
+    while (sp > 0) {
+      int h = w.stk[sp - 1];
+      sp--;
+      __syncwarp();
+      NodeRec r = tv.node[tv.nbase + h];
+      bool need = active && box_d2_lo(qx, qy, qz, eps, r) < thr;
+      if (need && node_compact(r, ll2_lo) &&
+          box_far_d2_hi(qx, qy, qz, eps, r) < ll2_lo) {
+        unite(a.parent, self, r.start, a.err);
+        need = false;
+      }
+      if (!__any_sync(FULL, need)) continue;
+      if (r.count <= tv.b) {
+        for (int c0 = 0; c0 < r.count; c0 += 32) {
+          int m = min(32, r.count - c0);
+          if (lane < m) {
+            w.sf[lane] = tv.posf[r.start + c0 + lane];
+            w.sp[lane] = tv.pos[r.start + c0 + lane];
+          }
+          __syncwarp();
+          if (need) {
+            for (int j = 0; j < m; j++) {
+              int ti = r.start + c0 + j;
+              // direct pass: the test is symmetric, so each pair is handled once
+              if (pass == 0 && ti <= self) continue;
+              float4 cf = w.sf[j];
+              if (pair_d2_lo(qx, qy, qz, cf.x, cf.y, cf.z, two_eps) < thr) {
+                P4 c = w.sp[j];
+                double d2 = dist2_exact(xq[0], xq[1], xq[2], c.x, c.y, c.z);
+                if (d2 < a.ll2) unite(a.parent, self, ti, a.err);
+              }
+            }
+          }
+          __syncwarp();
+        }
+      } else {
+        int hl = 2 * h + 1, hr = 2 * h + 2;
+        NodeRec rl = tv.node[tv.nbase + hl], rr = tv.node[tv.nbase + hr];
+        bool nl = need && box_d2_lo(qx, qy, qz, eps, rl) < thr;
+        bool nr = need && box_d2_lo(qx, qy, qz, eps, rr) < thr;
+        bool anyl = __any_sync(FULL, nl), anyr = __any_sync(FULL, nr);
+        if (sp + 2 > kStack) {
+          if (lane == 0) atomicExch(a.err, kErrCapacity);
+          return;
+        }
+        if (anyr) {
+          if (lane == 0) w.stk[sp] = hr;
+          sp++;
+        }
+        if (anyl) {
+          if (lane == 0) w.stk[sp] = hl;
+          sp++;
+        }
+        __syncwarp();
+      }
+    }
+  }
+}
+
+__global__ void k_flatten_count(int* parent, int n, int* cnt) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int x = i;
+  while (true) {
+    int p = parent[x];
+    if (p == x) break;
+    x = p;
+  }
+  parent[i] = x;  // no concurrent writers remain; roots are untouched
+  atomicAdd(&cnt[x], 1);
+}
+
+__global__ void k_valid(const int* parent, const int* cnt, int n, int minnum, int* flag) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  flag[i] = (parent[i] == i && cnt[i] >= minnum) ? 1 : 0;
+}
+
+// exclusive scan (three-phase, 1024 per block)
+__global__ void k_scan_blocks(const int* in, int* out, int* bsum, int n) {
+  __shared__ int s[1024];
+  int i = blockIdx.x * 1024 + threadIdx.x;
+  int v = i < n ? in[i] : 0;
+  s[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    int t = threadIdx.x >= o ? s[threadIdx.x - o] : 0;
+    __syncthreads();
+    s[threadIdx.x] += t;
+    __syncthreads();
+  }
+  if (i < n) out[i] = s[threadIdx.x] - v;
+  if (threadIdx.x == 1023) bsum[blockIdx.x] = s[1023];
+}
+__global__ void k_scan_sums(int* bsum, int nb, int* total) {
+  __shared__ int run;
+  if (threadIdx.x == 0) run = 0;
+  __syncthreads();
+  for (int c0 = 0; c0 < nb; c0 += 1024) {
+    __shared__ int s[1024];
+    int i = c0 + threadIdx.x;
+    int v = i < nb ? bsum[i] : 0;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+      int t = threadIdx.x >= o ? s[threadIdx.x - o] : 0;
+      __syncthreads();
+      s[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (i < nb) bsum[i] = run + s[threadIdx.x] - v;
+    __syncthreads();
+    if (threadIdx.x == 1023) run += s[1023];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = run;
+}
+__global__ void k_scan_add(int* out, const int* bsum, int n) {
+  int i = blockIdx.x * 1024 + threadIdx.x;
+  if (i < n) out[i] += bsum[blockIdx.x];
+}
+
+__global__ void k_label(const int* parent, const int* flag, const int* lbl, int n, int* group) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int r = parent[i];
+  group[i] = flag[r] ? lbl[r] + 1 : 0;
+}
+
+// order = 1: sort keys (size descending, then label) with a bitonic network in global
+// memory; then new_label[old] = rank + 1.
+__global__ void k_order_keys(const int* parent, const int* flag, const int* lbl, const int* cnt,
+                             int n, unsigned long long* keys) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (flag[i]) {
+    unsigned size = (unsigned)cnt[i];
+    keys[lbl[i]] = ((unsigned long long)(0xffffffffu - size) << 32) | (unsigned)lbl[i];
+  }
+}
+__global__ void k_pad(unsigned long long* keys, int g, int P) {
+  int i = g + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < P) keys[i] = ~0ull;
+}
+__global__ void k_bitonic(unsigned long long* keys, int P, int kk, int jj) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= P) return;
+  int u = t ^ jj;
+  if (u > t) {
+    bool up = (t & kk) == 0;
+    unsigned long long a = keys[t], b = keys[u];
+    if ((a > b) == up) {
+      keys[t] = b;
+      keys[u] = a;
+    }
+  }
+}
+__global__ void k_rank(const unsigned long long* keys, int g, int* newlbl) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g) return;
+  newlbl[(int)(keys[i] & 0xffffffffu)] = i + 1;
+}
+__global__ void k_relabel(int* group, const int* newlbl, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int g = group[i];
+  if (g > 0) group[i] = newlbl[g - 1];
+}
+
+}  // namespace
+
+int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tree,
+            int* h_ngroup, DevAlloc& alloc, cudaStream_t st) {
+  (void)nnodes;
+  int n = a.tv.n;
+  if (n == 0) {
+    *h_ngroup = 0;
+    return NBK_OK;
+  }
+  int* cnt;
+  int *flag, *lbl, *bsum, *d_total;
+  int nb = (n + 1023) / 1024;
+  NBK_TRY(alloc.get((void**)&cnt, sizeof(int) * n));
+  NBK_TRY(alloc.get((void**)&flag, sizeof(int) * n));
+  NBK_TRY(alloc.get((void**)&lbl, sizeof(int) * n));
+  NBK_TRY(alloc.get((void**)&bsum, sizeof(int) * (nb + 1)));
+  NBK_TRY(alloc.get((void**)&d_total, sizeof(int)));
+  k_iota<<<(n + 255) / 256, 256, 0, st>>>(a.parent, n); note_launch();
+  {
+    Phase ph("fof_prelink", st);
+    k_prelink<<<(n + 255) / 256, 256, 0, st>>>(a); note_launch();
+  }
+  int warps = (n + 31) / 32;
+  {
+    Phase ph("fof_link", st);
+    k_link<<<(warps + kWpb - 1) / kWpb, 32 * kWpb, 0, st>>>(a); note_launch();
+  }
+  Phase ph_label("fof_label", st);
+  NBK_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * n, st));
+  k_flatten_count<<<(n + 255) / 256, 256, 0, st>>>(a.parent, n, cnt); note_launch();
+  k_valid<<<(n + 255) / 256, 256, 0, st>>>(a.parent, cnt, n, minnum, flag); note_launch();
+  k_scan_blocks<<<nb, 1024, 0, st>>>(flag, lbl, bsum, n); note_launch();
+  k_scan_sums<<<1, 1024, 0, st>>>(bsum, nb, d_total); note_launch();
+  k_scan_add<<<nb, 1024, 0, st>>>(lbl, bsum, n); note_launch();
+  k_label<<<(n + 255) / 256, 256, 0, st>>>(a.parent, flag, lbl, n, d_group_tree); note_launch();
+  NBK_CUDA_TRY(cudaGetLastError());
+  int total = 0;
+  NBK_CUDA_TRY(cudaMemcpyAsync(&total, d_total, sizeof(int), cudaMemcpyDeviceToHost, st));
+  NBK_CUDA_TRY(cudaStreamSynchronize(st));
+  *h_ngroup = total;
+  if (order && total > 1) {
+    int P = 1;
+    while (P < total) P <<= 1;
+    unsigned long long* keys;
+    int* newlbl;
+    NBK_TRY(alloc.get((void**)&keys, sizeof(unsigned long long) * P));
+    NBK_TRY(alloc.get((void**)&newlbl, sizeof(int) * total));
+    k_order_keys<<<(n + 255) / 256, 256, 0, st>>>(a.parent, flag, lbl, cnt, n, keys); note_launch();
+    if (P > total) k_pad<<<(P - total + 255) / 256, 256, 0, st>>>(keys, total, P); note_launch();
+    for (int kk = 2; kk <= P; kk <<= 1)
+      for (int jj = kk >> 1; jj > 0; jj >>= 1)
+        k_bitonic<<<(P + 255) / 256, 256, 0, st>>>(keys, P, kk, jj); note_launch();
+    k_rank<<<(total + 255) / 256, 256, 0, st>>>(keys, total, newlbl); note_launch();
+    k_relabel<<<(n + 255) / 256, 256, 0, st>>>(d_group_tree, newlbl, n); note_launch();
+    NBK_CUDA_TRY(cudaGetLastError());
+  }
+  return NBK_OK;
+}
+
+}  // namespace nbk

@@ -1,0 +1,120 @@
+// Host-side declarations shared by the libnbkdt translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/nbkdt.h"
+#include "nbk_internal.cuh"
+
+#define NBK_TRY(expr)              \
+  do {                             \
+    int _s = (expr);               \
+    if (_s != NBK_OK) return _s;   \
+  } while (0)
+
+namespace nbk {
+
+constexpr int kLocalMax = 1024;  // subtrees up to this size finish in one CTA
+
+// One tree of a forest: particles [pstart, pstart+n) in both input and tree order, nodes
+// at [nbase, nbase + heap_slots(n, b)).
+struct TreeSpec {
+  int64_t pstart, n;
+  int nbase;
+};
+
+struct BuiltArrays {
+  P4* pos = nullptr;
+  float4* posf = nullptr;
+  V4* vel = nullptr;
+  int* perm = nullptr;
+  NodeRec* node = nullptr;
+  NodeX* nodex = nullptr;
+};
+
+// Stream-ordered device allocations. Scratch allocations made through get() are freed
+// together by release_all_scratch(); the device's default memory pool keeps the memory
+// cached, so repeated builds do not return to the driver.
+struct DevAlloc {
+  std::vector<void*> scratch;
+  cudaStream_t st = nullptr;
+  int get(void** p, size_t bytes);
+  int upload(void* dst, const void* src, size_t bytes, cudaStream_t s);
+  void release_all_scratch(cudaStream_t s);
+  ~DevAlloc();
+};
+int dev_malloc(void** p, size_t bytes, cudaStream_t st);
+void dev_free(void* p, cudaStream_t st);
+
+int64_t heap_slots(int64_t n, int b);
+int64_t count_nodes(int64_t n, int b);
+size_t local_build_smem();
+int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_in,
+                 const double* d_mass_in, const double* d_vel_in, BuiltArrays& out,
+                 DevAlloc& alloc, cudaStream_t st);
+
+// ---- kNN family
+enum Epi : int {
+  kEpiNN = 0,          // neighbour lists
+  kEpiDensity = 1,     // CalcDensity scatter
+  kEpiDensVel = 2,     // CalcDensity + CalcVelDensity from one search
+  kEpiVel = 3,         // CalcVelDensity
+  kEpiDensPart = 4,    // CalcDensityParticle (gather only)
+  kEpiVelPart = 5,     // CalcVelDensityParticle
+  kEpiDensSave = 6,    // CalcDensity scatter + save neighbour lists (adjoint forward)
+};
+
+struct KnnArgs {
+  TreeView tv;
+  int kheap;          // heap size (k, or k+1 for periodic searches)
+  int kout;           // entries per output row
+  int drop_largest;   // pop the largest entry before writing (periodic FindNearestPos)
+  int exclude_self;   // target search: skip the query itself and zero distances
+  int periodic;       // search mirror images
+  int min_image;      // image gates: 0 = the reference's, 1 = corrected
+  int qmode;          // 0: tree particles [q0, q0+nq), 1: coordinates qx, 2: targets qidx
+  int q0;
+  int nq;
+  const double* qx;
+  const int* qidx;
+  int nsmooth;
+  const double* kernel;
+  int kernres;
+  int* nn;            // nq x kout
+  double* d2;
+  double* rho;        // tree order (scatter) or query order (particle variants)
+  double* vden;
+  int* err;
+};
+int launch_knn(const KnnArgs& a, int epi, cudaStream_t st);
+
+// ---- FOF / ball / adjoint
+struct FofArgs {
+  TreeView tv;
+  double ll2;          // linking length squared
+  int crit;            // 0: plain FOF, 1: FOFCriterion
+  int cmp;             // comparator for crit
+  double params[8];
+  int* parent;         // tree order union-find forest
+  int* err;
+};
+int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tree,
+            int* h_ngroup, DevAlloc& alloc, cudaStream_t st);
+
+int run_ball(const TreeView& tv, int qmode, const int* qidx, const double* qx, int nq,
+             double fdist2, int exclude_self, int64_t* d_offsets, int* d_out,
+             int64_t out_capacity, int64_t* h_total, DevAlloc& alloc, cudaStream_t st);
+int run_ball_mark(const TreeView& tv, int target, double fdist2, int imark, int* d_mark,
+                  double* d_dist2, const int* d_perm, int target_search, cudaStream_t st);
+
+int run_density_adjoint(const TreeView& tv, int k, const int* d_nn, const double* d_w_tree,
+                        const double* d_rho_tree, const double* kernel, int kernres,
+                        double* d_gpos_tree, double* d_gmass_tree, cudaStream_t st);
+
+// permutation helpers
+int scatter_to_input_order(const double* tree_vals, const int* perm, double* out, int64_t n,
+                           int stride, cudaStream_t st);
+
+}  // namespace nbk

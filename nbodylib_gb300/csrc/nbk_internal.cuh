@@ -1,0 +1,226 @@
+// Internal types and device helpers shared by the libnbkdt kernels.
+//
+// HBM layout of a built tree (all arrays in tree order unless noted):
+//   P4      pos[n]    x, y, z, mass as FP64 (32 B, two 16-B vector loads)
+//   float4  posf[n]   x, y, z rounded to nearest FP32 (candidate filter)
+//   V4 vel[n]    vx, vy, vz, 0 (only when velocities were given)
+//   int32   perm[n]   tree index -> input index
+//   NodeRec node[]    heap-indexed (root 0, children 2h+1 / 2h+2): FP32 bounding box
+//                     rounded outward plus the particle range; 32 B per node
+//   NodeX   nodex[]   the same nodes with the exact FP64 bounding box and split plane
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cfloat>
+#include <string>
+
+namespace nbk {
+
+constexpr double kMaxValue = 1e32;  // MAXVALUE, src/Math/Precision.h
+constexpr int kWarp = 32;
+
+struct __align__(32) P4 {
+  double x, y, z, m;
+};
+
+struct __align__(32) V4 {
+  double x, y, z, w;
+};
+__host__ __device__ __forceinline__ V4 make_v4(double x, double y, double z, double w) {
+  V4 v;
+  v.x = x;
+  v.y = y;
+  v.z = z;
+  v.w = w;
+  return v;
+}
+
+struct __align__(16) NodeRec {
+  float lo[3];  // bounding box rounded down (lo) and up (hi): contains every particle
+  float hi[3];
+  int start;    // first particle (tree index, absolute)
+  int count;    // particles in the node; 0 marks an unused heap slot
+};
+
+struct NodeX {
+  double lo[3], hi[3];  // exact FP64 bounding box (min/max of the node's particles)
+  double split_val;     // coordinate of the median particle (the reference's cut_val)
+  int split_dim;        // -1 for a leaf
+  int pad;
+};
+
+// Device view of one tree (or of one tree of a batch).
+struct TreeView {
+  const P4* pos;
+  const float4* posf;
+  const V4* vel;
+  const int* perm;
+  const NodeRec* node;
+  const NodeX* nodex;
+  int n;       // particles in this tree
+  int pstart;  // absolute tree index of its first particle
+  int nbase;   // index of its root in the node arrays
+  int b;       // bucket size
+  int periodic;
+  double period[3];
+  float eps;  // bound on |x - float(x)| for any coordinate or image coordinate
+};
+
+// ---- exact FP64 helpers: explicit round-to-nearest ops are never contracted into FMAs
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+
+// DistanceSqd (src/KDTree/DistFunc.h:14-19): ((dx*dx + dy*dy) + dz*dz), each op rounded.
+__device__ __forceinline__ double dist2_exact(double ax, double ay, double az, double bx,
+                                              double by, double bz) {
+  double dx = dsub(ax, bx), dy = dsub(ay, by), dz = dsub(az, bz);
+  return dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz));
+}
+
+// Order-preserving map from FP64 to uint64 (-0.0 is folded onto +0.0 so that equal
+// values compare equal, as the reference's FP comparisons treat them).
+__host__ __device__ __forceinline__ uint64_t okey(double v) {
+  if (v == 0.0) v = 0.0;
+#ifdef __CUDA_ARCH__
+  uint64_t u = (uint64_t)__double_as_longlong(v);
+#else
+  uint64_t u;
+  memcpy(&u, &v, 8);
+#endif
+  return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+}
+__host__ __device__ __forceinline__ double okey_inv(uint64_t k) {
+  uint64_t u = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)u);
+#else
+  double v;
+  memcpy(&v, &u, 8);
+  return v;
+#endif
+}
+
+// ---- conservative FP32 bounds (never reject what the exact FP64 test would accept)
+// Lower bound of the squared distance from a query known to within +-eps of (qx,qy,qz)
+// to the box [lo, hi].
+__device__ __forceinline__ float box_d2_lo(float qx, float qy, float qz, float eps,
+                                           const NodeRec& r) {
+  float gx = fmaxf(0.f, fmaxf(__fsub_rd(r.lo[0], __fadd_ru(qx, eps)),
+                              __fsub_rd(__fsub_rd(qx, eps), r.hi[0])));
+  float gy = fmaxf(0.f, fmaxf(__fsub_rd(r.lo[1], __fadd_ru(qy, eps)),
+                              __fsub_rd(__fsub_rd(qy, eps), r.hi[1])));
+  float gz = fmaxf(0.f, fmaxf(__fsub_rd(r.lo[2], __fadd_ru(qz, eps)),
+                              __fsub_rd(__fsub_rd(qz, eps), r.hi[2])));
+  return __fadd_rd(__fadd_rd(__fmul_rd(gx, gx), __fmul_rd(gy, gy)), __fmul_rd(gz, gz));
+}
+// Upper bound of the squared distance from the query to the farthest box corner.
+__device__ __forceinline__ float box_far_d2_hi(float qx, float qy, float qz, float eps,
+                                               const NodeRec& r) {
+  float ax = fmaxf(__fsub_ru(__fadd_ru(qx, eps), r.lo[0]), __fsub_ru(r.hi[0], __fsub_rd(qx, eps)));
+  float ay = fmaxf(__fsub_ru(__fadd_ru(qy, eps), r.lo[1]), __fsub_ru(r.hi[1], __fsub_rd(qy, eps)));
+  float az = fmaxf(__fsub_ru(__fadd_ru(qz, eps), r.lo[2]), __fsub_ru(r.hi[2], __fsub_rd(qz, eps)));
+  return __fadd_ru(__fadd_ru(__fmul_ru(ax, ax), __fmul_ru(ay, ay)), __fmul_ru(az, az));
+}
+// Lower bound of the squared distance between a query and a particle whose FP32
+// roundings are (qx..) and (cx..), both within eps of the true coordinates.
+__device__ __forceinline__ float pair_d2_lo(float qx, float qy, float qz, float cx, float cy,
+                                            float cz, float two_eps) {
+  float dx = fmaxf(0.f, __fsub_rd(fabsf(__fsub_rz(qx, cx)), two_eps));
+  float dy = fmaxf(0.f, __fsub_rd(fabsf(__fsub_rz(qy, cy)), two_eps));
+  float dz = fmaxf(0.f, __fsub_rd(fabsf(__fsub_rz(qz, cz)), two_eps));
+  return __fadd_rd(__fadd_rd(__fmul_rd(dx, dx), __fmul_rd(dy, dy)), __fmul_rd(dz, dz));
+}
+// FP32 threshold above any value whose FP64 counterpart could still be below t.
+__device__ __forceinline__ float thresh_hi(double t) {
+  float f = __double2float_ru(t);
+  return __fmul_ru(f, 1.0f + 1.0f / 1048576.0f);
+}
+// FP32 threshold below which an FP64 value is certainly below t (for "all inside").
+__device__ __forceinline__ float thresh_lo(double t) {
+  float f = __double2float_rd(t);
+  return __fmul_rd(f, 1.0f - 1.0f / 1048576.0f);
+}
+
+// PeriodicReflection1D/2D/ND (src/KDTree/DistFunc.h:326-355): image of x0 across the
+// walls named by `mask` (bit k = dimension k); returns sval (a distance; for one
+// dimension the signed wall distance, otherwise sqrt of the summed squares).
+__device__ __forceinline__ double reflect(const double x0[3], double xp[3], const double p[3],
+                                          int mask) {
+  xp[0] = x0[0];
+  xp[1] = x0[1];
+  xp[2] = x0[2];
+  int cnt = (mask & 1) + ((mask >> 1) & 1) + ((mask >> 2) & 1);
+  if (cnt == 1) {
+    int k = (mask & 1) ? 0 : ((mask & 2) ? 1 : 2);
+    if (x0[k] < p[k] / 2.0) {
+      xp[k] = dadd(x0[k], p[k]);
+      return x0[k];
+    }
+    xp[k] = dsub(x0[k], p[k]);
+    return -xp[k];
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    if (!((mask >> k) & 1)) continue;
+    if (x0[k] < p[k] / 2.0) {
+      xp[k] = dadd(x0[k], p[k]);
+      s = dadd(s, dmul(x0[k], x0[k]));
+    } else {
+      xp[k] = dsub(x0[k], p[k]);
+      s = dadd(s, dmul(xp[k], xp[k]));
+    }
+  }
+  return __dsqrt_rn(s);
+}
+// The order in which the reference searches the images: x, y, z, xy, xz, yz, xyz
+// (KDSplitNode.cxx:1126-1147).
+__device__ __constant__ static const int kImageMask[8] = {0, 1, 2, 4, 3, 5, 6, 7};
+
+// Wsm (KDCalcSmoothQuantities.cxx:12-15) on the host-built table.
+__device__ __forceinline__ double wsm(double r, int i, int size, double delta, const double* x) {
+  if (i < size - 1) {
+    double xi = x[i], xj = x[i + 1];
+    return dadd(xi, __ddiv_rn(dmul(dsub(xj, xi), dsub(r, dmul(delta, (double)i))), delta));
+  }
+  return x[i];
+}
+
+// ---- device error word: kernels report bounded-wait and capacity failures here
+enum DeviceErr : int {
+  kErrNone = 0,
+  kErrIterCap = 1,   // a union-find or queue loop exceeded its iteration cap
+  kErrCapacity = 2,  // an output or stack capacity was exceeded
+  kErrTooFew = 3,    // fewer than k neighbours found
+};
+
+}  // namespace nbk
+
+// ---- host-side error state (thread local), set by every entry point
+namespace nbk {
+void set_error(const std::string& msg);
+const char* get_error();
+void note_launch();  // counts every kernel launch (reported by nbk_launch_count)
+
+// Phase trace: when enabled (nbk_trace_enable), a Phase records a CUDA event pair around
+// its scope on the given stream; the elapsed times are resolved when the trace is read.
+struct Phase {
+  const char* name;
+  cudaStream_t st;
+  cudaEvent_t a = nullptr, b = nullptr;
+  Phase(const char* n, cudaStream_t s);
+  ~Phase();
+};
+}  // namespace nbk
+
+#define NBK_CUDA_TRY(expr)                                                                  \
+  do {                                                                                      \
+    cudaError_t _e = (expr);                                                                \
+    if (_e != cudaSuccess) {                                                                \
+      ::nbk::set_error(std::string("CUDA error: ") + cudaGetErrorString(_e) + " at " +      \
+                       __FILE__ + ":" + std::to_string(__LINE__) + " (" #expr ")");         \
+      return NBK_ERR_CUDA;                                                                  \
+    }                                                                                       \
+  } while (0)

@@ -1,0 +1,244 @@
+"""Python mirror of the reference's ``NBody::KDTree`` interface over libnbkdt.
+
+The method names follow ``src/KDTree/KDTree.h`` (pelahi/NBodylib) so tests read like the
+reference's call sites. Arrays are numpy (host) or, when ``device=True``, torch CUDA
+tensors whose storage is passed to the library as device pointers. Neighbour lists hold
+tree indices (``KDTree.h:295``); ``GetPerm()[t]`` is the input index ("ID") of tree index
+``t``; per-particle results are returned in input order.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _capi
+
+TPHYS, TPROJ, TVEL, TPHS, TMETRIC = 0, 1, 2, 3, 4
+KSPH, KGAUSS, KEPAN, KTH = 0, 1, 2, 3
+FINDNEAREST, FINDNEARESTPOS = 0, 1
+PERIODIC_REF, PERIODIC_MIN_IMAGE = 0, 1
+FOF3D, FOFVEL, FOF6D = 0, 1, 2
+DEVICE_PTRS = 1
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data_as(ctypes.c_void_p)
+    return ctypes.c_void_p(a.data_ptr())  # torch tensor
+
+
+class KDTree:
+    """GPU kd-tree with the reference constructor's arguments (KDTree.h:229-245)."""
+
+    def __init__(self, pos, vel=None, mass=None, bucket_size=16, treetype=TPHYS,
+                 kerntype=KEPAN, kernres=1000, splitting_criterion=0, aniso=0, scale_space=0,
+                 period=None, device=False, stream=None):
+        self._lib = _capi.load()
+        self.device = device
+        if device:
+            import torch
+            self._torch = torch
+            pos = pos.contiguous()
+            self.n = pos.shape[0]
+            per = None if period is None else torch.as_tensor(
+                np.broadcast_to(np.asarray(period, np.float64), (3,)).copy(), device=pos.device)
+            args = [pos, None if vel is None else vel.contiguous(),
+                    None if mass is None else mass.contiguous()]
+        else:
+            pos = np.ascontiguousarray(pos, np.float64).reshape(-1, 3)
+            self.n = pos.shape[0]
+            vel = None if vel is None else np.ascontiguousarray(vel, np.float64).reshape(-1, 3)
+            mass = None if mass is None else np.ascontiguousarray(mass, np.float64).reshape(-1)
+            per = None if period is None else np.ascontiguousarray(
+                np.broadcast_to(np.asarray(period, np.float64), (3,)))
+            args = [pos, vel, mass]
+        self._keep = (args, per)
+        self.periodic = period is not None
+        self.bucket_size = bucket_size
+        self.kernres = max(100, kernres)
+        h = ctypes.c_void_p()
+        _capi.check(self._lib.nbk_create(_ptr(args[0]), _ptr(args[1]), _ptr(args[2]), self.n,
+                                         bucket_size, treetype, kerntype, kernres,
+                                         splitting_criterion, aniso, scale_space, _ptr(per),
+                                         DEVICE_PTRS if device else 0, ctypes.byref(h)))
+        self._h = h
+        if stream is not None:
+            self.set_stream(stream)
+
+    # ---- lifetime
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.nbk_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream):
+        ptr = stream.cuda_stream if hasattr(stream, "cuda_stream") else stream
+        _capi.check(self._lib.nbk_set_stream(self._h, ctypes.c_void_p(ptr)))
+
+    def sync(self):
+        _capi.check(self._lib.nbk_sync(self._h))
+
+    # ---- allocation helpers
+    def _empty(self, shape, dtype):
+        if self.device:
+            t = {np.int32: self._torch.int32, np.float64: self._torch.float64,
+                 np.int64: self._torch.int64}[dtype]
+            return self._torch.empty(shape, dtype=t, device="cuda")
+        return np.empty(shape, dtype)
+
+    # ---- getters (KDTree.h:282-289)
+    def _counts(self):
+        a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        d = ctypes.c_int32()
+        _capi.check(self._lib.nbk_get_counts(self._h, ctypes.byref(a), ctypes.byref(b),
+                                             ctypes.byref(c), ctypes.byref(d)))
+        return a.value, b.value, c.value, d.value
+
+    def GetNumNodes(self):
+        return self._counts()[1]
+
+    def GetNumLeafNodes(self):
+        return self._counts()[2]
+
+    def GetBucketSize(self):
+        return self._counts()[3]
+
+    def GetPerm(self):
+        out = self._empty(self.n, np.int32)
+        _capi.check(self._lib.nbk_get_perm(self._h, _ptr(out)))
+        return out
+
+    def GetKernel(self):
+        t = np.empty(self.kernres)
+        kn = ctypes.c_double()
+        _capi.check(self._lib.nbk_get_kernel(self._h, _ptr(t), ctypes.byref(kn)))
+        return t, kn.value
+
+    # ---- kNN (KDTree.h:300-313)
+    def FindNearest(self, k, periodic_mode=PERIODIC_REF):
+        """All-particle FindNearest(tt): (nn[n,k] tree indices, d2[n,k]), row = tree index."""
+        nn = self._empty((self.n, k), np.int32)
+        d2 = self._empty((self.n, k), np.float64)
+        _capi.check(self._lib.nbk_knn(self._h, k, FINDNEAREST, periodic_mode, _ptr(nn), _ptr(d2)))
+        return nn, d2
+
+    def FindNearestPos(self, k, periodic_mode=PERIODIC_REF):
+        nn = self._empty((self.n, k), np.int32)
+        d2 = self._empty((self.n, k), np.float64)
+        _capi.check(self._lib.nbk_knn(self._h, k, FINDNEARESTPOS, periodic_mode, _ptr(nn),
+                                      _ptr(d2)))
+        return nn, d2
+
+    def FindNearestPosPoints(self, x, k, periodic_mode=PERIODIC_REF):
+        """FindNearestPos(Double_t *x) for every row of x."""
+        if not self.device:
+            x = np.ascontiguousarray(x, np.float64).reshape(-1, 3)
+        nq = x.shape[0]
+        nn = self._empty((nq, k), np.int32)
+        d2 = self._empty((nq, k), np.float64)
+        _capi.check(self._lib.nbk_knn_points(self._h, _ptr(x), nq, k, periodic_mode, _ptr(nn),
+                                             _ptr(d2)))
+        return nn, d2
+
+    # ---- SPH (KDTree.h:407-425)
+    def CalcDensity(self, k=64):
+        rho = self._empty(self.n, np.float64)
+        _capi.check(self._lib.nbk_density(self._h, k, _ptr(rho)))
+        return rho
+
+    def CalcVelDensity(self, nsmooth=64, nsearch=64):
+        out = self._empty(self.n, np.float64)
+        _capi.check(self._lib.nbk_veldensity(self._h, nsmooth, nsearch, _ptr(out)))
+        return out
+
+    def CalcDensityAndVelDensity(self, k=64, nsmooth=64):
+        rho = self._empty(self.n, np.float64)
+        vd = self._empty(self.n, np.float64)
+        _capi.check(self._lib.nbk_density_veldensity(self._h, k, nsmooth, _ptr(rho), _ptr(vd)))
+        return rho, vd
+
+    def CalcDensityParticle(self, targets, k=64):
+        targets = self._targets(targets)
+        out = self._empty(len(targets), np.float64)
+        _capi.check(self._lib.nbk_density_particles(self._h, _ptr(targets), len(targets), k,
+                                                    _ptr(out)))
+        return out
+
+    def CalcVelDensityParticle(self, targets, nsmooth=64, nsearch=64):
+        targets = self._targets(targets)
+        out = self._empty(len(targets), np.float64)
+        _capi.check(self._lib.nbk_veldensity_particles(self._h, _ptr(targets), len(targets),
+                                                       nsmooth, nsearch, _ptr(out)))
+        return out
+
+    def _targets(self, targets):
+        if self.device:
+            return targets.to(self._torch.int32).contiguous()
+        return np.ascontiguousarray(np.atleast_1d(targets), np.int32)
+
+    # ---- ball search (KDTree.h:341-376)
+    def SearchBallPosTagged(self, targets, fdist2):
+        """Batch of SearchBallPosTagged(tt, fdist2): CSR (offsets[nt+1], tree indices)."""
+        targets = self._targets(targets)
+        return self._ball(self._lib.nbk_ball_tagged, targets, len(targets), fdist2)
+
+    def SearchBallPosTaggedPoints(self, x, fdist2):
+        if not self.device:
+            x = np.ascontiguousarray(x, np.float64).reshape(-1, 3)
+        return self._ball(self._lib.nbk_ball_tagged_points, x, x.shape[0], fdist2)
+
+    def _ball(self, fn, q, nq, fdist2):
+        offsets = self._empty(nq + 1, np.int64)
+        total = ctypes.c_int64()
+        cap = 0
+        st = fn(self._h, _ptr(q), nq, float(fdist2), _ptr(offsets), None, 0, ctypes.byref(total))
+        if st not in (0, 1):
+            _capi.check(st)
+        cap = max(total.value, 1)
+        out = self._empty(cap, np.int32)
+        _capi.check(fn(self._h, _ptr(q), nq, float(fdist2), _ptr(offsets), _ptr(out), cap,
+                       ctypes.byref(total)))
+        return offsets, out[: total.value]
+
+    def SearchBallPos(self, target, fdist2, imark, nn, dist2):
+        """SearchBallPos(tt, fdist2, imark, nn, dist2): marks input-order arrays in place."""
+        _capi.check(self._lib.nbk_ball_mark(self._h, int(target), float(fdist2), int(imark),
+                                            _ptr(nn), _ptr(dist2)))
+
+    # ---- FOF (KDTree.h:480-503)
+    def FOF(self, fdist, minnum=8, order=0):
+        group = self._empty(self.n, np.int32)
+        ng = ctypes.c_int32()
+        _capi.check(self._lib.nbk_fof(self._h, float(fdist), int(minnum), int(order),
+                                      _ptr(group), ctypes.byref(ng)))
+        return group, ng.value
+
+    def FOFCriterion(self, comparator, params, minnum=8, order=0):
+        p = np.zeros(20)
+        p[: len(params)] = params
+        if self.device:
+            p = self._torch.as_tensor(p, device="cuda")
+        group = self._empty(self.n, np.int32)
+        ng = ctypes.c_int32()
+        _capi.check(self._lib.nbk_fof_criterion(self._h, int(comparator), _ptr(p), int(minnum),
+                                                int(order), _ptr(group), ctypes.byref(ng)))
+        return group, ng.value
+
+    # ---- adjoint (no reference counterpart)
+    def DensityAdjoint(self, k, w):
+        w = w if self.device else np.ascontiguousarray(w, np.float64)
+        rho = self._empty(self.n, np.float64)
+        gp = self._empty((self.n, 3), np.float64)
+        gm = self._empty(self.n, np.float64)
+        _capi.check(self._lib.nbk_density_adjoint(self._h, k, _ptr(w), _ptr(rho), _ptr(gp),
+                                                  _ptr(gm)))
+        return rho, gp, gm

@@ -1,0 +1,141 @@
+"""Generate the golden fixtures from the reference NBodylib KDTree itself.
+
+Runs only where the reference checkout exists (it compiles oracle/_ref/libnbref.so from
+the reference's own sources). Each fixture stores the seeded inputs together with the
+reference's outputs, so the tests never need the reference at run time:
+
+    python tests/golden/make_golden.py
+
+Outputs are in input order ("ID"); neighbour lists hold IDs.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.abspath(os.path.join(HERE, "..", "..")))
+
+import oracle  # noqa: E402
+from nbodylib_gb300 import synthetic as syn  # noqa: E402
+
+
+def ref_tree(pos, vel, mass, b, kerntype, period):
+    return oracle.OracleTree(pos, vel, mass, b, 0, kerntype, 1000, period, backend="ref",
+                             nthreads=4)
+
+
+def uniform_periodic():
+    n = 1500
+    pos, mass = syn.uniform_box(n, 1.0, seed=11)
+    t = ref_tree(pos, None, mass, 16, 0, [1.0, 1.0, 1.0])
+    nn_fn, d2_fn = t.knn(16, method=0)
+    nn_fp, d2_fp = t.knn(16, method=1)
+    rho = t.density(32)
+    t2 = ref_tree(pos, None, mass, 16, 0, [1.0, 1.0, 1.0])
+    ll = syn.linking_length(n, 1.0, 0.5)
+    grp, ng = t2.fof(ll, 5, 0)
+    return dict(pos=pos, mass=mass, period=np.ones(3), b=16, kerntype=0, k=16,
+                nn_findnearest=nn_fn, d2_findnearest=d2_fn, nn_findnearestpos=nn_fp,
+                d2_findnearestpos=d2_fp, k_density=32, rho=rho, ll=ll, fof_minnum=5,
+                fof_group=grp, fof_ngroup=ng, num_nodes=t.num_nodes, num_leaves=t.num_leaves,
+                leaf_start_ids=_leaf_sets(t))
+
+
+def _leaf_sets(t):
+    """Leaf membership as a label per ID: the smallest ID in the same leaf."""
+    ids = t.ids()
+    ls = t.leaf_start()
+    lab = np.empty(len(ids), np.int64)
+    for s in np.unique(ls):
+        members = ids[ls == s]
+        lab[members] = members.min()
+    return lab
+
+
+def clustered():
+    n = 6000
+    box = 100.0
+    pos, mass, vel = syn.clustered_box(n, box, seed=12, velocities=True)
+    per = [box] * 3
+    rng = np.random.default_rng(13)
+    ids = rng.choice(n, 40, replace=False).astype(np.int32)
+    out = dict(pos=pos, mass=mass, vel=vel, period=np.full(3, box), b=16, kerntype=0)
+    t = ref_tree(pos, vel, mass, 16, 0, per)
+    out["num_nodes"] = t.num_nodes
+    out["num_leaves"] = t.num_leaves
+    out["leaf_start_ids"] = _leaf_sets(t)
+    out["k"] = 32
+    out["rho"] = t.density(32)
+    out["veldens_32_32"] = ref_tree(pos, vel, mass, 16, 0, per).veldensity(32, 32)
+    out["veldens_16_32"] = ref_tree(pos, vel, mass, 16, 0, per).veldensity(16, 32)
+    t3 = ref_tree(pos, vel, mass, 16, 0, per)
+    out["query_ids"] = ids
+    out["dens_particle"] = np.array([t3.density_particle(i, 32) for i in ids])
+    out["veldens_particle"] = np.array([t3.veldensity_particle(i, 16, 32) for i in ids])
+    ll = syn.linking_length(n, box)
+    out["ll"] = ll
+    g, ng = ref_tree(pos, vel, mass, 16, 0, per).fof(ll, 10, 0)
+    out["fof_group"], out["fof_ngroup"] = g, ng
+    g, ng = ref_tree(pos, vel, mass, 16, 0, per).fof(ll, 10, 1)
+    out["fof_group_ordered"], out["fof_ngroup_ordered"] = g, ng
+    r2 = (3 * ll) ** 2
+    out["ball_r2"] = r2
+    tb = ref_tree(pos, vel, mass, 16, 0, per)
+    lists = [tb.ball_tagged(int(i), r2) for i in ids]
+    out["ball_offsets"] = np.concatenate([[0], np.cumsum([len(x) for x in lists])]).astype(np.int64)
+    out["ball_ids"] = np.concatenate(lists).astype(np.int32)
+    return out
+
+
+def nonperiodic():
+    n = 700
+    pos, mass = syn.uniform_box(n, 2.0, seed=14)
+    rng = np.random.default_rng(15)
+    t = ref_tree(pos, None, mass, 8, 2, None)  # Epanechnikov, the constructor default
+    nn, d2 = t.knn(20, method=0)
+    rho = ref_tree(pos, None, mass, 8, 2, None).density(20)
+    ids = rng.choice(n, 25, replace=False).astype(np.int32)
+    r2 = 0.35 ** 2
+    tb = ref_tree(pos, None, mass, 8, 2, None)
+    lists = [tb.ball_tagged(int(i), r2) for i in ids]
+    marks = []
+    for i in ids[:10]:
+        m, d = tb.ball_mark(int(i), r2, imark=7)
+        marks.append(np.where(m == 7, d, -1.0))
+    x = rng.random((30, 3)) * 2.0
+    nnx, d2x = tb.knn_pos(x, 12)
+    return dict(pos=pos, mass=mass, b=8, kerntype=2, k=20, nn_findnearest=nn, d2_findnearest=d2,
+                rho=rho, num_nodes=t.num_nodes, num_leaves=t.num_leaves,
+                leaf_start_ids=_leaf_sets(t), query_ids=ids, ball_r2=r2,
+                ball_offsets=np.concatenate([[0], np.cumsum([len(v) for v in lists])]).astype(np.int64),
+                ball_ids=np.concatenate(lists).astype(np.int32),
+                mark_d2=np.array(marks), points=x, knn_points_nn=nnx, knn_points_d2=d2x)
+
+
+def tiny_periodic():
+    """n <= b: the reference's periodic searches fall back to the non-periodic target
+    search (KDLeafNode.cxx:658-661)."""
+    n = 10
+    pos, mass = syn.uniform_box(n, 1.0, seed=16)
+    t = ref_tree(pos, None, mass, 16, 0, [1.0, 1.0, 1.0])
+    nn, d2 = t.knn(5, method=0)
+    nnp, d2p = t.knn(5, method=1)
+    return dict(pos=pos, mass=mass, period=np.ones(3), b=16, k=5, nn_findnearest=nn,
+                d2_findnearest=d2, nn_findnearestpos=nnp, d2_findnearestpos=d2p)
+
+
+def main():
+    oracle.build(ref=True)
+    for name, fn in [("uniform_periodic", uniform_periodic), ("clustered", clustered),
+                     ("nonperiodic", nonperiodic), ("tiny_periodic", tiny_periodic)]:
+        d = fn()
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **{k: np.asarray(v) for k, v in d.items()})
+        print(path, os.path.getsize(path))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,160 @@
+"""GPU parity: tree build (same leaves as the reference), FOF partitions, ball search."""
+import numpy as np
+import pytest
+
+import oracle
+from nbodylib_gb300 import KDTree
+from nbodylib_gb300 import synthetic as syn
+from tests.helpers import assert_same_partition, canonical_groups, golden, to_ids
+
+pytestmark = pytest.mark.gpu
+
+
+def leaf_labels(t):
+    """Leaf membership per ID (label = smallest ID in the leaf), from the GPU tree."""
+    perm = t.GetPerm()
+    n = len(perm)
+    b = t.GetBucketSize()
+    # leaves are maximal runs of the ceil/floor halving of [0, n)
+    lab = np.empty(n, np.int64)
+
+    def rec(s, size):
+        if size <= b:
+            ids = perm[s:s + size]
+            lab[ids] = ids.min()
+            return
+        left = (size - 1) // 2 + 1
+        rec(s, left)
+        rec(s + left, size - left)
+
+    rec(0, n)
+    return lab
+
+
+@pytest.mark.parametrize("name", ["uniform_periodic", "clustered", "nonperiodic"])
+def test_build_same_nodes_and_leaves_as_reference(gpu, name):
+    g = golden(name)
+    t = KDTree(g["pos"], None, g["mass"], int(g["b"]), kerntype=0,
+               period=g["period"] if "period" in g else None)
+    assert t.GetNumNodes() == int(g["num_nodes"])
+    assert t.GetNumLeafNodes() == int(g["num_leaves"])
+    np.testing.assert_array_equal(leaf_labels(t), g["leaf_start_ids"])
+
+
+@pytest.mark.parametrize("n,b", [(1, 16), (17, 16), (1000, 16), (1025, 16), (3001, 7),
+                                  (1 << 20, 16), (300000, 2)])
+def test_build_leaf_sets_vs_oracle(gpu, port_built, n, b):
+    pos, mass = syn.clustered_box(n, 100.0, seed=n % 97)
+    o = oracle.OracleTree(pos, None, mass, b, 0, 0, 1000, None, backend="port", nthreads=8)
+    t = KDTree(pos, None, mass, b, kerntype=0)
+    ids, ls = o.ids(), o.leaf_start()
+    lab = np.empty(n, np.int64)
+    for s in np.unique(ls):
+        m = ids[ls == s]
+        lab[m] = m.min()
+    np.testing.assert_array_equal(leaf_labels(t), lab)
+    assert t.GetNumNodes() == o.num_nodes
+
+
+def test_golden_fof(gpu):
+    g = golden("clustered")
+    t = KDTree(g["pos"], g["vel"], g["mass"], 16, kerntype=0, period=g["period"])
+    grp, ng = t.FOF(float(g["ll"]), 10, 0)
+    assert ng == int(g["fof_ngroup"])
+    assert_same_partition(grp, g["fof_group"], "clustered FOF")
+    grp1, ng1 = t.FOF(float(g["ll"]), 10, 1)
+    assert ng1 == int(g["fof_ngroup_ordered"])
+    assert_same_partition(grp1, g["fof_group_ordered"], "ordered FOF")
+    sizes = np.bincount(grp1)[1:]
+    assert np.all(np.diff(sizes) <= 0)  # order=1: decreasing size
+    g = golden("uniform_periodic")
+    t = KDTree(g["pos"], None, g["mass"], 16, kerntype=0, period=g["period"])
+    grp, ng = t.FOF(float(g["ll"]), int(g["fof_minnum"]))
+    assert ng == int(g["fof_ngroup"])
+    assert_same_partition(grp, g["fof_group"], "uniform FOF")
+
+
+def test_fof_numbering_follows_tree_order(gpu):
+    """Groups are numbered by their first member in tree order (KDFOF.cxx:70-77)."""
+    pos, mass = syn.clustered_box(50000, 100.0, seed=5)
+    t = KDTree(pos, None, mass, 16, kerntype=0, period=[100.0] * 3)
+    grp, ng = t.FOF(syn.linking_length(50000, 100.0), 20)
+    perm = t.GetPerm()
+    g_tree = grp[perm]
+    first = {}
+    for ti, gg in enumerate(g_tree):
+        if gg > 0 and gg not in first:
+            first[gg] = ti
+    assert sorted(first, key=first.get) == list(range(1, ng + 1))
+
+
+def test_fof_2pow20_clustered_vs_oracle(gpu, port_built):
+    """The FOF workload: 2^20 particles, 500 Plummer spheres + 30% background, L=100,
+    ll = 0.2 mean spacing, minnum 20, periodic."""
+    n = 1 << 20
+    pos, mass = syn.clustered_box(n, 100.0, seed=2)
+    ll = syn.linking_length(n, 100.0)
+    o = oracle.OracleTree(pos, None, mass, 16, 0, 0, 1000, [100.0] * 3, backend="port",
+                          nthreads=16)
+    go, no = o.fof(ll, 20)
+    t = KDTree(pos, None, mass, 16, kerntype=0, period=[100.0] * 3)
+    gg, ng = t.FOF(ll, 20)
+    assert ng == no
+    assert_same_partition(gg, go, "2^20 FOF")
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_fof_random_vs_oracle(gpu, port_built, periodic):
+    pos, mass = syn.uniform_box(20000, 10.0, seed=9)
+    per = [10.0] * 3 if periodic else None
+    ll = syn.linking_length(20000, 10.0, 0.7)
+    o = oracle.OracleTree(pos, None, mass, 12, 0, 0, 1000, per, backend="port")
+    go, no = o.fof(ll, 3)
+    t = KDTree(pos, None, mass, 12, kerntype=0, period=per)
+    gg, ng = t.FOF(ll, 3)
+    assert ng == no
+    assert_same_partition(gg, go)
+
+
+def test_golden_ball(gpu):
+    for name in ["clustered", "nonperiodic"]:
+        g = golden(name)
+        t = KDTree(g["pos"], None, g["mass"], int(g["b"]), kerntype=0,
+                   period=g["period"] if "period" in g else None)
+        perm = t.GetPerm()
+        inv = np.argsort(perm)
+        off, out = t.SearchBallPosTagged(inv[g["query_ids"]], float(g["ball_r2"]))
+        ref_off = g["ball_offsets"]
+        for j in range(len(g["query_ids"])):
+            got = np.sort(perm[out[off[j]:off[j + 1]]])
+            want = np.sort(g["ball_ids"][ref_off[j]:ref_off[j + 1]])
+            np.testing.assert_array_equal(got, want)
+    g = golden("nonperiodic")
+    t = KDTree(g["pos"], None, g["mass"], int(g["b"]), kerntype=0)
+    inv = np.argsort(t.GetPerm())
+    for j, i in enumerate(g["query_ids"][:10]):
+        mark = np.zeros(len(g["pos"]), np.int32)
+        d2 = np.zeros(len(g["pos"]))
+        t.SearchBallPos(int(inv[i]), float(g["ball_r2"]), 7, mark, d2)
+        np.testing.assert_array_equal(np.where(mark == 7, d2, -1.0), g["mark_d2"][j])
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_ball_vs_oracle(gpu, port_built, periodic):
+    pos, mass = syn.clustered_box(40000, 100.0, seed=11)
+    per = [100.0] * 3 if periodic else None
+    o = oracle.OracleTree(pos, None, mass, 16, 0, 0, 1000, per, backend="port")
+    t = KDTree(pos, None, mass, 16, kerntype=0, period=per)
+    perm = t.GetPerm()
+    inv = np.argsort(perm)
+    ids = np.random.default_rng(12).choice(40000, 300, replace=False)
+    r2 = 4.0
+    off, out = t.SearchBallPosTagged(inv[ids], r2)
+    for j, i in enumerate(ids):
+        np.testing.assert_array_equal(np.sort(perm[out[off[j]:off[j + 1]]]),
+                                      o.ball_tagged(int(i), r2))
+    x = np.random.default_rng(13).random((200, 3)) * 100.0
+    off, out = t.SearchBallPosTaggedPoints(x, r2)
+    for j in range(200):
+        np.testing.assert_array_equal(np.sort(perm[out[off[j]:off[j + 1]]]),
+                                      o.ball_tagged_pos(x[j], r2))
