@@ -1,0 +1,102 @@
+// Hand-written adjoint of the SPH density (no reference counterpart: the reference has
+// no gradients). The forward pass is CalcDensity (KDCalcSmoothQuantities.cxx:203-305):
+//   rho_i = sum_{j in N(i)} w_ij m_j + sum_{l : i in N(l)} w_li m_l,
+//   w_ij  = 0.5 Wsm(q_ij) h_i^-3,  q_ij = r_ij / h_i,  h_i = 0.5 r_{i,K(i)}
+// where K(i) is the farthest of the k neighbours and Wsm interpolates the kernel table.
+// With the neighbour sets and each pair's table cell c frozen at the forward pass, Wsm is
+// linear in q inside the cell: T(q) = T[c] + (T[c+1]-T[c]) (q - c delta) / delta, so
+//   dw/dr = 0.5 h^-4 T'(q),   dw/dh = -0.5 h^-4 (3 T(q) + q T'(q)),   dh_i/dr_iK = 1/2.
+// For L = sum_i w_i log rho_i, with g_i = w_i / rho_i and c_ij = g_i m_j + g_j m_i:
+//   dL/dm_a = sum_{i: a in N(i)} g_i w_ia + sum_{j in N(a)} g_j w_aj
+//   dL/dx_i += c_ij dw/dr (x_i - x_j)/r_ij   (and the opposite on x_j)
+//   dL/dx_i += [sum_j c_ij dw/dh] (1/2) (x_i - x_K)/r_iK   (and the opposite on x_K).
+// The backward kernel recomputes every weight from the saved neighbour lists (4 B per
+// neighbour) instead of storing weights; one thread per particle, FP64 atomics for the
+// contributions that land on other particles.
+#include "nbk_build.h"
+
+namespace nbk {
+
+namespace {
+
+__global__ void __launch_bounds__(128) k_adjoint(TreeView tv, int K, const int* __restrict__ nn,
+                                                 const double* __restrict__ wt,
+                                                 const double* __restrict__ rho,
+                                                 const double* __restrict__ T, int kr,
+                                                 double* gpos, double* gmass) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= tv.n) return;
+  int ti = tv.pstart + i;
+  const int* row = nn + (size_t)i * K;
+  P4 xi = tv.pos[ti];
+  double gi = wt[ti] / rho[ti];
+  // farthest neighbour: the one that set h_i in the forward pass
+  double best = -1.0;
+  int kf = row[0];
+  for (int s = 0; s < K; s++) {
+    P4 xj = tv.pos[row[s]];
+    double d2 = dist2_exact(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z);
+    if (d2 > best) {
+      best = d2;
+      kf = row[s];
+    }
+  }
+  double rk = __dsqrt_rn(best);
+  double hh = 0.5 * rk;
+  double norm = 1.0 / pow(hh, 3.0);
+  double delta = 2.0 / (double)(kr - 1);
+  double A = 0.0, gmi = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
+  for (int s = 0; s < K; s++) {
+    int j = row[s];
+    P4 xj = tv.pos[j];
+    double dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
+    double rij = __dsqrt_rn(dist2_exact(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z));
+    double q = rij / hh;
+    int c = (int)(q * 0.5 * (double)(kr - 1));
+    double Tq = wsm(q, c, kr, delta, T);
+    double Tp = (c < kr - 1) ? (T[c + 1] - T[c]) / delta : 0.0;
+    double w = 0.5 * Tq * norm;
+    double gj = wt[j] / rho[j];
+    double cij = gi * xj.m + gj * xi.m;
+    atomicAdd(&gmass[j], gi * w);
+    gmi += gj * w;
+    double dwdr = 0.5 * norm * Tp / hh;
+    double dwdh = -0.5 * norm / hh * (3.0 * Tq + q * Tp);
+    A += cij * dwdh;
+    double coef = cij * dwdr / rij;
+    gx += coef * dx;
+    gy += coef * dy;
+    gz += coef * dz;
+    atomicAdd(&gpos[3 * (size_t)j + 0], -coef * dx);
+    atomicAdd(&gpos[3 * (size_t)j + 1], -coef * dy);
+    atomicAdd(&gpos[3 * (size_t)j + 2], -coef * dz);
+  }
+  P4 xk = tv.pos[kf];
+  double ch = A * 0.5 / rk;
+  double kx = ch * (xi.x - xk.x), ky = ch * (xi.y - xk.y), kz = ch * (xi.z - xk.z);
+  atomicAdd(&gpos[3 * (size_t)kf + 0], -kx);
+  atomicAdd(&gpos[3 * (size_t)kf + 1], -ky);
+  atomicAdd(&gpos[3 * (size_t)kf + 2], -kz);
+  atomicAdd(&gpos[3 * (size_t)ti + 0], gx + kx);
+  atomicAdd(&gpos[3 * (size_t)ti + 1], gy + ky);
+  atomicAdd(&gpos[3 * (size_t)ti + 2], gz + kz);
+  atomicAdd(&gmass[ti], gmi);
+}
+
+}  // namespace
+
+int run_density_adjoint(const TreeView& tv, int k, const int* d_nn, const double* d_w_tree,
+                        const double* d_rho_tree, const double* kernel, int kernres,
+                        double* d_gpos_tree, double* d_gmass_tree, cudaStream_t st) {
+  if (tv.n == 0) return NBK_OK;
+  NBK_CUDA_TRY(cudaMemsetAsync(d_gpos_tree, 0, sizeof(double) * 3 * tv.n, st));
+  NBK_CUDA_TRY(cudaMemsetAsync(d_gmass_tree, 0, sizeof(double) * tv.n, st));
+  Phase ph("adjoint_backward", st);
+  k_adjoint<<<(tv.n + 127) / 128, 128, 0, st>>>(tv, k, d_nn, d_w_tree, d_rho_tree, kernel, kernres,
+                                                d_gpos_tree, d_gmass_tree);
+  note_launch();
+  NBK_CUDA_TRY(cudaGetLastError());
+  return NBK_OK;
+}
+
+}  // namespace nbk

@@ -108,8 +108,12 @@ __global__ void __launch_bounds__(32 * kWpb) k_ball(BallArgs a) {
                 double d2 = dist2_exact(xq[0], xq[1], xq[2], c.x, c.y, c.z);
                 if (d2 < a.r2) {
                   if (FILL) {
-                    a.out[base + cnt] = ti;
-                    if (a.outd2) a.outd2[base + cnt] = d2;
+                    if (base + cnt < a.offsets[q + 1]) {
+                      a.out[base + cnt] = ti;
+                      if (a.outd2) a.outd2[base + cnt] = d2;
+                    } else {
+                      atomicExch(a.err, kErrCapacity);  // fill disagrees with count
+                    }
                   }
                   cnt++;
                 }

@@ -430,7 +430,7 @@ __global__ void __launch_bounds__(kThreads) k_local_build(
     const LRoot* __restrict__ roots, const double* Xa, const double* Ya, const double* Za,
     const int* IDa, const double* Xb, const double* Yb, const double* Zb, const int* IDb,
     const double* __restrict__ mass_in, const double* __restrict__ vel_in, int b,
-    NodeRec* node, NodeX* nodex, P4* pos, float4* posf, V4* vel, int* perm) {
+    NodeRec* node, NodeX* nodex, P4* pos, float4* posf, V4* vel, int* perm, int* err) {
   extern __shared__ __align__(16) unsigned char smem[];
   double* cx = (double*)smem;
   double* cy = cx + kLocalMax;
@@ -541,7 +541,8 @@ __global__ void __launch_bounds__(kThreads) k_local_build(
         for (int t = threadIdx.x; t < total; t += kThreads) {
           int u = t ^ jj;
           if (u > t) {
-            bool up = (t & kk) == 0;
+            // direction from the position inside the P-segment: every segment ascending
+            bool up = ((t & (P - 1)) & kk) == 0;
             unsigned long long a = skey[t], c = skey[u];
             unsigned short ia = sidx[t], ic = sidx[u];
             bool gt = (a > c) || (a == c && ia > ic);
@@ -560,7 +561,14 @@ __global__ void __launch_bounds__(kThreads) k_local_build(
     for (int t = threadIdx.x; t < total; t += kThreads) {
       int j = t / P, r = t - j * P;
       LNode nd = lv2[j];
-      if (r < nd.size) src[nd.start + r] = sidx[t];
+      if (r < nd.size) {
+        unsigned short sx = sidx[t];
+        if (sx >= R.size) {  // a padding slot inside the node: report, keep in bounds
+          atomicExch(err, 3);
+          sx = (unsigned short)(nd.start + r);
+        }
+        src[nd.start + r] = sx;
+      }
     }
     __syncthreads();
     double* tmp = (double*)skey;  // keys are no longer needed
@@ -765,7 +773,7 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
     }
     k_local_build<<<(unsigned)lroots.size(), kThreads, sm, st>>>(
         d_r, Xa, Ya, Za, IDa, Xb, Yb, Zb, IDb, d_mass_in, d_vel_in, b, out.node, out.nodex,
-        out.pos, out.posf, out.vel, out.perm); note_launch();
+        out.pos, out.posf, out.vel, out.perm, d_err); note_launch();
     NBK_CUDA_TRY(cudaGetLastError());
   }
   int h_err = 0;
@@ -777,7 +785,7 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
     return NBK_ERR_INVALID;
   }
   if (h_err) {
-    set_error("tree build: median partition inconsistent (device check)");
+    set_error("tree build: partition inconsistent (device check, code " + std::to_string(h_err) + ")");
     return NBK_ERR_DEVICE;
   }
   return NBK_OK;

@@ -78,6 +78,11 @@ __global__ void k_scatter_d(const double* tv, const int* perm, double* out, int6
   int64_t o = perm[i];
   for (int s = 0; s < stride; s++) out[o * stride + s] = tv[i * stride + s];
 }
+__global__ void k_gather_d(const double* in, const int* perm, double* out, int64_t n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  out[i] = in[perm[i]];
+}
 __global__ void k_scatter_i(const int* tv, const int* perm, int* out, int64_t n) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -863,14 +868,53 @@ int nbk_fof_criterion(nbk_tree* t, int comparator, const double* params, int32_t
 
 int nbk_density_adjoint(nbk_tree* t, int k, const double* w, double* rho, double* grad_pos,
                         double* grad_mass) {
-  (void)k;
-  (void)w;
-  (void)rho;
-  (void)grad_pos;
-  (void)grad_mass;
+  API_BEGIN
   NBK_TRY(check_tree(t));
-  set_error("nbk_density_adjoint: not yet available");
-  return NBK_ERR_UNSUPPORTED;
+  if (!w || !rho || !grad_pos || !grad_mass || k < 1) {
+    set_error("nbk_density_adjoint: invalid argument");
+    return NBK_ERR_INVALID;
+  }
+  if (k > t->n - 1) {
+    set_error("nbk_density_adjoint: k exceeds the number of other particles");
+    return NBK_ERR_TOO_FEW;
+  }
+  Stage S(t);
+  const double* dw;
+  double *drho, *dgp, *dgm;
+  NBK_TRY(S.in(w, t->n, &dw));
+  NBK_TRY(S.out(rho, t->n, &drho));
+  NBK_TRY(S.out(grad_pos, 3 * t->n, &dgp));
+  NBK_TRY(S.out(grad_mass, t->n, &dgm));
+  int* nn;
+  double *trho, *tw, *tgp, *tgm;
+  NBK_TRY(S.alloc.get((void**)&nn, sizeof(int) * t->n * k));
+  NBK_TRY(S.alloc.get((void**)&trho, sizeof(double) * t->n));
+  NBK_TRY(S.alloc.get((void**)&tw, sizeof(double) * t->n));
+  NBK_TRY(S.alloc.get((void**)&tgp, sizeof(double) * 3 * t->n));
+  NBK_TRY(S.alloc.get((void**)&tgm, sizeof(double) * t->n));
+  NBK_CUDA_TRY(cudaMemsetAsync(trho, 0, sizeof(double) * t->n, t->st));
+  NBK_TRY(clear_err(t));
+  // forward: CalcDensity, keeping each particle's neighbour list
+  KnnArgs a = base_args(t);
+  a.tv.periodic = 0;
+  a.kheap = k;
+  a.kout = k;
+  a.exclude_self = 1;
+  a.qmode = 0;
+  a.nq = (int)t->n;
+  a.rho = trho;
+  a.nn = nn;
+  NBK_TRY(launch_knn(a, kEpiDensSave, t->st));
+  k_gather_d<<<(unsigned)((t->n + 255) / 256), 256, 0, t->st>>>(dw, t->arr.perm, tw, t->n);
+  note_launch();
+  NBK_TRY(run_density_adjoint(a.tv, k, nn, tw, trho, t->d_kernel, t->kernres, tgp, tgm, t->st));
+  NBK_TRY(scatter_to_input_order(trho, t->arr.perm, drho, t->n, 1, t->st));
+  NBK_TRY(scatter_to_input_order(tgp, t->arr.perm, dgp, t->n, 3, t->st));
+  NBK_TRY(scatter_to_input_order(tgm, t->arr.perm, dgm, t->n, 1, t->st));
+  NBK_TRY(S.finish());
+  if (!t->dev()) NBK_TRY(check_err(t, "nbk_density_adjoint"));
+  return NBK_OK;
+  API_END
 }
 
 int nbk_batch_create(const double*, const double*, const int64_t*, int64_t, int, int, int,

@@ -82,6 +82,9 @@ def _lib(backend: str) -> ctypes.CDLL:
                                                  _c_dbl_p, _c_dbl_p, _c_dbl_p, _c_dbl_p])
         sig["density_frozen"] = (ctypes.c_int, [vp, ctypes.c_int, _c_int_p, _c_dbl_p, _c_dbl_p,
                                                 _c_dbl_p, _c_dbl_p])
+        sig["adj_create"] = (vp, [vp, ctypes.c_int, _c_int_p, _c_dbl_p, _c_dbl_p, _c_dbl_p])
+        sig["adj_fd"] = (ctypes.c_double, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double])
+        sig["adj_destroy"] = (None, [vp])
     else:
         sig["knn_pos"] = (ctypes.c_int, [vp, _c_dbl_p, ctypes.c_int, ctypes.c_int, _c_int_p,
                                          _c_dbl_p])
@@ -245,6 +248,19 @@ class OracleTree:
         self._f("density_adjoint")(self._h, k, _ip(nn_ids), _dp(pos), _dp(mass), _dp(w), _dp(rho),
                                    _dp(gp), _dp(gm))
         return rho, gp, gm
+
+    def local_fd(self, k, nn_ids, weights, coords, step=1e-6, mass=None):
+        """Central finite differences dL/dpos[a, d] for every (a, d) in coords, on the
+        frozen model, differencing only the affected loss terms."""
+        mass = self.mass if mass is None else np.ascontiguousarray(mass, np.float64)
+        nn_ids = np.ascontiguousarray(nn_ids, np.int32)
+        w = np.ascontiguousarray(weights, np.float64)
+        ctx = self._f("adj_create")(self._h, k, _ip(nn_ids), _dp(self.pos), _dp(mass), _dp(w))
+        try:
+            return np.array([self._f("adj_fd")(ctx, int(a), int(d), float(step))
+                             for a, d in coords])
+        finally:
+            self._f("adj_destroy")(ctx)
 
     def density_frozen(self, k, nn_ids, pos0, pos, mass=None):
         mass = self.mass if mass is None else np.ascontiguousarray(mass, np.float64)

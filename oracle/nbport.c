@@ -1277,3 +1277,146 @@ int pt_density_adjoint(PTree* t, int k, const int* nn, const double* pos, const 
     free(cell);
     return 0;
 }
+
+/* ---------------------------------------------------------------- local finite differences */
+/* Central finite difference of L = sum_i w_i log rho_i with respect to one coordinate,
+   restricted to the loss terms that coordinate can change, on the frozen model above.
+   Moving particle a changes w_aj (j in N(a)), w_la (a in N(l)) and h_l for every l whose
+   farthest neighbour is a; the affected densities are those of a, N(a), the l's, and
+   N(l) for those l. Differencing only these terms avoids the cancellation of a sum over
+   every particle. */
+typedef struct {
+    PTree* t;
+    int n, k;
+    const int* nn;
+    double* pos;
+    const double* mass;
+    const double* w;
+    int* kfar;
+    int* cell;
+    int *rev_off, *rev_l, *rev_s; /* (l, slot) pairs with nn[l][slot] = i */
+    int *kf_off, *kf_l;           /* l with farthest neighbour = i */
+    int* mark;
+    int* list;
+} AdjCtx;
+
+void* pt_adj_create(PTree* t, int k, const int* nn, const double* pos0, const double* mass,
+                    const double* w) {
+    int n = t->n;
+    AdjCtx* c = (AdjCtx*)calloc(1, sizeof(AdjCtx));
+    c->t = t;
+    c->n = n;
+    c->k = k;
+    c->nn = nn;
+    c->mass = mass;
+    c->w = w;
+    c->pos = (double*)malloc(sizeof(double) * 3 * (size_t)n);
+    memcpy(c->pos, pos0, sizeof(double) * 3 * (size_t)n);
+    c->kfar = (int*)malloc(sizeof(int) * n);
+    c->cell = (int*)malloc(sizeof(int) * (size_t)n * k);
+    frozen_setup(t, k, nn, pos0, c->kfar, c->cell);
+    c->rev_off = (int*)calloc((size_t)n + 1, sizeof(int));
+    c->kf_off = (int*)calloc((size_t)n + 1, sizeof(int));
+    for (size_t e = 0; e < (size_t)n * k; e++) c->rev_off[nn[e] + 1]++;
+    for (int i = 0; i < n; i++) c->kf_off[nn[(size_t)i * k + c->kfar[i]] + 1]++;
+    for (int i = 0; i < n; i++) {
+        c->rev_off[i + 1] += c->rev_off[i];
+        c->kf_off[i + 1] += c->kf_off[i];
+    }
+    c->rev_l = (int*)malloc(sizeof(int) * (size_t)n * k);
+    c->rev_s = (int*)malloc(sizeof(int) * (size_t)n * k);
+    c->kf_l = (int*)malloc(sizeof(int) * n);
+    int* fill = (int*)calloc((size_t)n, sizeof(int));
+    for (int l = 0; l < n; l++)
+        for (int s = 0; s < k; s++) {
+            int i = nn[(size_t)l * k + s];
+            int p = c->rev_off[i] + fill[i]++;
+            c->rev_l[p] = l;
+            c->rev_s[p] = s;
+        }
+    memset(fill, 0, sizeof(int) * n);
+    for (int l = 0; l < n; l++) {
+        int a = nn[(size_t)l * k + c->kfar[l]];
+        c->kf_l[c->kf_off[a] + fill[a]++] = l;
+    }
+    free(fill);
+    c->mark = (int*)calloc((size_t)n, sizeof(int));
+    c->list = (int*)malloc(sizeof(int) * (size_t)n);
+    return c;
+}
+
+void pt_adj_destroy(void* h) {
+    AdjCtx* c = (AdjCtx*)h;
+    if (!c) return;
+    free(c->pos);
+    free(c->kfar);
+    free(c->cell);
+    free(c->rev_off);
+    free(c->rev_l);
+    free(c->rev_s);
+    free(c->kf_off);
+    free(c->kf_l);
+    free(c->mark);
+    free(c->list);
+    free(c);
+}
+
+static double adj_h(const AdjCtx* c, int l) {
+    const double* xl = c->pos + 3 * (size_t)l;
+    int kf = c->nn[(size_t)l * c->k + c->kfar[l]];
+    return 0.5 * sqrt(dist2_n(xl, c->pos + 3 * (size_t)kf, 3));
+}
+
+static double adj_w(const AdjCtx* c, int l, int s, double hl) {
+    int j = c->nn[(size_t)l * c->k + s];
+    double r = sqrt(dist2_n(c->pos + 3 * (size_t)l, c->pos + 3 * (size_t)j, 3));
+    double delta = 2.0 / (double)(c->t->kernres - 1);
+    double T = table_val(c->t, c->cell[(size_t)l * c->k + s], r / hl, delta);
+    return 0.5 * T / pow(hl, 3.0);
+}
+
+static double adj_rho(const AdjCtx* c, int i) {
+    double rho = 0, hi = adj_h(c, i);
+    for (int s = 0; s < c->k; s++) rho += adj_w(c, i, s, hi) * c->mass[c->nn[(size_t)i * c->k + s]];
+    for (int p = c->rev_off[i]; p < c->rev_off[i + 1]; p++) {
+        int l = c->rev_l[p];
+        rho += adj_w(c, l, c->rev_s[p], adj_h(c, l)) * c->mass[l];
+    }
+    return rho;
+}
+
+double pt_adj_fd(void* h, int a, int d, double step) {
+    AdjCtx* c = (AdjCtx*)h;
+    int cnt = 0;
+#define ADD(x)                         \
+    do {                               \
+        int _x = (x);                  \
+        if (!c->mark[_x]) {            \
+            c->mark[_x] = 1;           \
+            c->list[cnt++] = _x;       \
+        }                              \
+    } while (0)
+    ADD(a);
+    for (int s = 0; s < c->k; s++) ADD(c->nn[(size_t)a * c->k + s]);
+    for (int p = c->rev_off[a]; p < c->rev_off[a + 1]; p++) ADD(c->rev_l[p]);
+    for (int p = c->kf_off[a]; p < c->kf_off[a + 1]; p++) {
+        int l = c->kf_l[p];
+        ADD(l);
+        for (int s = 0; s < c->k; s++) ADD(c->nn[(size_t)l * c->k + s]);
+    }
+#undef ADD
+    double x0 = c->pos[3 * (size_t)a + d];
+    double sum = 0;
+    double* rp = (double*)malloc(sizeof(double) * cnt);
+    c->pos[3 * (size_t)a + d] = x0 + step;
+    for (int q = 0; q < cnt; q++) rp[q] = adj_rho(c, c->list[q]);
+    c->pos[3 * (size_t)a + d] = x0 - step;
+    for (int q = 0; q < cnt; q++) {
+        double rm = adj_rho(c, c->list[q]);
+        sum += c->w[c->list[q]] * log1p((rp[q] - rm) / rm);
+    }
+    c->pos[3 * (size_t)a + d] = x0;
+    for (int q = 0; q < cnt; q++) c->mark[c->list[q]] = 0;
+    free(rp);
+    return sum / (2 * step);
+}

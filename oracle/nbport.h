@@ -58,6 +58,12 @@ int pt_density_adjoint(PTree* t, int k, const int* nn_ids, const double* pos,
    evaluated at positions pos; used by the finite-difference check. */
 int pt_density_frozen(PTree* t, int k, const int* nn_ids, const double* pos0,
                       const double* pos, const double* mass, double* rho_out);
+/* Central finite difference dL/dpos[a][d] of the frozen model, differencing only the
+   loss terms that coordinate changes. The context keeps pointers to nn_ids, mass, w. */
+void* pt_adj_create(PTree* t, int k, const int* nn_ids, const double* pos0,
+                    const double* mass, const double* w);
+double pt_adj_fd(void* ctx, int a, int d, double step);
+void pt_adj_destroy(void* ctx);
 
 #ifdef __cplusplus
 }
