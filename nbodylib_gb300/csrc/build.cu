@@ -161,7 +161,7 @@ __device__ void write_node(NodeRec* node, NodeX* nodex, int idx, const double lo
 
 // DetermineSplitDim (KDTree.cxx:459-504): spread = max - min per dimension in FP64, the
 // first strictly larger spread wins.
-__global__ void k_gnode_split(GNode* g, int ng, NodeRec* node, NodeX* nodex) {
+__global__ void k_gnode_split(GNode* g, int ng, NodeRec* node, NodeX* nodex, int p0) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= ng) return;
   GNode s = g[i];
@@ -188,7 +188,7 @@ __global__ void k_gnode_split(GNode* g, int ng, NodeRec* node, NodeX* nodex) {
   s.first_diff = x ? 63 - __clzll((long long)x) : -1;
   g[i] = s;
   // the split value is written once the median key is known (k_chunk_scan)
-  write_node(node, nodex, s.node, lo, hi, s.start, s.size, dim, 0.0);
+  write_node(node, nodex, s.node, lo, hi, p0 + s.start, s.size, dim, 0.0);
 }
 
 __global__ void __launch_bounds__(kThreads) k_hist(const Chunk* __restrict__ chunks,
@@ -430,7 +430,7 @@ __global__ void __launch_bounds__(kThreads) k_local_build(
     const LRoot* __restrict__ roots, const double* Xa, const double* Ya, const double* Za,
     const int* IDa, const double* Xb, const double* Yb, const double* Zb, const int* IDb,
     const double* __restrict__ mass_in, const double* __restrict__ vel_in, int b,
-    NodeRec* node, NodeX* nodex, P4* pos, float4* posf, V4* vel, int* perm, int* err) {
+    NodeRec* node, NodeX* nodex, P4* pos, float4* posf, V4* vel, int* perm, int* err, int p0) {
   extern __shared__ __align__(16) unsigned char smem[];
   double* cx = (double*)smem;
   double* cy = cx + kLocalMax;
@@ -496,7 +496,8 @@ __global__ void __launch_bounds__(kThreads) k_local_build(
           }
         }
         lv[j].dim = dim;
-        write_node(node, nodex, R.nbase + nd.h, lo, hi, R.start + nd.start, nd.size, dim, 0.0);
+        write_node(node, nodex, R.nbase + nd.h, lo, hi, p0 + R.start + nd.start, nd.size, dim,
+                   0.0);
       }
     }
     if (threadIdx.x == 0) {
@@ -606,8 +607,8 @@ __global__ void __launch_bounds__(kThreads) k_local_build(
   }
   // final tree-order arrays
   for (int e = threadIdx.x; e < R.size; e += kThreads) {
-    int t = R.start + e;
-    int ii = id[e];
+    int t = p0 + R.start + e;  // absolute tree index
+    int ii = p0 + id[e];  // absolute input index
     double m = mass_in ? mass_in[ii] : 1.0;
     P4 p;
     p.x = cx[e];
@@ -655,8 +656,13 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
                  const double* d_mass_in, const double* d_vel_in, BuiltArrays& out,
                  DevAlloc& alloc, cudaStream_t st) {
   Phase ph("build", st);
-  int64_t ntot = 0;
-  for (auto& t : trees) ntot = std::max<int64_t>(ntot, t.pstart + t.n);
+  // internal buffers cover only [p0, p0 + ntot), the particles of these trees
+  int64_t p0 = trees.empty() ? 0 : trees[0].pstart, pend = 0;
+  for (auto& t : trees) {
+    p0 = std::min<int64_t>(p0, t.pstart);
+    pend = std::max<int64_t>(pend, t.pstart + t.n);
+  }
+  int64_t ntot = pend - p0;
   if (ntot == 0) return NBK_OK;
   double *Xa, *Ya, *Za, *Xb, *Yb, *Zb;
   int *IDa, *IDb, *d_err;
@@ -670,7 +676,8 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
   NBK_TRY(alloc.get((void**)&IDb, sizeof(int) * ntot));
   NBK_TRY(alloc.get((void**)&d_err, sizeof(int)));
   NBK_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
-  k_init_soa<<<(unsigned)((ntot + 255) / 256), 256, 0, st>>>(d_pos_in, Xa, Ya, Za, IDa, ntot, d_err); note_launch();
+  k_init_soa<<<(unsigned)((ntot + 255) / 256), 256, 0, st>>>(d_pos_in + 3 * p0, Xa, Ya, Za, IDa, ntot,
+                                                            d_err); note_launch();
   NBK_CUDA_TRY(cudaGetLastError());
 
   // host plan of the global levels and of the local subtree roots
@@ -682,8 +689,8 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
   std::vector<HN> cur, nxt;
   for (auto& t : trees) {
     if (t.n <= 0) continue;
-    if (t.n <= kLocalMax) lroots.push_back({(int)t.pstart, (int)t.n, t.nbase, 0, 0, 0});
-    else cur.push_back({t.pstart, t.n, 0, t.nbase});
+    if (t.n <= kLocalMax) lroots.push_back({(int)(t.pstart - p0), (int)t.n, t.nbase, 0, 0, 0});
+    else cur.push_back({t.pstart - p0, t.n, 0, t.nbase});
   }
   int buf = 0;  // buffer holding the current level's particles
   std::vector<GNode> gn;
@@ -737,7 +744,7 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
     int* I2 = buf ? IDa : IDb;
     k_gnode_reset<<<(ng + 127) / 128, 128, 0, st>>>(d_g, ng); note_launch();
     k_bbox<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z); note_launch();
-    k_gnode_split<<<(ng + 127) / 128, 128, 0, st>>>(d_g, ng, out.node, out.nodex); note_launch();
+    k_gnode_split<<<(ng + 127) / 128, 128, 0, st>>>(d_g, ng, out.node, out.nodex, (int)p0); note_launch();
     for (int pass = 0; pass < 8; pass++) {
       int shift = 56 - 8 * pass;
       k_hist<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, d_hist, shift); note_launch();
@@ -773,7 +780,7 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
     }
     k_local_build<<<(unsigned)lroots.size(), kThreads, sm, st>>>(
         d_r, Xa, Ya, Za, IDa, Xb, Yb, Zb, IDb, d_mass_in, d_vel_in, b, out.node, out.nodex,
-        out.pos, out.posf, out.vel, out.perm, d_err); note_launch();
+        out.pos, out.posf, out.vel, out.perm, d_err, (int)p0); note_launch();
     NBK_CUDA_TRY(cudaGetLastError());
   }
   int h_err = 0;

@@ -48,6 +48,8 @@ double w_epan(double r, double h) {
   return rh <= 1.0 ? (1.0 - rh * rh) : 0.;
 }
 
+}  // namespace
+
 // KDTree::KernelConstruction (KDTree.cxx:1144-1183) for ND dimensions; Gamma(ND/2+1)
 // from std::tgamma.
 void kernel_table(int kerntype, int kernres, int nd, std::vector<double>& T, double& norm) {
@@ -70,6 +72,8 @@ void kernel_table(int kerntype, int kernres, int nd, std::vector<double>& T, dou
   T.resize(kernres);
   for (int i = 0; i < kernres; i++) T[i] = kn * f(i * delta, 1.0);
 }
+
+namespace {
 
 __global__ void k_scatter_d(const double* tv, const int* perm, double* out, int64_t n,
                             int stride) {
@@ -128,6 +132,8 @@ void resolve_pending() {
 
 Phase::Phase(const char* n, cudaStream_t s) : name(n), st(s) {
   if (!g_trace_on.load(std::memory_order_relaxed)) return;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
   cudaEventCreate(&a);
   cudaEventCreate(&b);
   cudaEventRecord(a, st);
@@ -917,15 +923,6 @@ int nbk_density_adjoint(nbk_tree* t, int k, const double* w, double* rho, double
   API_END
 }
 
-int nbk_batch_create(const double*, const double*, const int64_t*, int64_t, int, int, int,
-                     unsigned, nbk_batch** out) {
-  if (out) *out = nullptr;
-  set_error("batched path not yet available");
-  return NBK_ERR_UNSUPPORTED;
-}
-int nbk_batch_destroy(nbk_batch*) { return NBK_OK; }
-int nbk_batch_set_stream(nbk_batch*, void*) { return NBK_ERR_UNSUPPORTED; }
-int nbk_batch_density(nbk_batch*, int, double*, int) { return NBK_ERR_UNSUPPORTED; }
-int nbk_batch_density_pertree(nbk_batch*, int, double*) { return NBK_ERR_UNSUPPORTED; }
+
 
 }  // extern "C"

@@ -17,6 +17,8 @@
 // the FP64 test would accept; a candidate that survives is tested in FP64 with the
 // reference's arithmetic, d2 = ((dx*dx + dy*dy) + dz*dz), and accepted when d2 < top
 // (strict, as the reference's `dist2 < pq->TopPriority()`).
+#include <algorithm>
+
 #include "nbk_build.h"
 
 namespace nbk {
@@ -145,36 +147,12 @@ __device__ void traverse(const TreeView& tv, WarpSmem<KMAX>& w, int lane, bool a
   }
 }
 
+// One warp's work: up to 32 queries of one tree (lane = query). `qslot` indexes the
+// per-query outputs, `self` is the query's tree index (-1 for a coordinate query), K the
+// heap size. All lanes of the warp call this together.
 template <int KMAX, int EPI>
-__global__ void __launch_bounds__(32 * (KMAX <= 32 ? 8 : (KMAX <= 64 ? 4 : 2)))
-    k_knn(KnnArgs a) {
-  constexpr int WPB = KMAX <= 32 ? 8 : (KMAX <= 64 ? 4 : 2);
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  WarpSmem<KMAX>* ws = reinterpret_cast<WarpSmem<KMAX>*>(smem_raw);
-  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  WarpSmem<KMAX>& w = ws[warp];
-  int gw = blockIdx.x * WPB + warp;
-  int qi = gw * 32 + lane;  // query slot
-  if (gw * 32 >= a.nq) return;
-  const TreeView& tv = a.tv;
-  bool valid = qi < a.nq;
-  int self = -1;
-  double x0[3] = {0, 0, 0};
-  if (valid) {
-    if (a.qmode == 0) self = a.q0 + qi;
-    else if (a.qmode == 2) self = a.qidx[qi];
-    if (a.qmode == 1) {
-      x0[0] = a.qx[3 * (size_t)qi];
-      x0[1] = a.qx[3 * (size_t)qi + 1];
-      x0[2] = a.qx[3 * (size_t)qi + 2];
-    } else {
-      P4 p = tv.pos[self];
-      x0[0] = p.x;
-      x0[1] = p.y;
-      x0[2] = p.z;
-    }
-  }
-  const int K = a.kheap;
+__device__ void run_warp(const KnnArgs& a, const TreeView& tv, WarpSmem<KMAX>& w, int lane,
+                         bool valid, int qi, int self, const double x0[3], int K) {
   for (int s = 0; s < K; s++) {
     w.hd[s][lane] = kMaxValue;
     w.hi[s][lane] = -1;
@@ -290,9 +268,74 @@ __global__ void __launch_bounds__(32 * (KMAX <= 32 ? 8 : (KMAX <= 64 ? 4 : 2)))
   }
 }
 
+template <int KMAX>
+constexpr int warps_per_block() {
+  return KMAX <= 32 ? 8 : (KMAX <= 64 ? 4 : 2);
+}
+
+template <int KMAX, int EPI>
+__global__ void __launch_bounds__(32 * warps_per_block<KMAX>()) k_knn(KnnArgs a) {
+  constexpr int WPB = warps_per_block<KMAX>();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  WarpSmem<KMAX>* ws = reinterpret_cast<WarpSmem<KMAX>*>(smem_raw);
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int gw = blockIdx.x * WPB + warp;
+  int qi = gw * 32 + lane;  // query slot
+  if (gw * 32 >= a.nq) return;
+  const TreeView& tv = a.tv;
+  bool valid = qi < a.nq;
+  int self = -1;
+  double x0[3] = {0, 0, 0};
+  if (valid) {
+    if (a.qmode == 0) self = a.q0 + qi;
+    else if (a.qmode == 2) self = a.qidx[qi];
+    if (a.qmode == 1) {
+      x0[0] = a.qx[3 * (size_t)qi];
+      x0[1] = a.qx[3 * (size_t)qi + 1];
+      x0[2] = a.qx[3 * (size_t)qi + 2];
+    } else {
+      P4 p = tv.pos[self];
+      x0[0] = p.x;
+      x0[1] = p.y;
+      x0[2] = p.z;
+    }
+  }
+  run_warp<KMAX, EPI>(a, tv, ws[warp], lane, valid, qi, self, x0, a.kheap);
+}
+
+// Batched density: a persistent grid whose warps pull (tree, query bucket) work items
+// from an atomic counter until the list is exhausted; every tree is searched with its
+// own k = min(k, n_tree - 1). The loop is bounded by the item count.
+template <int KMAX>
+__global__ void __launch_bounds__(32 * warps_per_block<KMAX>()) k_knn_batch(KnnArgs a, BatchArgs b) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  WarpSmem<KMAX>* ws = reinterpret_cast<WarpSmem<KMAX>*>(smem_raw);
+  int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int guard = 0; guard < b.nitems + 1; guard++) {
+    int item = 0;
+    if (lane == 0) item = atomicAdd(b.counter, 1);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= b.nitems) break;
+    WorkItem it = b.items[item];
+    TreeInfo ti = b.trees[it.tree];
+    TreeView tv = a.tv;
+    tv.n = ti.n;
+    tv.pstart = ti.pstart;
+    tv.nbase = ti.nbase;
+    int K = min(a.kheap, ti.n - 1);
+    if (K < 1) continue;
+    bool valid = lane < it.count;
+    int self = ti.pstart + it.q0 + (valid ? lane : 0);
+    P4 p = tv.pos[self];
+    double x0[3] = {p.x, p.y, p.z};
+    run_warp<KMAX, kEpiDensity>(a, tv, ws[warp], lane, valid, self, self, x0, K);
+    __syncwarp();
+  }
+}
+
 template <int KMAX, int EPI>
 int launch_t(const KnnArgs& a, cudaStream_t st) {
-  constexpr int WPB = KMAX <= 32 ? 8 : (KMAX <= 64 ? 4 : 2);
+  constexpr int WPB = warps_per_block<KMAX>();
   size_t sm = sizeof(WarpSmem<KMAX>) * WPB;
   static bool set = false;
   if (!set) {
@@ -321,7 +364,38 @@ int launch_e(const KnnArgs& a, cudaStream_t st) {
   return NBK_ERR_UNSUPPORTED;
 }
 
+template <int KMAX>
+int launch_batch_t(const KnnArgs& a, const BatchArgs& b, cudaStream_t st) {
+  constexpr int WPB = warps_per_block<KMAX>();
+  size_t sm = sizeof(WarpSmem<KMAX>) * WPB;
+  static int grid = 0;
+  if (grid == 0) {
+    NBK_CUDA_TRY(cudaFuncSetAttribute(k_knn_batch<KMAX>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    int dev = 0, nsm = 0, per = 0;
+    NBK_CUDA_TRY(cudaGetDevice(&dev));
+    NBK_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    NBK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_knn_batch<KMAX>, 32 * WPB, sm));
+    grid = nsm * (per > 0 ? per : 1);
+  }
+  int blocks = std::min(grid, (b.nitems + WPB - 1) / WPB);
+  if (blocks <= 0) return NBK_OK;
+  Phase ph("knn_density_batch", st);
+  k_knn_batch<KMAX><<<blocks, 32 * WPB, sm, st>>>(a, b); note_launch();
+  NBK_CUDA_TRY(cudaGetLastError());
+  return NBK_OK;
+}
+
 }  // namespace
+
+int launch_knn_batch(const KnnArgs& a, const BatchArgs& b, cudaStream_t st) {
+  if (a.kheap <= 16) return launch_batch_t<16>(a, b, st);
+  if (a.kheap <= 33) return launch_batch_t<33>(a, b, st);
+  if (a.kheap <= 65) return launch_batch_t<65>(a, b, st);
+  if (a.kheap <= 128) return launch_batch_t<128>(a, b, st);
+  set_error("k larger than 127 is not supported by the GPU kNN kernels");
+  return NBK_ERR_UNSUPPORTED;
+}
 
 int launch_knn(const KnnArgs& a, int epi, cudaStream_t st) {
   switch (epi) {

@@ -90,6 +90,22 @@ struct KnnArgs {
 };
 int launch_knn(const KnnArgs& a, int epi, cudaStream_t st);
 
+// ---- batched path: many trees, one persistent launch
+struct WorkItem {
+  int tree, q0, count, pad;  // queries [q0, q0+count) of tree `tree`
+};
+struct TreeInfo {
+  int pstart, n, nbase, pad;
+};
+struct BatchArgs {
+  const WorkItem* items;
+  const TreeInfo* trees;
+  int nitems;
+  int* counter;  // zeroed before each launch
+};
+// Density of every particle of every tree (a.kheap = k, clamped per tree to n-1).
+int launch_knn_batch(const KnnArgs& a, const BatchArgs& b, cudaStream_t st);
+
 // ---- FOF / ball / adjoint
 struct FofArgs {
   TreeView tv;
@@ -112,6 +128,8 @@ int run_ball_mark(const TreeView& tv, int target, double fdist2, int imark, int*
 int run_density_adjoint(const TreeView& tv, int k, const int* d_nn, const double* d_w_tree,
                         const double* d_rho_tree, const double* kernel, int kernres,
                         double* d_gpos_tree, double* d_gmass_tree, cudaStream_t st);
+
+void kernel_table(int kerntype, int kernres, int nd, std::vector<double>& T, double& norm);
 
 // permutation helpers
 int scatter_to_input_order(const double* tree_vals, const int* perm, double* out, int64_t n,

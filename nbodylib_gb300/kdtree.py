@@ -242,3 +242,66 @@ class KDTree:
         _capi.check(self._lib.nbk_density_adjoint(self._h, k, _ptr(w), _ptr(rho), _ptr(gp),
                                                   _ptr(gm)))
         return rho, gp, gm
+
+
+class BatchedDensity:
+    """Many independent per-group trees built and searched together (nbk_batch_*).
+
+    pos: (N, 3), mass: (N,), offsets: (G+1,) CSR over groups (host arrays, or torch CUDA
+    tensors with device=True). bucket_size <= 0 selects the autotuned leaf size.
+    """
+
+    def __init__(self, pos, mass, offsets, bucket_size=0, kerntype=KSPH, kernres=1000,
+                 device=False):
+        self._lib = _capi.load()
+        self.device = device
+        if device:
+            import torch
+            self._torch = torch
+            args = (pos.contiguous(), None if mass is None else mass.contiguous(),
+                    offsets.to(torch.int64).contiguous())
+        else:
+            args = (np.ascontiguousarray(pos, np.float64).reshape(-1, 3),
+                    None if mass is None else np.ascontiguousarray(mass, np.float64),
+                    np.ascontiguousarray(offsets, np.int64))
+        self._keep = args
+        self.n = int(args[2][-1])
+        self.ngroups = len(args[2]) - 1
+        h = ctypes.c_void_p()
+        _capi.check(self._lib.nbk_batch_create(_ptr(args[0]), _ptr(args[1]), _ptr(args[2]),
+                                               self.ngroups, bucket_size, kerntype, kernres,
+                                               DEVICE_PTRS if device else 0, ctypes.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.nbk_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self):
+        b, q = ctypes.c_int32(), ctypes.c_int32()
+        buf = ctypes.create_string_buffer(1 << 14)
+        _capi.check(self._lib.nbk_batch_get_params(self._h, ctypes.byref(b), ctypes.byref(q),
+                                                   buf, len(buf)))
+        return b.value, q.value, buf.value.decode()
+
+    def _out(self):
+        if self.device:
+            return self._torch.empty(self.n, dtype=self._torch.float64, device="cuda")
+        return np.empty(self.n)
+
+    def density(self, k=32, use_graph=True, out=None):
+        rho = self._out() if out is None else out
+        _capi.check(self._lib.nbk_batch_density(self._h, k, _ptr(rho), 1 if use_graph else 0))
+        return rho
+
+    def density_pertree(self, k=32, out=None):
+        rho = self._out() if out is None else out
+        _capi.check(self._lib.nbk_batch_density_pertree(self._h, k, _ptr(rho)))
+        return rho

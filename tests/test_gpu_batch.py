@@ -1,0 +1,47 @@
+"""GPU batched path: many per-group trees, one persistent density launch (optionally a
+replayed CUDA graph), autotuned leaf / query-bucket sizes; checked per group against the
+oracle's KDTree(group) + CalcDensity(min(k, n-1)) and against the per-tree loop."""
+import numpy as np
+import pytest
+
+import oracle
+from nbodylib_gb300 import BatchedDensity
+from nbodylib_gb300 import synthetic as syn
+from tests.helpers import assert_density_close
+
+pytestmark = pytest.mark.gpu
+
+
+def reference_batch(pos, mass, off, k, b):
+    rho = np.empty(len(mass))
+    for g in range(len(off) - 1):
+        s, e = off[g], off[g + 1]
+        t = oracle.OracleTree(pos[s:e], None, mass[s:e], b, 0, 0, 1000, None, backend="port")
+        rho[s:e] = t.density(min(k, e - s - 1))
+    return rho
+
+
+@pytest.mark.parametrize("bucket", [16, 0])
+def test_batched_density_vs_oracle(gpu, port_built, bucket):
+    sizes = syn.group_sizes(300, 20, 3000, seed=41)
+    sizes[:3] = [2, 3, 33]  # tiny groups: k is clamped to n - 1
+    pos, vel, mass, off = syn.plummer_groups(sizes, seed=41)
+    want = reference_batch(pos, mass, off, 32, 16)
+    B = BatchedDensity(pos, mass, off, bucket_size=bucket)
+    b, qb, tune = B.params()
+    if bucket == 0:
+        assert b in (8, 12, 16, 24, 32) and qb in (16, 32) and "chosen" in tune
+    for use_graph in (False, True, True):
+        assert_density_close(B.density(32, use_graph=use_graph), want, f"batched graph={use_graph}")
+    assert_density_close(B.density_pertree(32), want, "per-tree loop")
+    B.close()
+
+
+def test_batched_large_groups(gpu, port_built):
+    """Groups above the 1024-particle per-CTA limit go through the level-synchronous
+    phase together."""
+    sizes = np.array([5000, 1025, 70000, 20, 4096, 1500])
+    pos, vel, mass, off = syn.plummer_groups(sizes, seed=43)
+    want = reference_batch(pos, mass, off, 32, 16)
+    B = BatchedDensity(pos, mass, off, bucket_size=16)
+    assert_density_close(B.density(32), want, "large groups")
