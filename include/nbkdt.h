@@ -149,6 +149,12 @@ int nbk_get_kernel(const nbk_tree* tree, double* table, double* kernnorm);
  */
 int nbk_knn(nbk_tree* tree, int k, int variant, int periodic_mode, int32_t* nn, double* d2);
 
+/* FindNearest(tt, ...) / FindNearestPos(tt, ...) (KDFindNearest.cxx:247-334) for a batch
+   of target particles (tree indices): row i of nn/d2 belongs to targets[i]; semantics as
+   nbk_knn. */
+int nbk_knn_targets(nbk_tree* tree, const int32_t* targets, int64_t ntargets, int k,
+                    int variant, int periodic_mode, int32_t* nn, double* d2);
+
 /* k nearest neighbours of nq coordinates (nq x 3). Replaces
    KDTree::FindNearestPos(Double_t* x, Int_t* nn, Double_t* dist2, Int_t Nsearch)
    (KDFindNearest.cxx:509-520); nothing is excluded. */

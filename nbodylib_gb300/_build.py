@@ -16,8 +16,10 @@ OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libnbkdt.so")
 SOURCES = ["capi.cu", "build.cu", "knn.cu", "fof.cu", "ball.cu", "adjoint.cu", "batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-         "-Xptxas", "-warn-spills"]
+# Host code is compiled without floating-point contraction: the kernel table is built on
+# the host and must round exactly as the reference's (GCC on aarch64 would fuse a*b+c).
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
+         "-ffp-contract=off", "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 
 def nvcc() -> str:

@@ -573,6 +573,53 @@ int nbk_knn(nbk_tree* t, int k, int variant, int periodic_mode, int32_t* nn, dou
   API_END
 }
 
+int nbk_knn_targets(nbk_tree* t, const int32_t* targets, int64_t nt, int k, int variant,
+                    int periodic_mode, int32_t* nn, double* d2) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  if (k < 1 || !targets || !nn || !d2 || nt < 0) {
+    set_error("nbk_knn_targets: invalid argument");
+    return NBK_ERR_INVALID;
+  }
+  if (variant != NBK_FINDNEAREST && variant != NBK_FINDNEARESTPOS) {
+    set_error("nbk_knn_targets: unknown variant");
+    return NBK_ERR_INVALID;
+  }
+  if (nt == 0) return NBK_OK;
+  if (!t->dev())
+    for (int64_t i = 0; i < nt; i++)
+      if (targets[i] < 0 || targets[i] >= t->n) {
+        set_error("nbk_knn_targets: target index out of range");
+        return NBK_ERR_INVALID;
+      }
+  Stage S(t);
+  const int* dt;
+  int* dnn;
+  double* dd2;
+  NBK_TRY(S.in(targets, nt, &dt));
+  NBK_TRY(S.out(nn, (size_t)nt * k, &dnn));
+  NBK_TRY(S.out(d2, (size_t)nt * k, &dd2));
+  NBK_TRY(clear_err(t));
+  KnnArgs a = base_args(t);
+  bool per = t->periodic;
+  a.kheap = per ? k + 1 : k;
+  a.kout = k;
+  a.drop_largest = (per && variant == NBK_FINDNEARESTPOS) ? 1 : 0;
+  a.periodic = a.tv.periodic;
+  a.exclude_self = a.tv.periodic ? 0 : 1;
+  a.min_image = periodic_mode == NBK_PERIODIC_MIN_IMAGE;
+  a.qmode = 2;
+  a.qidx = dt;
+  a.nq = (int)nt;
+  a.nn = dnn;
+  a.d2 = dd2;
+  NBK_TRY(launch_knn(a, kEpiNN, t->st));
+  NBK_TRY(S.finish());
+  if (!t->dev()) NBK_TRY(check_err(t, "nbk_knn_targets"));
+  return NBK_OK;
+  API_END
+}
+
 int nbk_knn_points(nbk_tree* t, const double* x, int64_t nq, int k, int periodic_mode,
                    int32_t* nn, double* d2) {
   API_BEGIN
@@ -861,15 +908,47 @@ int nbk_fof(nbk_tree* t, double fdist, int32_t minnum, int order, int32_t* group
 
 int nbk_fof_criterion(nbk_tree* t, int comparator, const double* params, int32_t minnum,
                       int order, int32_t* group, int32_t* ngroup) {
-  (void)comparator;
-  (void)params;
-  (void)minnum;
-  (void)order;
-  (void)group;
-  (void)ngroup;
+  API_BEGIN
   NBK_TRY(check_tree(t));
-  set_error("nbk_fof_criterion: not yet available");
-  return NBK_ERR_UNSUPPORTED;
+  if (!group || !ngroup || !params) {
+    set_error("nbk_fof_criterion: invalid argument");
+    return NBK_ERR_INVALID;
+  }
+  if (comparator < NBK_FOF3D || comparator > NBK_FOF6D) {
+    set_error("nbk_fof_criterion: only the FOF3d, FOFVel and FOF6d comparators run on the GPU");
+    return NBK_ERR_UNSUPPORTED;
+  }
+  if (comparator != NBK_FOF3D && !t->has_vel) {
+    set_error("nbk_fof_criterion: FOFVel and FOF6d need velocities at nbk_create");
+    return NBK_ERR_INVALID;
+  }
+  double p[8];
+  if (t->dev()) NBK_CUDA_TRY(cudaMemcpy(p, params, sizeof(p), cudaMemcpyDeviceToHost));
+  else memcpy(p, params, sizeof(p));
+  Stage S(t);
+  int* dg;
+  NBK_TRY(S.out(group, t->n, &dg));
+  int *parent, *gtree;
+  NBK_TRY(S.alloc.get((void**)&parent, sizeof(int) * t->n));
+  NBK_TRY(S.alloc.get((void**)&gtree, sizeof(int) * t->n));
+  NBK_TRY(clear_err(t));
+  FofArgs a{};
+  a.tv = t->view();
+  a.crit = 1;
+  a.cmp = comparator;
+  for (int i = 0; i < 8; i++) a.params[i] = p[i];
+  a.parent = parent;
+  a.err = t->d_err;
+  int ng = 0;
+  NBK_TRY(run_fof(a, (int)t->nslots, minnum, order, gtree, &ng, S.alloc, t->st));
+  k_scatter_i<<<(unsigned)((t->n + 255) / 256), 256, 0, t->st>>>(gtree, t->arr.perm, dg, t->n);
+  note_launch();
+  NBK_CUDA_TRY(cudaGetLastError());
+  NBK_TRY(S.finish());
+  NBK_TRY(check_err(t, "nbk_fof_criterion"));
+  *ngroup = ng;
+  return NBK_OK;
+  API_END
 }
 
 int nbk_density_adjoint(nbk_tree* t, int k, const double* w, double* rho, double* grad_pos,

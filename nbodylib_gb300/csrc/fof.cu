@@ -187,6 +187,109 @@ __global__ void __launch_bounds__(32 * kWpb) k_link(FofArgs a) {
   }
 }
 
+// ---- FOFCriterion (KDFOF.cxx:157-265). The comparators of FOFFunc.h:30-55, in the
+// reference's operation order: total += (a-b)*(a-b)/params[6] per dimension (FOF6d
+// interleaves position and velocity terms), linked when total < 1.
+__device__ __forceinline__ bool crit_cmp(int cmp, const double* p, const double xa[3],
+                                         const V4& va, const P4& xb, const V4& vb) {
+  double total = 0.0;
+  double xb3[3] = {xb.x, xb.y, xb.z}, va3[3] = {va.x, va.y, va.z}, vb3[3] = {vb.x, vb.y, vb.z};
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    if (cmp == 0 || cmp == 2) {
+      double d = dsub(xa[j], xb3[j]);
+      total = dadd(total, __ddiv_rn(dmul(d, d), p[6]));
+    }
+    if (cmp == 1) {
+      double d = dsub(va3[j], vb3[j]);
+      total = dadd(total, __ddiv_rn(dmul(d, d), p[6]));
+    }
+    if (cmp == 2) {
+      double d = dsub(va3[j], vb3[j]);
+      total = dadd(total, __ddiv_rn(dmul(d, d), p[7]));
+    }
+  }
+  return total < 1.0;
+}
+
+// Node pruning of SplitNode::FOFSearchCriterion (KDSplitNode.cxx:991-1028): the far child
+// is opened when rd + (-old^2 + new^2) * invscaling < 1, with old/new the offsets to the
+// cut planes along the path. This reachability is part of the reference's result (pairs
+// it never reaches are never compared), so it is reproduced exactly: one thread per
+// particle walks the tree with the same split planes, carrying rd and the offsets.
+__device__ __forceinline__ double crit_invscaling(const double* p, int cd) {
+  int tt = (int)p[0];
+  if (tt == 0) return 1.0 / p[1];
+  if (tt == 2) return 1.0 / p[2];
+  if (tt == 3) return 1.0 / p[(cd < 3) * 1 + (cd >= 3) * 2];
+  return 1.0;
+}
+
+__global__ void __launch_bounds__(128) k_crit_link(FofArgs a) {
+  const TreeView& tv = a.tv;
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= tv.n) return;
+  int self = tv.pstart + q;
+  P4 me = tv.pos[self];
+  V4 mv = tv.vel ? tv.vel[self] : make_v4(0, 0, 0, 0);
+  double x0[3] = {me.x, me.y, me.z};
+  int stk_h[kStack];
+  double stk_rd[kStack], stk_off[kStack][3];
+  int npass = tv.periodic ? 8 : 1;
+  for (int pass = 0; pass < npass; pass++) {
+    double xq[3] = {x0[0], x0[1], x0[2]};
+    if (pass > 0) reflect(x0, xq, tv.period, kImageMask[pass]);  // ungated (:1649-1681)
+    int sp = 0;
+    stk_h[0] = 0;
+    stk_rd[0] = 0.0;
+    stk_off[0][0] = stk_off[0][1] = stk_off[0][2] = 0.0;
+    sp = 1;
+    while (sp > 0) {
+      sp--;
+      int h = stk_h[sp];
+      double rd = stk_rd[sp];
+      double off[3] = {stk_off[sp][0], stk_off[sp][1], stk_off[sp][2]};
+      NodeRec r = tv.node[tv.nbase + h];
+      if (r.count <= tv.b) {
+        for (int i = r.start; i < r.start + r.count; i++) {
+          if (i == self) continue;
+          P4 xb = tv.pos[i];
+          V4 vb = tv.vel ? tv.vel[i] : make_v4(0, 0, 0, 0);
+          if (crit_cmp(a.cmp, a.params, xq, mv, xb, vb)) unite(a.parent, self, i, a.err);
+        }
+        continue;
+      }
+      const NodeX& nx = tv.nodex[tv.nbase + h];
+      int cd = nx.split_dim;
+      double old_off = off[cd];
+      double new_off = dsub(xq[cd], nx.split_val);
+      int nearh = new_off < 0 ? 2 * h + 1 : 2 * h + 2;
+      int farh = new_off < 0 ? 2 * h + 2 : 2 * h + 1;
+      double rdf = dadd(rd, dmul(dadd(dmul(-old_off, old_off), dmul(new_off, new_off)),
+                                 crit_invscaling(a.params, cd)));
+      if (sp + 2 > kStack) {
+        atomicExch(a.err, kErrCapacity);
+        return;
+      }
+      if (rdf < 1.0) {
+        stk_h[sp] = farh;
+        stk_rd[sp] = rdf;
+        stk_off[sp][0] = off[0];
+        stk_off[sp][1] = off[1];
+        stk_off[sp][2] = off[2];
+        stk_off[sp][cd] = new_off;
+        sp++;
+      }
+      stk_h[sp] = nearh;
+      stk_rd[sp] = rd;
+      stk_off[sp][0] = off[0];
+      stk_off[sp][1] = off[1];
+      stk_off[sp][2] = off[2];
+      sp++;
+    }
+  }
+}
+
 __global__ void k_flatten_count(int* parent, int n, int* cnt) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -316,12 +419,15 @@ int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tr
   NBK_TRY(alloc.get((void**)&bsum, sizeof(int) * (nb + 1)));
   NBK_TRY(alloc.get((void**)&d_total, sizeof(int)));
   k_iota<<<(n + 255) / 256, 256, 0, st>>>(a.parent, n); note_launch();
-  {
+  if (!a.crit) {
     Phase ph("fof_prelink", st);
     k_prelink<<<(n + 255) / 256, 256, 0, st>>>(a); note_launch();
   }
   int warps = (n + 31) / 32;
-  {
+  if (a.crit) {
+    Phase ph("fof_criterion_link", st);
+    k_crit_link<<<(n + 127) / 128, 128, 0, st>>>(a); note_launch();
+  } else {
     Phase ph("fof_link", st);
     k_link<<<(warps + kWpb - 1) / kWpb, 32 * kWpb, 0, st>>>(a); note_launch();
   }

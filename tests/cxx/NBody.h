@@ -1,0 +1,67 @@
+// Test stand-in for NBodylib's NBody.h: just enough of NBody::Particle, NBody::System and
+// NBody::Coordinate (the accessors include/nbkdt/KDTree.h uses) to compile and run the
+// drop-in KDTree where NBodylib itself is not installed. The member layout follows the
+// reference's default Particle (88 bytes: mass, position[3], velocity[3], pid, id, type,
+// rho, phi).
+#pragma once
+#include <cmath>
+#include <cstddef>
+
+typedef double Double_t;
+typedef int Int_t;
+
+namespace NBody {
+
+class Coordinate {
+ public:
+  Coordinate(Double_t x = 0, Double_t y = 0, Double_t z = 0) {
+    c_[0] = x;
+    c_[1] = y;
+    c_[2] = z;
+  }
+  Double_t* GetCoord() { return c_; }
+  Double_t operator[](int i) const { return c_[i]; }
+
+ private:
+  Double_t c_[3];
+};
+
+class Particle {
+ public:
+  Particle() = default;
+  Double_t GetMass() const { return mass_; }
+  void SetMass(Double_t m) { mass_ = m; }
+  Double_t GetPosition(int j) const { return pos_[j]; }
+  const Double_t* GetPosition() const { return pos_; }
+  void SetPosition(int j, Double_t v) { pos_[j] = v; }
+  Double_t GetVelocity(int j) const { return vel_[j]; }
+  void SetVelocity(int j, Double_t v) { vel_[j] = v; }
+  Int_t GetID() const { return id_; }
+  void SetID(const Int_t& i) { id_ = i; }
+  Int_t GetPID() const { return pid_; }
+  void SetPID(const Int_t& i) { pid_ = i; }
+  Double_t GetDensity() const { return rho_; }
+  void SetDensity(const Double_t& r) { rho_ = r; }
+
+ private:
+  Double_t mass_ = 0;
+  Double_t pos_[3] = {0, 0, 0};
+  Double_t vel_[3] = {0, 0, 0};
+  Int_t pid_ = 0, id_ = 0, type_ = 0;
+  Double_t rho_ = 0, phi_ = 0;
+};
+
+class System {
+ public:
+  System(Particle* p, Int_t n, Coordinate period) : p_(p), n_(n), period_(period) {}
+  Particle* Parts() const { return p_; }
+  Int_t GetNumParts() const { return n_; }
+  Coordinate GetPeriod() const { return period_; }
+
+ private:
+  Particle* p_;
+  Int_t n_;
+  Coordinate period_;
+};
+
+}  // namespace NBody

@@ -1,0 +1,90 @@
+// Exercises the drop-in NBody::KDTree (include/nbkdt/KDTree.h) the way reference code
+// calls it (src/tests/test_kdtree.cxx, src/Analysis/Density.cxx:157-163), on particles
+// read from a binary file, and writes every result keyed by particle ID so a test can
+// compare it with the oracle.
+//
+//   dropin_demo <in.bin> <out.bin>
+//   in.bin : int32 n, int32 periodic, double box, double ll, then n x (x y z vx vy vz m)
+//   out.bin: int32 n, int32 numnodes, int32 numleaves, int32 ngroup,
+//            n x int32 group (by ID), n x double rho (by ID, CalcDensity(32)),
+//            n x 16 int32 FindNearest IDs (row by ID), n x 16 double d2,
+//            int32 ball count, ball IDs, double rho after the destructor (input order)
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include <nbkdt/KDTree.h>
+
+using namespace NBody;
+
+int main(int argc, char** argv) {
+  if (argc < 3) return 2;
+  FILE* f = fopen(argv[1], "rb");
+  if (!f) return 2;
+  int n = 0, periodic = 0;
+  double box = 0, ll = 0;
+  if (fread(&n, 4, 1, f) != 1 || fread(&periodic, 4, 1, f) != 1 || fread(&box, 8, 1, f) != 1 ||
+      fread(&ll, 8, 1, f) != 1)
+    return 2;
+  std::vector<Particle> parts(n);
+  for (int i = 0; i < n; i++) {
+    double v[7];
+    if (fread(v, 8, 7, f) != 7) return 2;
+    for (int j = 0; j < 3; j++) {
+      parts[i].SetPosition(j, v[j]);
+      parts[i].SetVelocity(j, v[3 + j]);
+    }
+    parts[i].SetMass(v[6]);
+    parts[i].SetPID(i);
+  }
+  fclose(f);
+  double period[3] = {box, box, box};
+  std::vector<int> group(n), nnid((size_t)n * 16), ballid;
+  std::vector<double> rho(n), d2((size_t)n * 16), rho_after(n);
+  int numnodes, numleaves, ngroup = 0;
+  {
+    KDTree tree(parts.data(), n, 16, KDTree::TPHYS, KDTree::KSPH, 1000, 0, 0, 0,
+                periodic ? period : NULL);
+    numnodes = tree.GetNumNodes();
+    numleaves = tree.GetNumLeafNodes();
+    // IDs follow the particles (KDTree.cxx:1291)
+    Int_t* g = tree.FOF(ll, ngroup, 20);
+    for (int i = 0; i < n; i++) group[i] = g[i];
+    delete[] g;
+    tree.CalcDensity(32);
+    for (int t = 0; t < n; t++) rho[parts[t].GetID()] = parts[t].GetDensity();
+    std::vector<Int_t> nn(16);
+    std::vector<Double_t> dd(16);
+    for (int t = 0; t < n; t++) {
+      tree.FindNearest(t, nn.data(), dd.data(), 16);
+      int id = parts[t].GetID();
+      for (int j = 0; j < 16; j++) {
+        nnid[(size_t)id * 16 + j] = parts[nn[j]].GetID();
+        d2[(size_t)id * 16 + j] = dd[j];
+      }
+    }
+    // the tree index of ID 0
+    int t0 = 0;
+    while (parts[t0].GetID() != 0) t0++;
+    std::vector<Int_t> tagged = tree.SearchBallPosTagged(t0, 4 * ll * ll);
+    for (Int_t t : tagged) ballid.push_back(parts[t].GetID());
+  }
+  // the destructor restored input order
+  for (int i = 0; i < n; i++) rho_after[i] = parts[i].GetDensity();
+  FILE* o = fopen(argv[2], "wb");
+  fwrite(&n, 4, 1, o);
+  fwrite(&numnodes, 4, 1, o);
+  fwrite(&numleaves, 4, 1, o);
+  fwrite(&ngroup, 4, 1, o);
+  fwrite(group.data(), 4, n, o);
+  fwrite(rho.data(), 8, n, o);
+  fwrite(nnid.data(), 4, (size_t)n * 16, o);
+  fwrite(d2.data(), 8, (size_t)n * 16, o);
+  int nb = (int)ballid.size();
+  fwrite(&nb, 4, 1, o);
+  fwrite(ballid.data(), 4, nb, o);
+  fwrite(rho_after.data(), 8, n, o);
+  fclose(o);
+  printf("dropin ok: n=%d nodes=%d groups=%d\n", n, numnodes, ngroup);
+  return 0;
+}

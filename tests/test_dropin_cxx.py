@@ -1,0 +1,87 @@
+"""The C++ drop-in NBody::KDTree (include/nbkdt/KDTree.h): it compiles against the
+reference's own NBody headers (source compatibility, CPU) and, run on the GPU through a
+reference-style call sequence, gives the oracle's results (GPU)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from nbodylib_gb300 import _build
+from nbodylib_gb300 import synthetic as syn
+from tests.helpers import assert_density_close, assert_knn_equal, assert_same_partition
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+SRC = os.path.join(HERE, "cxx", "dropin_demo.cpp")
+
+
+def compile_demo(out, include_nbody, link=True):
+    libdir = os.path.dirname(_build.LIB)
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
+           *sum((["-I", d] for d in include_nbody), []), SRC, "-o", out]
+    cmd += ["-L", libdir, "-lnbkdt", f"-Wl,-rpath,{libdir}"] if link else ["-c"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+
+
+def test_compiles_against_the_reference_headers(lib_built, tmp_path):
+    ref = os.environ.get("NBKDT_REF_SRC", oracle.DEFAULT_REF_SRC)
+    if not os.path.isdir(os.path.join(ref, "src", "NBody")):
+        pytest.skip("reference checkout not present on this machine")
+    inc = [os.path.join(ROOT, "oracle", "gslshim"), os.path.join(ref, "src", "NBody"),
+           os.path.join(ref, "src", "Math")]
+    # compile only: linking needs NBodylib's own library (Particle's constructors)
+    compile_demo(str(tmp_path / "demo_ref.o"), inc, link=False)
+
+
+def test_compiles_against_the_standin(lib_built, tmp_path):
+    compile_demo(str(tmp_path / "demo"), [os.path.join(HERE, "cxx")])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("periodic", [0, 1])
+def test_dropin_runs_like_the_reference(gpu, port_built, tmp_path, periodic):
+    exe = str(tmp_path / "demo")
+    compile_demo(exe, [os.path.join(HERE, "cxx")])
+    n, box = 20000, 100.0
+    pos, mass, vel = syn.clustered_box(n, box, seed=8, velocities=True)
+    ll = syn.linking_length(n, box)
+    inp = tmp_path / "in.bin"
+    with open(inp, "wb") as f:
+        np.array([n, periodic], np.int32).tofile(f)
+        np.array([box, ll], np.float64).tofile(f)
+        np.concatenate([pos, vel, mass[:, None]], 1).astype(np.float64).tofile(f)
+    out = tmp_path / "out.bin"
+    r = subprocess.run([exe, str(inp), str(out)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    raw = open(out, "rb").read()
+    off = 0
+
+    def take(dt, cnt):
+        nonlocal off
+        a = np.frombuffer(raw, dt, cnt, off)
+        off += a.nbytes
+        return a
+
+    n_, nodes, leaves, ngroup = take(np.int32, 4)
+    group = take(np.int32, n)
+    rho = take(np.float64, n)
+    nnid = take(np.int32, n * 16).reshape(n, 16)
+    d2 = take(np.float64, n * 16).reshape(n, 16)
+    nb = take(np.int32, 1)[0]
+    ball = take(np.int32, nb)
+    rho_after = take(np.float64, n)
+    per = [box] * 3 if periodic else None
+    o = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, per, backend="port")
+    assert nodes == o.num_nodes and leaves == o.num_leaves
+    go, no = o.fof(ll, 20)
+    assert ngroup == no
+    assert_same_partition(group, go, "drop-in FOF")
+    oi, od = o.knn(16, 0)
+    assert_knn_equal(nnid, d2, oi, od, "drop-in FindNearest")
+    ro = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, per, backend="port").density(32)
+    assert_density_close(rho, ro, "drop-in CalcDensity")
+    assert_density_close(rho_after, ro, "input order restored by the destructor")
+    np.testing.assert_array_equal(np.sort(ball), o.ball_tagged(0, 4 * ll * ll))

@@ -13,7 +13,7 @@ from tests.helpers import assert_density_close
 pytestmark = pytest.mark.gpu
 
 FD_RTOL = 1e-6      # relative error against central finite differences
-GRAD_RTOL = 1e-9    # GPU vs CPU restatement (differ only by summation order)
+GRAD_RTOL = 1e-8    # GPU vs CPU restatement: summation order (atomics) and cancellation
 
 
 def _rel(a, b, scale):

@@ -158,3 +158,22 @@ def test_ball_vs_oracle(gpu, port_built, periodic):
     for j in range(200):
         np.testing.assert_array_equal(np.sort(perm[out[off[j]:off[j + 1]]]),
                                       o.ball_tagged_pos(x[j], r2))
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+@pytest.mark.parametrize("cmp", [0, 2])
+def test_fof_criterion_vs_oracle(gpu, port_built, periodic, cmp):
+    """FOFCriterion with FOF3d / FOF6d (FOFFunc.h:30-55); params[6] (the linking length^2)
+    below params[1] (the search distance^2), so every linked pair is reached from both
+    ends and the reference's breadth-first result is a partition of the link graph."""
+    n = 30000
+    pos, mass, vel = syn.clustered_box(n, 100.0, seed=17, velocities=True)
+    per = [100.0] * 3 if periodic else None
+    ll = syn.linking_length(n, 100.0)
+    params = [0, (1.5 * ll) ** 2, 0, 0, 0, 0, ll * ll, 0.01]
+    o = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, per, backend="port")
+    go, no = o.fof_criterion(cmp, params, 10)
+    t = KDTree(pos, vel, mass, 16, kerntype=0, period=per)
+    gg, ng = t.FOFCriterion(cmp, params, 10)
+    assert ng == no
+    assert_same_partition(gg, go, f"FOFCriterion cmp={cmp}")
