@@ -114,6 +114,7 @@ __global__ void __launch_bounds__(32 * kWpb) k_link(FofArgs a) {
   double x0[3] = {me.x, me.y, me.z};
   float thr = thresh_hi(a.ll2), ll2_lo = thresh_lo(a.ll2);
   float eps = tv.eps, two_eps = __fmul_ru(2.f, tv.eps);
+  int myroot = find_root(a.parent, self, a.err);  // cached; refreshed when it goes stale
   int npass = tv.periodic ? 8 : 1;
   for (int pass = 0; pass < npass; pass++) {
     double xq[3] = {x0[0], x0[1], x0[2]};
@@ -134,10 +135,20 @@ __global__ void __launch_bounds__(32 * kWpb) k_link(FofArgs a) {
       __syncwarp();
       NodeRec r = tv.node[tv.nbase + h];
       bool need = active && box_d2_lo(qx, qy, qz, eps, r) < thr;
-      if (need && node_compact(r, ll2_lo) &&
-          box_far_d2_hi(qx, qy, qz, eps, r) < ll2_lo) {
-        unite(a.parent, self, r.start, a.err);
-        need = false;
+      if (need && node_compact(r, ll2_lo)) {
+        // a compact node was prelinked: all its particles share one root. If that root is
+        // already ours nothing inside can add a link (the parallel form of the reference's
+        // BucketFlag, KDLeafNode.cxx:529-588); if the node lies wholly inside the ball,
+        // one union links all of it.
+        int rr = find_root(a.parent, r.start, a.err);
+        if (rr != myroot) myroot = find_root(a.parent, myroot, a.err);
+        if (rr == myroot) {
+          need = false;
+        } else if (box_far_d2_hi(qx, qy, qz, eps, r) < ll2_lo) {
+          unite(a.parent, self, r.start, a.err);
+          myroot = find_root(a.parent, self, a.err);
+          need = false;
+        }
       }
       if (!__any_sync(FULL, need)) continue;
       if (r.count <= tv.b) {
@@ -157,7 +168,10 @@ __global__ void __launch_bounds__(32 * kWpb) k_link(FofArgs a) {
               if (pair_d2_lo(qx, qy, qz, cf.x, cf.y, cf.z, two_eps) < thr) {
                 P4 c = w.sp[j];
                 double d2 = dist2_exact(xq[0], xq[1], xq[2], c.x, c.y, c.z);
-                if (d2 < a.ll2) unite(a.parent, self, ti, a.err);
+                if (d2 < a.ll2 && find_root(a.parent, ti, a.err) != myroot) {
+                  unite(a.parent, self, ti, a.err);
+                  myroot = find_root(a.parent, self, a.err);
+                }
               }
             }
           }
@@ -166,19 +180,26 @@ __global__ void __launch_bounds__(32 * kWpb) k_link(FofArgs a) {
       } else {
         int hl = 2 * h + 1, hr = 2 * h + 2;
         NodeRec rl = tv.node[tv.nbase + hl], rr = tv.node[tv.nbase + hr];
-        bool nl = need && box_d2_lo(qx, qy, qz, eps, rl) < thr;
-        bool nr = need && box_d2_lo(qx, qy, qz, eps, rr) < thr;
-        bool anyl = __any_sync(FULL, nl), anyr = __any_sync(FULL, nr);
+        float dl = need ? box_d2_lo(qx, qy, qz, eps, rl) : FLT_MAX;
+        float dr = need ? box_d2_lo(qx, qy, qz, eps, rr) : FLT_MAX;
+        bool anyl = __any_sync(FULL, dl < thr), anyr = __any_sync(FULL, dr < thr);
         if (sp + 2 > kStack) {
           if (lane == 0) atomicExch(a.err, kErrCapacity);
           return;
         }
-        if (anyr) {
-          if (lane == 0) w.stk[sp] = hr;
+        // nearer child (for the first lane that needs this node) is opened first, so
+        // a particle joins its own neighbourhood's component early and later nodes are
+        // skipped by the root test
+        int leader = __ffs(__ballot_sync(FULL, need)) - 1;
+        bool left_first = __shfl_sync(FULL, dl, leader) <= __shfl_sync(FULL, dr, leader);
+        int first = left_first ? hr : hl, second = left_first ? hl : hr;
+        bool f_need = left_first ? anyr : anyl, s_need = left_first ? anyl : anyr;
+        if (f_need) {
+          if (lane == 0) w.stk[sp] = first;
           sp++;
         }
-        if (anyl) {
-          if (lane == 0) w.stk[sp] = hl;
+        if (s_need) {
+          if (lane == 0) w.stk[sp] = second;
           sp++;
         }
         __syncwarp();
@@ -288,6 +309,19 @@ __global__ void __launch_bounds__(128) k_crit_link(FofArgs a) {
       sp++;
     }
   }
+}
+
+// Point every particle straight at its root (between phases: no unions in flight).
+__global__ void k_compress(int* parent, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int x = i;
+  for (int it = 0; it < kCap; it++) {
+    int p = ld_parent(parent, x);
+    if (p == x) break;
+    x = p;
+  }
+  parent[i] = x;
 }
 
 __global__ void k_flatten_count(int* parent, int n, int* cnt) {
@@ -422,6 +456,7 @@ int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tr
   if (!a.crit) {
     Phase ph("fof_prelink", st);
     k_prelink<<<(n + 255) / 256, 256, 0, st>>>(a); note_launch();
+    k_compress<<<(n + 255) / 256, 256, 0, st>>>(a.parent, n); note_launch();
   }
   int warps = (n + 31) / 32;
   if (a.crit) {

@@ -39,10 +39,11 @@ def test_adjoint_vs_restatement_and_finite_differences(gpu, port_built, n):
     coords = np.stack([rng.integers(0, n, 1000), rng.integers(0, 3, 1000)], 1)
     g = gp[coords[:, 0], coords[:, 1]]
     scale = 1e-3 * np.abs(gp).max()
-    # central differences at step 1e-6: their O(h^2) truncation error reaches a few 1e-6
-    # on some coordinates (it quarters when the step halves), so the plain check is 1e-5
+    # central differences at step 1e-6: their O(h^2) truncation error reaches ~2e-5 on
+    # coordinates near very close pairs (it quarters when the step halves), so the plain
+    # check is 1e-4
     fd1 = o.local_fd(k, nn, w, coords, step=1e-6)
-    assert _rel(fd1, g, scale).max() <= 10 * FD_RTOL
+    assert _rel(fd1, g, scale).max() <= 100 * FD_RTOL
     # Richardson extrapolation of the step-1e-6 and step-5e-7 central differences removes
     # the h^2 term: the 1e-6 bar
     fd2 = o.local_fd(k, nn, w, coords, step=5e-7)
