@@ -348,6 +348,46 @@ def run_reference(args, world, rank):
                     "d2h_bytes_per_step": 0}}
 
 
+def profile_case(args):
+    """A small case of one kernel family, device-resident, for ncu captures: the FOF step
+    (build + FOF) or the kNN-density step on args.n clustered particles, or the batched
+    density on a power-law group batch of about args.n particles."""
+    import torch
+
+    from nbodylib_gb300 import BatchedDensity, KDTree, _build
+    from nbodylib_gb300 import synthetic as syn
+    _build.build()
+    torch.cuda.set_device(0)
+    n = args.n
+    box = BOX * (n / N_FOF) ** (1.0 / 3.0)  # keep the FOF workload's number density
+    pos, mass = syn.clustered_box(n, box, seed=2)
+    dpos, dmass = torch.from_numpy(pos).cuda(), torch.from_numpy(mass).cuda()
+    if args.profile == "batch":
+        sizes = syn.group_sizes(20000, 20, 200000, seed=4)
+        sizes = sizes[np.cumsum(sizes) <= n]
+        gp, gv, gm, off = syn.plummer_groups(sizes, seed=4)
+        B = BatchedDensity(torch.from_numpy(gp).cuda(), torch.from_numpy(gm).cuda(),
+                           torch.from_numpy(off).cuda(), bucket_size=16, device=True)
+        out = torch.empty(len(gm), dtype=torch.float64, device="cuda")
+        for _ in range(args.steps):
+            B.density(32, use_graph=True, out=out)
+        torch.cuda.synchronize()
+        return
+    for _ in range(args.steps):
+        per = [box] * 3 if args.profile == "fof" else None
+        t = KDTree(dpos, None, dmass, BUCKET, kerntype=0, period=per, device=True)
+        if args.profile == "fof":
+            t.FOF(syn.linking_length(n, box), MINNUM)
+        elif args.profile == "knn":
+            t.CalcDensity(32)
+        elif args.profile == "adjoint":
+            w = torch.ones(n, dtype=torch.float64, device="cuda")
+            t.DensityAdjoint(32, w)
+        t.sync()
+        t.close()
+    torch.cuda.synchronize()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -355,7 +395,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--profile", choices=["fof", "knn", "build", "batch", "adjoint"],
+                    help="run only `steps` steps of one small case (for ncu), print nothing")
+    ap.add_argument("--n", type=int, default=1 << 18, help="particles for --profile")
     args = ap.parse_args()
+    if args.profile:
+        profile_case(args)
+        return
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     if args.impl == "reference":
         # only rank 0 times the CPU path; no process group is needed
