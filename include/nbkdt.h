@@ -170,6 +170,17 @@ int nbk_knn_points(nbk_tree* tree, const double* x, int64_t nq, int k, int perio
  */
 int nbk_density(nbk_tree* tree, int k, double* rho);
 
+/* nbk_density without any device allocation (no counterpart in the reference: it exists
+   for callers that cannot allocate device memory while they run, e.g. codes that own all
+   HBM through their own pool, or work inside a stream being captured into a CUDA graph).
+   The tree must already exist; rho_dev is a caller-owned DEVICE buffer of n doubles
+   (input order), whatever the tree's pointer mode. The scratch is a static device array
+   of 4,194,304 doubles (32 MiB, held per GPU until exit): larger trees return
+   NBK_ERR_INVALID. All calls share it, so calls that overlap on the GPU race and must be
+   serialised by the caller. The first call on each device sets the scratch up; make it
+   before any stream capture. */
+int nbk_density_noalloc(nbk_tree* tree, int k, double* rho_dev);
+
 /* Gather-only density of selected particles. Replaces KDTree::CalcDensityParticle
    (KDCalcSmoothQuantities.cxx:768-843): no 0.5 factor, no scatter.
    targets: tree indices. out: one value per target. */

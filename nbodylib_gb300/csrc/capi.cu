@@ -313,6 +313,37 @@ int check_tree(const nbk_tree* t) {
 
 }  // namespace
 
+namespace nbk {
+// CalcDensity with caller-supplied memory only: `scratch` (t->n doubles, tree order) and
+// the device output `rho_dev` (t->n doubles, input order). Used by nbk_density_noalloc
+// (noalloc.cu), which owns the scratch; nothing here allocates.
+int density_into_scratch(nbk_tree* t, int k, double* scratch, double* rho_dev) {
+  if (!t || !scratch || !rho_dev || k < 1) {
+    set_error("nbk_density_noalloc: invalid argument");
+    return NBK_ERR_INVALID;
+  }
+  if (k > t->n - 1) {
+    set_error("nbk_density_noalloc: k = " + std::to_string(k) + " exceeds the " +
+              std::to_string(t->n - 1) + " other particles");
+    return NBK_ERR_TOO_FEW;
+  }
+  NBK_CUDA_TRY(cudaMemsetAsync(scratch, 0, sizeof(double) * t->n, t->st));
+  NBK_TRY(clear_err(t));
+  KnnArgs a = base_args(t);
+  a.tv.periodic = 0;  // CalcDensity ignores the period (KDCalcSmoothQuantities.cxx:227)
+  a.kheap = k;
+  a.kout = k;
+  a.exclude_self = 1;
+  a.qmode = 0;
+  a.nq = (int)t->n;
+  a.rho = scratch;
+  NBK_TRY(launch_knn(a, kEpiDensity, t->st));
+  NBK_TRY(scatter_to_input_order(scratch, t->arr.perm, rho_dev, t->n, 1, t->st));
+  return check_err(t, "nbk_density_noalloc");
+}
+int64_t tree_size(const nbk_tree* t) { return t ? t->n : 0; }
+}  // namespace nbk
+
 extern "C" {
 
 const char* nbk_last_error(void) { return get_error(); }
@@ -654,6 +685,7 @@ int nbk_knn_points(nbk_tree* t, const double* x, int64_t nq, int k, int periodic
   return NBK_OK;
   API_END
 }
+
 
 static int density_common(nbk_tree* t, int k, int nsmooth, double* rho, double* vden, int epi) {
   if (k < 1) {
