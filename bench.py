@@ -246,7 +246,9 @@ def knn_density_components(args, lib):
 
     from nbodylib_gb300 import KDTree
     from nbodylib_gb300 import synthetic as syn
-    out = {}
+    fp64 = ctypes.c_double()
+    lib.nbk_probe_fp64(ctypes.byref(fp64))
+    out = {"fp64_peak_gflops_measured": fp64.value}
     cases = [("uniform_32768_periodic_k32", syn.uniform_box(32768, 1.0, seed=1), [1.0] * 3, 32),
              ("clustered_2pow20_k32", syn.clustered_box(N_FOF, BOX, seed=2), None, 32)]
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
@@ -290,6 +292,11 @@ def knn_density_components(args, lib):
             "density_queries_per_s": n / (kd_ms / 1e3),
             "fp64_flop_per_query": 20 * k,
             "algorithmic_bytes_per_query": 40,
+            # FP64 roofline of the density kernel: 20k algorithmic flop per query over the
+            # measured FMA rate of this GPU
+            "roofline_fp64": {"achieved_gflops": 20 * k * n / (kd_ms / 1e3) / 1e9,
+                              "peak_gflops": fp64.value,
+                              "frac": 20 * k * n / (kd_ms / 1e3) / 1e9 / fp64.value},
             "phase_ms": {kk: round(v["ms"] / max(v["count"], 1), 4) for kk, v in tr.items()},
         }
     return out

@@ -94,6 +94,10 @@ long long nbk_launch_count(void);
    stream it runs on, without synchronising; nbk_trace_json resolves the pending events
    and writes {"phase": {"count": c, "ms": total}, ...} into buf (NUL-terminated) and
    returns the length it needs. */
+/* Measured FP64 FMA throughput of the current GPU in GFLOP/s (2 flops per FMA), the
+   denominator of the FP64 roofline. (No reference counterpart.) */
+int nbk_probe_fp64(double* gflops);
+
 int nbk_trace_enable(int on);
 int nbk_trace_reset(void);
 int64_t nbk_trace_json(char* buf, int64_t cap);

@@ -25,6 +25,7 @@ SIGNATURES = {
     "nbk_last_error": (ctypes.c_char_p, []),
     "nbk_version": (ctypes.c_char_p, []),
     "nbk_launch_count": (ctypes.c_longlong, []),
+    "nbk_probe_fp64": (c_int, [c_dblp]),
     "nbk_trace_enable": (c_int, [c_int]),
     "nbk_trace_reset": (c_int, []),
     "nbk_trace_json": (c_i64, [ctypes.c_char_p, c_i64]),
