@@ -34,6 +34,9 @@ N_FOF = 1 << 20
 BOX = 100.0
 MINNUM = 20
 BUCKET = 16
+# DRAM bytes of one k_link launch at 2^20 particles: 200.6 MB measured by ncu on the same
+# recipe at 2^22 particles (the bench's --profile fof case), divided by 4
+K_LINK_DRAM_BYTES_PER_LAUNCH = 200.628e6 / 4
 
 
 def log(*a):
@@ -212,7 +215,7 @@ def run_gpu(args, world, rank, local):
         per_launch_s = link["ms"] / link["count"] / 1e3
         achieved = 28.0 * N_FOF / per_launch_s / 1e9
     phases = {k: round(v["ms"] / max(v["count"], 1), 4) for k, v in trace.items()}
-    comps = knn_density_components(args, lib)
+    comps = components(args, lib)
     result = {
         "metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot_s * 1e3 / args.steps,
@@ -228,7 +231,11 @@ def run_gpu(args, world, rank, local):
                 "d2h_bytes_per_step": int(g.nbytes + 4)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                     "frac": (achieved / hbm) if achieved else None,
+                     "traffic": K_LINK_DRAM_BYTES_PER_LAUNCH,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
+                                       "one k_link launch on 2^22 clustered particles at the "
+                                       "same density, scaled by particles to 2^20",
                      "kernel": "fof_link (k_link)", "peak_source": which,
                      "algorithmic_bytes_per_launch": 28 * N_FOF},
         "phase_ms_per_step": phases,
@@ -240,18 +247,55 @@ def run_gpu(args, world, rank, local):
     return result
 
 
-def knn_density_components(args, lib):
-    """kNN-density on the plain 32768-particle box and on 2^20 clustered particles."""
+def _timed(fn, reps, flush=None):
+    """Mean CUDA-event milliseconds of fn() over reps calls (L2 flushed before each)."""
+    import torch
+    ms = []
+    for _ in range(reps):
+        if flush is not None:
+            flush.zero_()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        fn()
+        e.record()
+        torch.cuda.synchronize()
+        ms.append(s.elapsed_time(e))
+    return float(np.mean(ms))
+
+
+def _trace(lib, fn):
+    """Run fn() with the library's phase trace on; return {phase: ms per call}."""
+    lib.nbk_trace_reset()
+    lib.nbk_trace_enable(1)
+    fn()
+    lib.nbk_trace_enable(0)
+    buf = ctypes.create_string_buffer(1 << 16)
+    lib.nbk_trace_json(buf, len(buf))
+    tr = json.loads(buf.value.decode())
+    return {k: v["ms"] / max(v["count"], 1) for k, v in tr.items()}
+
+
+def components(args, lib):
+    """The other workloads of the metric: kNN-density on the 32768-particle uniform box and
+    on 2^20 clustered particles, kNN density + velocity density on 256^3 clustered
+    particles (k=64), the batched persistent density on the power-law group batch against
+    the per-tree loop, and the density adjoint against its forward."""
     import torch
 
-    from nbodylib_gb300 import KDTree
+    from nbodylib_gb300 import BatchedDensity, KDTree
     from nbodylib_gb300 import synthetic as syn
     fp64 = ctypes.c_double()
     lib.nbk_probe_fp64(ctypes.byref(fp64))
     out = {"fp64_peak_gflops_measured": fp64.value}
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    reps = max(3, args.steps)
+
+    def fp64_roofline(flop_per_query, n, ms):
+        g = flop_per_query * n / (ms / 1e3) / 1e9
+        return {"achieved_gflops": g, "peak_gflops": fp64.value, "frac": g / fp64.value}
+
     cases = [("uniform_32768_periodic_k32", syn.uniform_box(32768, 1.0, seed=1), [1.0] * 3, 32),
              ("clustered_2pow20_k32", syn.clustered_box(N_FOF, BOX, seed=2), None, 32)]
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     for name, (pos, mass), per, k in cases:
         dpos = torch.from_numpy(pos).cuda()
         dmass = torch.from_numpy(mass).cuda()
@@ -259,46 +303,102 @@ def knn_density_components(args, lib):
 
         def step():
             t = KDTree(dpos, None, dmass, BUCKET, kerntype=0, period=per, device=True)
-            nn, d2 = t.FindNearest(k)
+            t.FindNearest(k)
             rho = t.CalcDensity(k)
             t.sync()
             t.close()
             return rho
 
-        for _ in range(3):
-            step()
-        lib.nbk_trace_reset()
-        lib.nbk_trace_enable(1)
-        ms = []
-        for _ in range(max(3, args.steps)):
-            flush.zero_()
-            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            s.record()
-            step()
-            e.record()
-            torch.cuda.synchronize()
-            ms.append(s.elapsed_time(e))
-        lib.nbk_trace_enable(0)
-        buf = ctypes.create_string_buffer(1 << 16)
-        lib.nbk_trace_json(buf, len(buf))
-        tr = json.loads(buf.value.decode())
-        dens = tr.get("knn_density", {"count": 1, "ms": float("nan")})
-        kd_ms = dens["ms"] / max(dens["count"], 1)
+        _timed(step, 3)
+        step_ms = _timed(step, reps, flush)
+        ph = _trace(lib, lambda: [(flush.zero_(), step()) for _ in range(reps)])
+        kd_ms = ph.get("knn_density", float("nan"))
         out[name] = {
-            "n": n, "k": k,
-            "step_ms": float(np.mean(ms)),
-            "queries_per_s_step": n / (np.mean(ms) / 1e3),
+            "n": n, "k": k, "step_ms": step_ms,
+            "queries_per_s_step": n / (step_ms / 1e3),
             "density_kernel_ms": kd_ms,
             "density_queries_per_s": n / (kd_ms / 1e3),
             "fp64_flop_per_query": 20 * k,
             "algorithmic_bytes_per_query": 40,
             # FP64 roofline of the density kernel: 20k algorithmic flop per query over the
             # measured FMA rate of this GPU
-            "roofline_fp64": {"achieved_gflops": 20 * k * n / (kd_ms / 1e3) / 1e9,
-                              "peak_gflops": fp64.value,
-                              "frac": 20 * k * n / (kd_ms / 1e3) / 1e9 / fp64.value},
-            "phase_ms": {kk: round(v["ms"] / max(v["count"], 1), 4) for kk, v in tr.items()},
+            "roofline_fp64": fp64_roofline(20 * k, n, kd_ms),
+            "phase_ms": {kk: round(v, 4) for kk, v in ph.items()},
         }
+        del dpos, dmass
+
+    # 256^3 clustered particles in L=250 with velocities: CalcDensity(64), then
+    # CalcVelDensity(64, 64) on the same tree
+    n3 = 1 << 24
+    pos, mass, vel = syn.clustered_box(n3, 250.0, seed=3, velocities=True)
+    dpos, dmass, dvel = (torch.from_numpy(a).cuda() for a in (pos, mass, vel))
+    del pos, mass, vel
+
+    def step3():
+        t = KDTree(dpos, dvel, dmass, BUCKET, kerntype=0, device=True)
+        t.CalcDensity(64)
+        t.CalcVelDensity(64, 64)
+        t.sync()
+        t.close()
+
+    _timed(step3, 1)
+    ms3 = _timed(step3, 2, flush)
+    ph3 = _trace(lib, step3)
+    out["clustered_256cubed_k64_density_veldensity"] = {
+        "n": n3, "k": 64, "step_ms": ms3, "particles_per_s_step": n3 / (ms3 / 1e3),
+        "density_kernel_ms": ph3.get("knn_density"),
+        "veldensity_kernel_ms": ph3.get("knn_veldensity"),
+        # 20k flop for the physical density; the velocity density adds 8 per neighbour
+        # for |dv| and 12 for the kernel
+        "roofline_fp64_density": fp64_roofline(20 * 64, n3, ph3.get("knn_density", float("nan"))),
+        "phase_ms": {kk: round(v, 4) for kk, v in ph3.items()},
+    }
+    del dpos, dmass, dvel
+    torch.cuda.empty_cache()
+
+    # batched persistent density (one graph launch) against the per-tree loop
+    sizes = syn.group_sizes(20000, 20, 200000, seed=4)
+    gp, gv, gm, off = syn.plummer_groups(sizes, seed=4)
+    B = BatchedDensity(torch.from_numpy(gp).cuda(), torch.from_numpy(gm).cuda(),
+                       torch.from_numpy(off).cuda(), bucket_size=0, device=True)
+    rho = torch.empty(len(gm), dtype=torch.float64, device="cuda")
+    B.density(32, use_graph=True, out=rho)
+    B.density_pertree(32, out=rho)
+    batched_ms = _timed(lambda: B.density(32, use_graph=True, out=rho), reps, flush)
+    pertree_ms = _timed(lambda: B.density_pertree(32, out=rho), 2, flush)
+    b, qb, _ = B.params()
+    out["batched_20000_groups_k32"] = {
+        "groups": len(sizes), "particles": int(len(gm)), "k": "min(32, n-1)",
+        "autotuned_bucket": b, "autotuned_query_bucket": qb,
+        "batched_graph_ms": batched_ms, "pertree_loop_ms": pertree_ms,
+        "speedup_batched_vs_pertree": pertree_ms / batched_ms,
+        "batched_queries_per_s": len(gm) / (batched_ms / 1e3),
+        "target": ">= 5x",
+    }
+    B.close()
+    del B, rho
+
+    # adjoint: d(sum w log rho)/d(x, m) with frozen neighbour lists against the forward
+    pos, mass = syn.clustered_box(N_FOF, BOX, seed=2)
+    dpos, dmass = torch.from_numpy(pos).cuda(), torch.from_numpy(mass).cuda()
+    w = torch.from_numpy(np.random.default_rng(5).standard_normal(N_FOF)).cuda()
+    t = KDTree(dpos, None, dmass, BUCKET, kerntype=0, device=True)
+    t.DensityAdjoint(32, w)
+    t.CalcDensity(32)
+    t.sync()
+    fwd_ms = _timed(lambda: t.CalcDensity(32), reps, flush)
+    adj_ms = _timed(lambda: t.DensityAdjoint(32, w), reps, flush)
+    pha = _trace(lib, lambda: t.DensityAdjoint(32, w))
+    t.close()
+    bwd = pha.get("adjoint_backward", float("nan"))
+    out["adjoint_clustered_2pow20_k32"] = {
+        "n": N_FOF, "k": 32, "forward_density_ms": fwd_ms,
+        "forward_with_saved_lists_plus_backward_ms": adj_ms,
+        "backward_kernel_ms": bwd,
+        "backward_over_forward": bwd / fwd_ms,
+        "phase_ms": {kk: round(v, 4) for kk, v in pha.items()},
+        "target": "backward <= 2x forward",
+    }
     return out
 
 

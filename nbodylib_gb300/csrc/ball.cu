@@ -67,7 +67,8 @@ __global__ void __launch_bounds__(32 * kWpb) k_ball(BallArgs a) {
   }
   int64_t base = (FILL && valid) ? a.offsets[q] : 0;
   int cnt = 0;
-  float thr = thresh_hi(a.r2);
+  float thr = thresh_hi(a.r2), r2_lo = thresh_lo(a.r2);
+  long long r2k = a.r2 > 0.0 ? dkey(a.r2) : 0;  // nothing is inside r2 <= 0 or NaN
   float eps = tv.eps, two_eps = __fmul_ru(2.f, tv.eps);
   int npass = tv.periodic ? 8 : 1;
   for (int pass = 0; pass < npass; pass++) {
@@ -104,9 +105,17 @@ __global__ void __launch_bounds__(32 * kWpb) k_ball(BallArgs a) {
               if (a.exclude_self && pass == 0 && ti == self) continue;
               float4 cf = w.sf[j];
               if (pair_d2_lo(qx, qy, qz, cf.x, cf.y, cf.z, two_eps) < thr) {
-                P4 c = w.sp[j];
-                double d2 = dist2_exact(xq[0], xq[1], xq[2], c.x, c.y, c.z);
-                if (d2 < a.r2) {
+                // FP32 upper bound inside the ball decides without FP64 unless the
+                // distance itself is wanted
+                double d2 = 0.0;
+                bool in = !(FILL && a.outd2) &&
+                          pair_d2_hi(qx, qy, qz, cf.x, cf.y, cf.z, two_eps) < r2_lo;
+                if (!in) {
+                  P4 c = w.sp[j];
+                  d2 = dist2_exact(xq[0], xq[1], xq[2], c.x, c.y, c.z);
+                  in = dkey(d2) < r2k;  // d2 < r2
+                }
+                if (in) {
                   if (FILL) {
                     if (base + cnt < a.offsets[q + 1]) {
                       a.out[base + cnt] = ti;

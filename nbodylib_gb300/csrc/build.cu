@@ -17,6 +17,7 @@
 // level by level, sorting each node by its split key with a bitonic network, and writes
 // the final tree-order arrays.
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "nbk_build.h"
@@ -654,7 +655,7 @@ int64_t count_nodes(int64_t n, int b) {
 // Build every tree of the forest. All arrays live on `st`. Returns NBK status.
 int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_in,
                  const double* d_mass_in, const double* d_vel_in, BuiltArrays& out,
-                 DevAlloc& alloc, cudaStream_t st) {
+                 DevAlloc& alloc, cudaStream_t st, NodeX* root_out) {
   Phase ph("build", st);
   // internal buffers cover only [p0, p0 + ntot), the particles of these trees
   int64_t p0 = trees.empty() ? 0 : trees[0].pstart, pend = 0;
@@ -676,15 +677,17 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
   NBK_TRY(alloc.get((void**)&IDb, sizeof(int) * ntot));
   NBK_TRY(alloc.get((void**)&d_err, sizeof(int)));
   NBK_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
-  k_init_soa<<<(unsigned)((ntot + 255) / 256), 256, 0, st>>>(d_pos_in + 3 * p0, Xa, Ya, Za, IDa, ntot,
-                                                            d_err); note_launch();
-  NBK_CUDA_TRY(cudaGetLastError());
 
-  // host plan of the global levels and of the local subtree roots
+  // The whole plan (every global level's nodes and chunks, every subtree handed to the
+  // per-CTA phase) depends only on the tree sizes, so it is computed on the host first
+  // and uploaded once; the levels then run back to back with no host round trip.
   std::vector<LRoot> lroots;
   struct HN {
     int64_t start, size;
     int h, nbase;
+  };
+  struct Level {
+    int g0, ng, c0, nc, buf;
   };
   std::vector<HN> cur, nxt;
   for (auto& t : trees) {
@@ -692,22 +695,18 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
     if (t.n <= kLocalMax) lroots.push_back({(int)(t.pstart - p0), (int)t.n, t.nbase, 0, 0, 0});
     else cur.push_back({t.pstart - p0, t.n, 0, t.nbase});
   }
-  int buf = 0;  // buffer holding the current level's particles
   std::vector<GNode> gn;
   std::vector<Chunk> ch;
-  GNode* d_g = nullptr;
-  Chunk* d_c = nullptr;
-  unsigned *d_hist = nullptr, *d_cl = nullptr, *d_ce = nullptr, *d_bl = nullptr, *d_be = nullptr;
-  size_t cap_g = 0, cap_c = 0;
+  std::vector<Level> levels;
+  int buf = 0, max_ng = 0;
   while (!cur.empty()) {
-    gn.clear();
-    ch.clear();
+    Level L{(int)gn.size(), (int)cur.size(), (int)ch.size(), 0, buf};
     for (size_t i = 0; i < cur.size(); i++) {
       GNode g{};
       g.start = (int)cur[i].start;
       g.size = (int)cur[i].size;
       g.node = cur[i].nbase + cur[i].h;
-      g.first_chunk = (int)ch.size();
+      g.first_chunk = (int)ch.size() - L.c0;
       int nc = (int)((cur[i].size + kChunk - 1) / kChunk);
       g.nchunks = nc;
       for (int c = 0; c < nc; c++) {
@@ -717,31 +716,61 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
       }
       gn.push_back(g);
     }
-    int ng = (int)gn.size(), nc = (int)ch.size();
-    if ((size_t)ng > cap_g) {
-      cap_g = std::max<size_t>(ng, 2 * cap_g);
-      NBK_TRY(alloc.get((void**)&d_g, sizeof(GNode) * cap_g));
-      NBK_TRY(alloc.get((void**)&d_hist, sizeof(unsigned) * 256 * cap_g));
-      NBK_CUDA_TRY(cudaMemsetAsync(d_hist, 0, sizeof(unsigned) * 256 * cap_g, st));
+    L.nc = (int)ch.size() - L.c0;
+    levels.push_back(L);
+    max_ng = std::max(max_ng, L.ng);
+    buf ^= 1;
+    nxt.clear();
+    for (auto& c : cur) {
+      int64_t l = (c.size - 1) / 2 + 1;
+      HN Lh = {c.start, l, 2 * c.h + 1, c.nbase};
+      HN Rh = {c.start + l, c.size - l, 2 * c.h + 2, c.nbase};
+      for (HN x : {Lh, Rh}) {
+        if (x.size <= kLocalMax) lroots.push_back({(int)x.start, (int)x.size, x.nbase, x.h, buf, 0});
+        else nxt.push_back(x);
+      }
     }
-    if ((size_t)nc > cap_c) {
-      cap_c = std::max<size_t>(nc, 2 * cap_c);
-      NBK_TRY(alloc.get((void**)&d_c, sizeof(Chunk) * cap_c));
-      NBK_TRY(alloc.get((void**)&d_cl, sizeof(unsigned) * cap_c));
-      NBK_TRY(alloc.get((void**)&d_ce, sizeof(unsigned) * cap_c));
-      NBK_TRY(alloc.get((void**)&d_bl, sizeof(unsigned) * cap_c));
-      NBK_TRY(alloc.get((void**)&d_be, sizeof(unsigned) * cap_c));
-    }
-    NBK_TRY(alloc.upload(d_g, gn.data(), sizeof(GNode) * ng, st));
-    NBK_TRY(alloc.upload(d_c, ch.data(), sizeof(Chunk) * nc, st));
-    const double* X = buf ? Xb : Xa;
-    const double* Y = buf ? Yb : Ya;
-    const double* Z = buf ? Zb : Za;
-    const int* I = buf ? IDb : IDa;
-    double* X2 = buf ? Xa : Xb;
-    double* Y2 = buf ? Ya : Yb;
-    double* Z2 = buf ? Za : Zb;
-    int* I2 = buf ? IDa : IDb;
+    cur.swap(nxt);
+  }
+  // one upload: [GNode...][Chunk...][LRoot...]
+  size_t bg = sizeof(GNode) * gn.size(), bc = sizeof(Chunk) * ch.size(),
+         br = sizeof(LRoot) * lroots.size();
+  std::vector<unsigned char> plan(bg + bc + br + 16);
+  memcpy(plan.data(), gn.data(), bg);
+  memcpy(plan.data() + bg, ch.data(), bc);
+  memcpy(plan.data() + bg + bc, lroots.data(), br);
+  unsigned char* d_plan;
+  NBK_TRY(alloc.get((void**)&d_plan, plan.size()));
+  NBK_CUDA_TRY(cudaMemcpyAsync(d_plan, plan.data(), plan.size(), cudaMemcpyHostToDevice, st));
+  GNode* d_gall = (GNode*)d_plan;
+  Chunk* d_call = (Chunk*)(d_plan + bg);
+  LRoot* d_r = (LRoot*)(d_plan + bg + bc);
+  unsigned *d_hist = nullptr, *d_cl = nullptr, *d_ce = nullptr, *d_bl = nullptr, *d_be = nullptr;
+  if (!levels.empty()) {
+    size_t ncall = std::max<size_t>(ch.size(), 1);
+    NBK_TRY(alloc.get((void**)&d_hist, sizeof(unsigned) * 256 * max_ng));
+    NBK_CUDA_TRY(cudaMemsetAsync(d_hist, 0, sizeof(unsigned) * 256 * max_ng, st));
+    NBK_TRY(alloc.get((void**)&d_cl, sizeof(unsigned) * ncall));
+    NBK_TRY(alloc.get((void**)&d_ce, sizeof(unsigned) * ncall));
+    NBK_TRY(alloc.get((void**)&d_bl, sizeof(unsigned) * ncall));
+    NBK_TRY(alloc.get((void**)&d_be, sizeof(unsigned) * ncall));
+  }
+  k_init_soa<<<(unsigned)((ntot + 255) / 256), 256, 0, st>>>(d_pos_in + 3 * p0, Xa, Ya, Za, IDa, ntot,
+                                                            d_err); note_launch();
+  NBK_CUDA_TRY(cudaGetLastError());
+  for (const Level& L : levels) {
+    GNode* d_g = d_gall + L.g0;
+    Chunk* d_c = d_call + L.c0;
+    unsigned *cl = d_cl + L.c0, *ce = d_ce + L.c0, *bl = d_bl + L.c0, *be = d_be + L.c0;
+    int ng = L.ng, nc = L.nc;
+    const double* X = L.buf ? Xb : Xa;
+    const double* Y = L.buf ? Yb : Ya;
+    const double* Z = L.buf ? Zb : Za;
+    const int* I = L.buf ? IDb : IDa;
+    double* X2 = L.buf ? Xa : Xb;
+    double* Y2 = L.buf ? Ya : Yb;
+    double* Z2 = L.buf ? Za : Zb;
+    int* I2 = L.buf ? IDa : IDb;
     k_gnode_reset<<<(ng + 127) / 128, 128, 0, st>>>(d_g, ng); note_launch();
     k_bbox<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z); note_launch();
     k_gnode_split<<<(ng + 127) / 128, 128, 0, st>>>(d_g, ng, out.node, out.nodex, (int)p0); note_launch();
@@ -750,27 +779,12 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
       k_hist<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, d_hist, shift); note_launch();
       k_select<<<(ng + 3) / 4, 128, 0, st>>>(d_g, ng, d_hist, shift); note_launch();
     }
-    k_count<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, d_cl, d_ce); note_launch();
-    k_chunk_scan<<<ng, kThreads, 0, st>>>(d_g, d_cl, d_ce, d_bl, d_be, out.nodex); note_launch();
-    k_scatter<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, I, X2, Y2, Z2, I2, d_bl, d_be, d_err); note_launch();
+    k_count<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, cl, ce); note_launch();
+    k_chunk_scan<<<ng, kThreads, 0, st>>>(d_g, cl, ce, bl, be, out.nodex); note_launch();
+    k_scatter<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, I, X2, Y2, Z2, I2, bl, be, d_err); note_launch();
     NBK_CUDA_TRY(cudaGetLastError());
-    buf ^= 1;
-    nxt.clear();
-    for (auto& c : cur) {
-      int64_t l = (c.size - 1) / 2 + 1;
-      HN L = {c.start, l, 2 * c.h + 1, c.nbase};
-      HN Rr = {c.start + l, c.size - l, 2 * c.h + 2, c.nbase};
-      for (HN x : {L, Rr}) {
-        if (x.size <= kLocalMax) lroots.push_back({(int)x.start, (int)x.size, x.nbase, x.h, buf, 0});
-        else nxt.push_back(x);
-      }
-    }
-    cur.swap(nxt);
   }
   if (!lroots.empty()) {
-    LRoot* d_r;
-    NBK_TRY(alloc.get((void**)&d_r, sizeof(LRoot) * lroots.size()));
-    NBK_TRY(alloc.upload(d_r, lroots.data(), sizeof(LRoot) * lroots.size(), st));
     size_t sm = local_build_smem();
     static bool attr_set = false;
     if (!attr_set) {
@@ -783,6 +797,9 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
         out.pos, out.posf, out.vel, out.perm, d_err, (int)p0); note_launch();
     NBK_CUDA_TRY(cudaGetLastError());
   }
+  if (root_out && !trees.empty())
+    NBK_CUDA_TRY(cudaMemcpyAsync(root_out, out.nodex + trees[0].nbase, sizeof(NodeX),
+                                 cudaMemcpyDeviceToHost, st));
   int h_err = 0;
   NBK_CUDA_TRY(cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
   NBK_CUDA_TRY(cudaStreamSynchronize(st));

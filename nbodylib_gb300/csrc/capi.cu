@@ -494,11 +494,10 @@ int nbk_create(const double* pos, const double* vel, const double* mass, int64_t
     d_mass = m;
   }
   std::vector<TreeSpec> trees{{0, n, 0}};
-  NBK_TRY(build_forest(trees, bucket_size, d_pos, d_mass, d_vel, A, alloc, st));
-  // FP32 rounding bound for coordinates and image coordinates
+  // the root's exact box comes back with the build's own final synchronisation
   NodeX root;
-  NBK_CUDA_TRY(cudaMemcpyAsync(&root, A.nodex, sizeof(NodeX), cudaMemcpyDeviceToHost, st));
-  NBK_CUDA_TRY(cudaStreamSynchronize(st));
+  NBK_TRY(build_forest(trees, bucket_size, d_pos, d_mass, d_vel, A, alloc, st, &root));
+  // FP32 rounding bound for coordinates and image coordinates
   double maxabs = 0;
   for (int d = 0; d < 3; d++)
     maxabs = std::max(maxabs, std::max(std::fabs(root.lo[d]), std::fabs(root.hi[d])));

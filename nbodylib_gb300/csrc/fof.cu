@@ -30,7 +30,7 @@ __device__ __forceinline__ int ld_parent(const int* p, int x) {
   return *((volatile const int*)p + x);
 }
 
-__device__ int find_root(int* parent, int x, int* err) {
+__device__ __forceinline__ int find_root(int* parent, int x, int* err) {
   for (int it = 0; it < kCap; it++) {
     int p = ld_parent(parent, x);
     if (p == x) return x;
@@ -42,7 +42,7 @@ __device__ int find_root(int* parent, int x, int* err) {
   return x;
 }
 
-__device__ void unite(int* parent, int a, int b, int* err) {
+__device__ __forceinline__ void unite(int* parent, int a, int b, int* err) {
   for (int it = 0; it < 1 << 20; it++) {
     a = find_root(parent, a, err);
     b = find_root(parent, b, err);
@@ -113,6 +113,7 @@ __global__ void __launch_bounds__(32 * kWpb) k_link(FofArgs a) {
   P4 me = tv.pos[self];
   double x0[3] = {me.x, me.y, me.z};
   float thr = thresh_hi(a.ll2), ll2_lo = thresh_lo(a.ll2);
+  long long ll2k = a.ll2 > 0.0 ? dkey(a.ll2) : 0;  // no link for ll2 <= 0 or NaN
   float eps = tv.eps, two_eps = __fmul_ru(2.f, tv.eps);
   int myroot = find_root(a.parent, self, a.err);  // cached; refreshed when it goes stale
   int npass = tv.periodic ? 8 : 1;
@@ -166,9 +167,14 @@ __global__ void __launch_bounds__(32 * kWpb) k_link(FofArgs a) {
               if (pass == 0 && ti <= self) continue;
               float4 cf = w.sf[j];
               if (pair_d2_lo(qx, qy, qz, cf.x, cf.y, cf.z, two_eps) < thr) {
-                P4 c = w.sp[j];
-                double d2 = dist2_exact(xq[0], xq[1], xq[2], c.x, c.y, c.z);
-                if (d2 < a.ll2 && find_root(a.parent, ti, a.err) != myroot) {
+                // decided in FP32 when the upper bound is already inside; only pairs
+                // within a few FP32 ulps of the linking length take the FP64 test
+                bool in = pair_d2_hi(qx, qy, qz, cf.x, cf.y, cf.z, two_eps) < ll2_lo;
+                if (!in) {
+                  P4 c = w.sp[j];
+                  in = dkey(dist2_exact(xq[0], xq[1], xq[2], c.x, c.y, c.z)) < ll2k;
+                }
+                if (in && find_root(a.parent, ti, a.err) != myroot) {
                   unite(a.parent, self, ti, a.err);
                   myroot = find_root(a.parent, self, a.err);
                 }

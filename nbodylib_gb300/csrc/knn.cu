@@ -45,12 +45,12 @@ __device__ __forceinline__ void heap_sift(WarpSmem<KMAX>& w, int lane, int K, in
     double dc = w.hd[c][lane];
     if (c + 1 < K) {
       double dc2 = w.hd[c + 1][lane];
-      if (dc2 > dc) {
+      if (dkey(dc2) > dkey(dc)) {
         c = c + 1;
         dc = dc2;
       }
     }
-    if (d >= dc) break;
+    if (dkey(d) >= dkey(dc)) break;
     w.hd[pos][lane] = dc;
     w.hi[pos][lane] = w.hi[c][lane];
     pos = c;
@@ -77,7 +77,8 @@ __device__ void traverse(const TreeView& tv, WarpSmem<KMAX>& w, int lane, bool a
   float qx = __double2float_rn(xq[0]), qy = __double2float_rn(xq[1]),
         qz = __double2float_rn(xq[2]);
   float eps = tv.eps, two_eps = __fmul_ru(2.f, tv.eps);
-  float thr = thresh_hi(top);
+  long long topk = dkey(top);
+  float thr = thresh_hi_bits(topk);
   int sp = 0;
   if (lane == 0) w.stk[0] = 0;
   sp = 1;
@@ -105,12 +106,14 @@ __device__ void traverse(const TreeView& tv, WarpSmem<KMAX>& w, int lane, bool a
               P4 c = w.sp[j];
               double d2 = dist2_exact(xq[0], xq[1], xq[2], c.x, c.y, c.z);
               int ti = r.start + c0 + j;
-              bool ok = d2 < top;
-              if (exclude_self) ok = ok && ti != self && d2 > 0.0;
+              long long dk = dkey(d2);
+              bool ok = dk < topk;  // d2 < top
+              if (exclude_self) ok = ok && ti != self && dk != 0;
               if (ok) {
                 heap_sift<KMAX>(w, lane, K, 0, d2, ti);
                 top = w.hd[0][lane];
-                thr = thresh_hi(top);
+                topk = dkey(top);
+                thr = thresh_hi_bits(topk);
               }
             }
           }
@@ -181,6 +184,7 @@ __device__ void run_warp(const KnnArgs& a, const TreeView& tv, WarpSmem<KMAX>& w
 
   const int kr = a.kernres;
   const double delta = 2.0 / (double)(kr - 1);
+  const double inv_delta = 0.5 * (double)(kr - 1);  // exact
   if (EPI == kEpiNN) {
     int Kc = K;
     double d;
@@ -208,16 +212,19 @@ __device__ void run_warp(const KnnArgs& a, const TreeView& tv, WarpSmem<KMAX>& w
   P4 me = tv.pos[self];
   if (EPI == kEpiDensity || EPI == kEpiDensVel || EPI == kEpiDensPart || EPI == kEpiDensSave) {
     // KDCalcSmoothQuantities.cxx:260-286
+    // One reciprocal per query replaces the per-neighbour divisions (r/h and the table
+    // step); the density moves by a few units in the last place, far inside 1e-12.
     double hh = 0.5 * __dsqrt_rn(top);
-    double norm = 1.0 / pow(hh, 3.0);
+    double ih = 1.0 / hh;
+    double norm = dmul(dmul(ih, ih), ih);  // 1 / h^3 (the reference takes pow(h, 3))
     double acc = 0.0;
     for (int s = 0; s < K; s++) {
       double d2 = w.hd[s][lane];
       int j = w.hi[s][lane];
       double rij = __dsqrt_rn(d2);
-      double q = __ddiv_rn(rij, hh);
+      double q = dmul(rij, ih);
       int ci = (int)dmul(dmul(q, 0.5), (double)(kr - 1));
-      double W = wsm(q, ci, kr, delta, T);
+      double W = wsm_mul(q, ci, kr, delta, inv_delta, T);
       double mj = tv.pos[j].m;
       if (EPI == kEpiDensPart) {
         acc = dadd(acc, dmul(dmul(W, norm), mj));
@@ -249,19 +256,20 @@ __device__ void run_warp(const KnnArgs& a, const TreeView& tv, WarpSmem<KMAX>& w
       }
       for (int s = ns; s < K; s++) {
         double d = w.hd[s][lane];
-        if (d < w.hd[0][lane]) heap_sift<KMAX>(w, lane, ns, 0, d, w.hi[s][lane]);
+        if (dkey(d) < dkey(w.hd[0][lane])) heap_sift<KMAX>(w, lane, ns, 0, d, w.hi[s][lane]);
       }
     }
-    double vmax = 0.0;
-    for (int s = 0; s < ns; s++) vmax = fmax(vmax, w.hd[s][lane]);
-    double hh = 0.5 * vmax;
-    double norm = 1.0 / pow(hh, 3.0);
+    long long vmaxk = 0;
+    for (int s = 0; s < ns; s++) vmaxk = max(vmaxk, dkey(w.hd[s][lane]));
+    double hh = 0.5 * __longlong_as_double(vmaxk);
+    double ih = 1.0 / hh;
+    double norm = dmul(dmul(ih, ih), ih);
     double acc = 0.0;
     for (int s = 0; s < ns; s++) {
       double rij = w.hd[s][lane];
-      double q = __ddiv_rn(rij, hh);
+      double q = dmul(rij, ih);
       int ci = (int)dmul(dmul(q, 0.5), (double)(kr - 1));
-      acc = dadd(acc, dmul(wsm(q, ci, kr, delta, T), norm));
+      acc = dadd(acc, dmul(wsm_mul(q, ci, kr, delta, inv_delta, T), norm));
     }
     if (EPI == kEpiVelPart) a.vden[qi] = acc;
     else a.vden[self] = acc;

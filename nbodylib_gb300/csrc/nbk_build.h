@@ -51,9 +51,11 @@ void dev_free(void* p, cudaStream_t st);
 int64_t heap_slots(int64_t n, int b);
 int64_t count_nodes(int64_t n, int b);
 size_t local_build_smem();
+// Builds every tree of the forest; if root_out is given, the first tree's root node
+// (exact bounding box) is copied there before the build's final synchronisation.
 int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_in,
                  const double* d_mass_in, const double* d_vel_in, BuiltArrays& out,
-                 DevAlloc& alloc, cudaStream_t st);
+                 DevAlloc& alloc, cudaStream_t st, NodeX* root_out = nullptr);
 
 // ---- kNN family
 enum Epi : int {

@@ -132,10 +132,41 @@ __device__ __forceinline__ float pair_d2_lo(float qx, float qy, float qz, float 
   float dz = fmaxf(0.f, __fsub_rd(fabsf(__fsub_rz(qz, cz)), two_eps));
   return __fadd_rd(__fadd_rd(__fmul_rd(dx, dx), __fmul_rd(dy, dy)), __fmul_rd(dz, dz));
 }
+// Upper bound of the squared distance between a query and a particle (the counterpart of
+// pair_d2_lo): below thresh_lo(t) it proves the FP64 distance is below t without FP64 work.
+__device__ __forceinline__ float pair_d2_hi(float qx, float qy, float qz, float cx, float cy,
+                                            float cz, float two_eps) {
+  float dx = __fadd_ru(qx >= cx ? __fsub_ru(qx, cx) : __fsub_ru(cx, qx), two_eps);
+  float dy = __fadd_ru(qy >= cy ? __fsub_ru(qy, cy) : __fsub_ru(cy, qy), two_eps);
+  float dz = __fadd_ru(qz >= cz ? __fsub_ru(qz, cz) : __fsub_ru(cz, qz), two_eps);
+  return __fadd_ru(__fadd_ru(__fmul_ru(dx, dx), __fmul_ru(dy, dy)), __fmul_ru(dz, dz));
+}
 // FP32 threshold above any value whose FP64 counterpart could still be below t.
 __device__ __forceinline__ float thresh_hi(double t) {
   float f = __double2float_ru(t);
   return __fmul_ru(f, 1.0f + 1.0f / 1048576.0f);
+}
+
+// ---- integer forms for non-negative doubles (squared distances, |dv|). Their bit
+// patterns read as signed 64-bit integers order exactly as the values do, so compares
+// and the FP32 threshold run on the integer pipe; GB300's FP64 pipe retires only about
+// two operations per SM clock and is kept for the arithmetic.
+__device__ __forceinline__ long long dkey(double v) { return __double_as_longlong(v); }
+// An FP32 value >= v (v >= 0 given by its bits), from the bits alone: the mantissa is
+// truncated to 23 bits and bumped by one unit when anything was cut; values below the
+// smallest normal FP32 map to it, values beyond the FP32 range to +inf.
+__device__ __forceinline__ float f32_above(long long bits) {
+  unsigned long long u = (unsigned long long)bits;
+  int e = (int)(u >> 52);  // sign bit is 0
+  if (e < 1023 - 126) return __uint_as_float(0x00800000u);
+  if (e > 1023 + 127) return __uint_as_float(0x7f800000u);
+  unsigned f = ((unsigned)(e - 1023 + 127) << 23) | (unsigned)((u >> 29) & 0x7fffffu);
+  if (u & 0x1fffffffull) f += 1u;  // a carry into the exponent is still an upper bound
+  return __uint_as_float(f);
+}
+// thresh_hi for a non-negative t given by its bits.
+__device__ __forceinline__ float thresh_hi_bits(long long tbits) {
+  return __fmul_ru(f32_above(tbits), 1.0f + 1.0f / 1048576.0f);
 }
 // FP32 threshold below which an FP64 value is certainly below t (for "all inside").
 __device__ __forceinline__ float thresh_lo(double t) {
@@ -148,31 +179,23 @@ __device__ __forceinline__ float thresh_lo(double t) {
 // dimension the signed wall distance, otherwise sqrt of the summed squares).
 __device__ __forceinline__ double reflect(const double x0[3], double xp[3], const double p[3],
                                           int mask) {
-  xp[0] = x0[0];
-  xp[1] = x0[1];
-  xp[2] = x0[2];
-  int cnt = (mask & 1) + ((mask >> 1) & 1) + ((mask >> 2) & 1);
-  if (cnt == 1) {
-    int k = (mask & 1) ? 0 : ((mask & 2) ? 1 : 2);
-    if (x0[k] < p[k] / 2.0) {
-      xp[k] = dadd(x0[k], p[k]);
-      return x0[k];
-    }
-    xp[k] = dsub(x0[k], p[k]);
-    return -xp[k];
-  }
-  double s = 0.0;
+  // every index is a compile-time constant after unrolling, so the arrays stay in registers
+  double s = 0.0, s1 = 0.0;
 #pragma unroll
   for (int k = 0; k < 3; k++) {
+    xp[k] = x0[k];
     if (!((mask >> k) & 1)) continue;
     if (x0[k] < p[k] / 2.0) {
       xp[k] = dadd(x0[k], p[k]);
+      s1 = x0[k];
       s = dadd(s, dmul(x0[k], x0[k]));
     } else {
       xp[k] = dsub(x0[k], p[k]);
+      s1 = -xp[k];
       s = dadd(s, dmul(xp[k], xp[k]));
     }
   }
+  if (__popc(mask) == 1) return s1;
   return __dsqrt_rn(s);
 }
 // The order in which the reference searches the images: x, y, z, xy, xz, yz, xyz
@@ -184,6 +207,18 @@ __device__ __forceinline__ double wsm(double r, int i, int size, double delta, c
   if (i < size - 1) {
     double xi = x[i], xj = x[i + 1];
     return dadd(xi, __ddiv_rn(dmul(dsub(xj, xi), dsub(r, dmul(delta, (double)i))), delta));
+  }
+  return x[i];
+}
+// The same interpolation with the division by delta replaced by a multiplication by
+// inv_delta = (size - 1) / 2, which is exact in FP64; the result differs from wsm() by a
+// few units in the last place (the interpolation is continuous across cells, so the
+// cell index may come from a quotient that differs in its last bit too).
+__device__ __forceinline__ double wsm_mul(double r, int i, int size, double delta,
+                                          double inv_delta, const double* x) {
+  if (i < size - 1) {
+    double xi = x[i], xj = x[i + 1];
+    return dadd(xi, dmul(dmul(dsub(xj, xi), dsub(r, dmul(delta, (double)i))), inv_delta));
   }
   return x[i];
 }
