@@ -247,17 +247,19 @@ def run_gpu(args, world, rank, local):
     return result
 
 
-def _timed(fn, reps, flush=None):
-    """Mean CUDA-event milliseconds of fn() over reps calls (L2 flushed before each)."""
+def _timed(fn, reps, flush=None, stream=None):
+    """Mean CUDA-event milliseconds of fn() over reps calls (L2 flushed before each), the
+    events recorded on the stream the work is launched on."""
     import torch
     ms = []
     for _ in range(reps):
         if flush is not None:
             flush.zero_()
+            torch.cuda.synchronize()
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        s.record()
+        s.record(stream)
         fn()
-        e.record()
+        e.record(stream)
         torch.cuda.synchronize()
         ms.append(s.elapsed_time(e))
     return float(np.mean(ms))
@@ -356,27 +358,48 @@ def components(args, lib):
     del dpos, dmass, dvel
     torch.cuda.empty_cache()
 
-    # batched persistent density (one graph launch) against the per-tree loop
+    # batched persistent density against the plain per-tree loop on the power-law group
+    # batch: build + search (a new batch of groups each time, as a halo finder sees them)
+    # and search alone (graph replay against one launch per group over the same forest)
     sizes = syn.group_sizes(20000, 20, 200000, seed=4)
     gp, gv, gm, off = syn.plummer_groups(sizes, seed=4)
-    B = BatchedDensity(torch.from_numpy(gp).cuda(), torch.from_numpy(gm).cuda(),
-                       torch.from_numpy(off).cuda(), bucket_size=0, device=True)
+    dgp, dgm, doff = (torch.from_numpy(a).cuda() for a in (gp, gm, off))
+    st = torch.cuda.Stream()
     rho = torch.empty(len(gm), dtype=torch.float64, device="cuda")
+
+    def batched_build_search():
+        B = BatchedDensity(dgp, dgm, doff, bucket_size=BUCKET, device=True)
+        B.set_stream(st)
+        B.density(32, use_graph=False, out=rho)
+        B.close()
+
+    batched_build_search()
+    bbs_ms = _timed(batched_build_search, reps, flush, st)
+    B = BatchedDensity(dgp, dgm, doff, bucket_size=BUCKET, device=True)
+    B.set_stream(st)
     B.density(32, use_graph=True, out=rho)
-    B.density_pertree(32, out=rho)
-    batched_ms = _timed(lambda: B.density(32, use_graph=True, out=rho), reps, flush)
-    pertree_ms = _timed(lambda: B.density_pertree(32, out=rho), 2, flush)
-    b, qb, _ = B.params()
-    out["batched_20000_groups_k32"] = {
-        "groups": len(sizes), "particles": int(len(gm)), "k": "min(32, n-1)",
-        "autotuned_bucket": b, "autotuned_query_bucket": qb,
-        "batched_graph_ms": batched_ms, "pertree_loop_ms": pertree_ms,
-        "speedup_batched_vs_pertree": pertree_ms / batched_ms,
-        "batched_queries_per_s": len(gm) / (batched_ms / 1e3),
-        "target": ">= 5x",
-    }
+    B.density_pertree_search(32, out=rho)
+    graph_ms = _timed(lambda: B.density(32, use_graph=True, out=rho), reps, flush, st)
+    loop_search_ms = _timed(lambda: B.density_pertree_search(32, out=rho), 2, flush, st)
+    pertree_ms = _timed(lambda: B.density_pertree(32, out=rho), 1, flush, st)
     B.close()
-    del B, rho
+    Bt = BatchedDensity(dgp, dgm, doff, bucket_size=0, device=True)  # autotuned b, qb
+    bt, qbt, _ = Bt.params()
+    Bt.set_stream(st)
+    Bt.density(32, use_graph=True, out=rho)
+    graph_tuned_ms = _timed(lambda: Bt.density(32, use_graph=True, out=rho), reps, flush, st)
+    Bt.close()
+    out["batched_20000_groups_k32"] = {
+        "groups": len(sizes), "particles": int(len(gm)), "k": "min(32, n-1)", "bucket": BUCKET,
+        "build_plus_search": {"batched_ms": bbs_ms, "pertree_loop_ms": pertree_ms,
+                              "speedup": pertree_ms / bbs_ms},
+        "search_only": {"batched_graph_ms": graph_ms, "pertree_loop_ms": loop_search_ms,
+                        "speedup": loop_search_ms / graph_ms},
+        "autotuned": {"bucket": bt, "query_bucket": qbt, "batched_graph_ms": graph_tuned_ms},
+        "batched_queries_per_s": len(gm) / (graph_ms / 1e3),
+        "target": "batched >= 5x the per-tree loop",
+    }
+    del B, Bt, rho, dgp, dgm, doff
 
     # adjoint: d(sum w log rho)/d(x, m) with frozen neighbour lists against the forward
     pos, mass = syn.clustered_box(N_FOF, BOX, seed=2)
@@ -386,8 +409,8 @@ def components(args, lib):
     t.DensityAdjoint(32, w)
     t.CalcDensity(32)
     t.sync()
-    fwd_ms = _timed(lambda: t.CalcDensity(32), reps, flush)
-    adj_ms = _timed(lambda: t.DensityAdjoint(32, w), reps, flush)
+    fwd_ms = _timed(lambda: (t.CalcDensity(32), t.sync()), reps, flush)
+    adj_ms = _timed(lambda: (t.DensityAdjoint(32, w), t.sync()), reps, flush)
     pha = _trace(lib, lambda: t.DensityAdjoint(32, w))
     t.close()
     bwd = pha.get("adjoint_backward", float("nan"))

@@ -281,6 +281,9 @@ int nbk_batch_density(nbk_batch* batch, int k, double* rho, int use_graph);
 /* The plain comparator: the same density computed by one build + one kNN-density
    launch sequence per group, looping over groups on the host. */
 int nbk_batch_density_pertree(nbk_batch* batch, int k, double* rho);
+/* The search half of the plain comparator: one kNN-density launch per group over the
+   forest the batch already built, looping over groups on the host (no builds). */
+int nbk_batch_density_pertree_search(nbk_batch* batch, int k, double* rho);
 /* The leaf size and query-bucket size in use, and (when autotuned) the tuner's timings
    as JSON in tune_json (NUL-terminated, up to cap bytes). (No reference counterpart.) */
 int nbk_batch_get_params(const nbk_batch* batch, int32_t* bucket_size, int32_t* query_bucket,

@@ -438,8 +438,9 @@ int nbk_batch_density(nbk_batch* B, int k, double* rho, int use_graph) {
   BAPI_END
 }
 
-int nbk_batch_density_pertree(nbk_batch* B, int k, double* rho) {
-  BAPI_BEGIN
+// The plain method: per group, (optionally) a tree build and one kNN-density launch, in a
+// host loop over groups.
+static int pertree(nbk_batch* B, int k, double* rho, bool build) {
   if (!B || !rho || k < 1) {
     set_error("nbk_batch_density_pertree: invalid argument");
     return NBK_ERR_INVALID;
@@ -448,14 +449,15 @@ int nbk_batch_density_pertree(nbk_batch* B, int k, double* rho) {
   cudaStream_t st = B->st;
   NBK_CUDA_TRY(cudaMemsetAsync(B->d_err, 0, sizeof(int), st));
   NBK_CUDA_TRY(cudaMemsetAsync(B->d_rho_tree, 0, sizeof(double) * B->ntot, st));
-  // the plain method: per group, a tree build and one kNN-density launch, in a host loop
   for (int64_t g = 0; g < B->ngroups; g++) {
     const TreeSpec& ts = B->trees[g];
     if (ts.n < 2) continue;
-    DevAlloc alloc;
-    alloc.st = st;
-    std::vector<TreeSpec> one{ts};
-    NBK_TRY(build_forest(one, B->b, B->d_pos_in, B->d_mass_in, nullptr, B->arr, alloc, st));
+    if (build) {
+      DevAlloc alloc;
+      alloc.st = st;
+      std::vector<TreeSpec> one{ts};
+      NBK_TRY(build_forest(one, B->b, B->d_pos_in, B->d_mass_in, nullptr, B->arr, alloc, st));
+    }
     KnnArgs a = batch_args(B, std::min<int64_t>(k, ts.n - 1));
     a.tv.n = (int)ts.n;
     a.tv.pstart = (int)ts.pstart;
@@ -470,6 +472,17 @@ int nbk_batch_density_pertree(nbk_batch* B, int k, double* rho) {
     NBK_CUDA_TRY(cudaMemcpyAsync(rho, out, sizeof(double) * B->ntot, cudaMemcpyDeviceToHost, st));
   NBK_TRY(check_batch_err(B));
   return NBK_OK;
+}
+
+int nbk_batch_density_pertree(nbk_batch* B, int k, double* rho) {
+  BAPI_BEGIN
+  return pertree(B, k, rho, true);
+  BAPI_END
+}
+
+int nbk_batch_density_pertree_search(nbk_batch* B, int k, double* rho) {
+  BAPI_BEGIN
+  return pertree(B, k, rho, false);
   BAPI_END
 }
 

@@ -96,11 +96,11 @@ constexpr int kWpb = 8;
 
 struct FofSmem {
   float4 sf[32];
-  P4 sp[32];
+  int par[32];  // parents of the staged leaf particles, read once per leaf
   int stk[kStack];
 };
 
-__global__ void __launch_bounds__(32 * kWpb) k_link(FofArgs a) {
+__global__ void __launch_bounds__(32 * kWpb, 8) k_link(FofArgs a) {
   __shared__ FofSmem sm[kWpb];
   const unsigned FULL = 0xffffffffu;
   int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(32 * kWpb) k_link(FofArgs a) {
           int m = min(32, r.count - c0);
           if (lane < m) {
             w.sf[lane] = tv.posf[r.start + c0 + lane];
-            w.sp[lane] = tv.pos[r.start + c0 + lane];
+            w.par[lane] = ld_parent(a.parent, r.start + c0 + lane);
           }
           __syncwarp();
           if (need) {
@@ -165,18 +165,26 @@ __global__ void __launch_bounds__(32 * kWpb) k_link(FofArgs a) {
               int ti = r.start + c0 + j;
               // direct pass: the test is symmetric, so each pair is handled once
               if (pass == 0 && ti <= self) continue;
+              // a staged parent equal to our root proves one component for good (links
+              // and path halving never separate a component), so no root chase is needed
+              int pj = w.par[j];
+              if (pj == myroot || ti == myroot) continue;
               float4 cf = w.sf[j];
               if (pair_d2_lo(qx, qy, qz, cf.x, cf.y, cf.z, two_eps) < thr) {
                 // decided in FP32 when the upper bound is already inside; only pairs
                 // within a few FP32 ulps of the linking length take the FP64 test
                 bool in = pair_d2_hi(qx, qy, qz, cf.x, cf.y, cf.z, two_eps) < ll2_lo;
                 if (!in) {
-                  P4 c = w.sp[j];
+                  P4 c = tv.pos[ti];
                   in = dkey(dist2_exact(xq[0], xq[1], xq[2], c.x, c.y, c.z)) < ll2k;
                 }
-                if (in && find_root(a.parent, ti, a.err) != myroot) {
-                  unite(a.parent, self, ti, a.err);
-                  myroot = find_root(a.parent, self, a.err);
+                if (in) {
+                  int rt = find_root(a.parent, pj, a.err);
+                  if (rt != myroot) myroot = find_root(a.parent, myroot, a.err);
+                  if (rt != myroot) {
+                    unite(a.parent, self, ti, a.err);
+                    myroot = find_root(a.parent, self, a.err);
+                  }
                 }
               }
             }

@@ -305,3 +305,15 @@ class BatchedDensity:
         rho = self._out() if out is None else out
         _capi.check(self._lib.nbk_batch_density_pertree(self._h, k, _ptr(rho)))
         return rho
+
+    def density_pertree_search(self, k=32, out=None):
+        """The per-group search loop over the already-built forest (no builds)."""
+        rho = self._out() if out is None else out
+        _capi.check(self._lib.nbk_batch_density_pertree_search(self._h, k, _ptr(rho)))
+        return rho
+
+    def set_stream(self, stream):
+        """Run on a caller's CUDA stream (a torch Stream or a raw handle). Graph capture
+        needs a stream other than the legacy default stream."""
+        ptr = stream.cuda_stream if hasattr(stream, "cuda_stream") else stream
+        _capi.check(self._lib.nbk_batch_set_stream(self._h, ctypes.c_void_p(ptr)))

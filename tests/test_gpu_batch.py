@@ -34,6 +34,26 @@ def test_batched_density_vs_oracle(gpu, port_built, bucket):
     for use_graph in (False, True, True):
         assert_density_close(B.density(32, use_graph=use_graph), want, f"batched graph={use_graph}")
     assert_density_close(B.density_pertree(32), want, "per-tree loop")
+    assert_density_close(B.density_pertree_search(32), want, "per-tree search loop")
+    B.close()
+
+
+def test_batched_graph_on_caller_stream(gpu, port_built):
+    """A graph captured and replayed on a caller's torch stream gives the same density
+    as the host-array path, for device-resident inputs."""
+    import torch
+    sizes = syn.group_sizes(200, 20, 2000, seed=44)
+    pos, vel, mass, off = syn.plummer_groups(sizes, seed=44)
+    want = reference_batch(pos, mass, off, 32, 16)
+    st = torch.cuda.Stream()
+    B = BatchedDensity(torch.from_numpy(pos).cuda(), torch.from_numpy(mass).cuda(),
+                       torch.from_numpy(off).cuda(), bucket_size=16, device=True)
+    B.set_stream(st)
+    rho = torch.empty(len(mass), dtype=torch.float64, device="cuda")
+    for _ in range(3):
+        B.density(32, use_graph=True, out=rho)
+    st.synchronize()
+    assert_density_close(rho.cpu().numpy(), want, "graph on caller stream")
     B.close()
 
 
