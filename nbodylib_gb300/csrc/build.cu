@@ -13,8 +13,8 @@
 //   split     per node: spread, split dimension, target rank
 //   select    8 radix passes of 8 bits find the key of the median particle exactly
 //   partition stable 3-way (less / equal / greater) scatter into the other buffer
-// Phase 2: one CTA per subtree of <= kLocalMax particles finishes it in shared memory,
-// level by level, sorting each node by its split key with a bitonic network, and writes
+// Phase 2: one CTA per subtree of <= kLocalMax particles finishes it in shared memory:
+// one sort per dimension, then level by level stable splits of index lists; it writes
 // the final tree-order arrays.
 #include <algorithm>
 #include <cstring>
@@ -26,10 +26,9 @@ namespace nbk {
 
 namespace {
 
-constexpr int kChunk = 4096;
+constexpr int kChunk = 2048;  // 8 particles per thread, loads issued together
 constexpr int kThreads = 256;
 constexpr int kRounds = kChunk / kThreads;
-constexpr int kSortCap = 4 * kLocalMax;
 constexpr int kLevelCap = kLocalMax;  // level lists hold up to 2*size/(b+1) nodes
 
 struct GNode {
@@ -61,11 +60,6 @@ struct LRoot {
   int buf;          // which ping-pong buffer holds its particles
   int pad;
 };
-
-__device__ __forceinline__ double coord_of(const double* X, const double* Y, const double* Z,
-                                           int d, int i) {
-  return d == 0 ? X[i] : (d == 1 ? Y[i] : Z[i]);
-}
 
 __global__ void k_init_soa(const double* __restrict__ pos_in, double* X, double* Y, double* Z,
                            int* ID, int64_t n, int* err) {
@@ -109,15 +103,28 @@ __global__ void __launch_bounds__(kThreads) k_bbox(const Chunk* __restrict__ chu
                                                    const double* Z) {
   Chunk c = chunks[blockIdx.x];
   unsigned long long mn[3] = {~0ull, ~0ull, ~0ull}, mx[3] = {0ull, 0ull, 0ull};
-  for (int i = threadIdx.x; i < c.len; i += kThreads) {
-    int p = c.start + i;
-    unsigned long long k0 = okey(X[p]), k1 = okey(Y[p]), k2 = okey(Z[p]);
-    mn[0] = min(mn[0], k0);
-    mx[0] = max(mx[0], k0);
-    mn[1] = min(mn[1], k1);
-    mx[1] = max(mx[1], k1);
-    mn[2] = min(mn[2], k2);
-    mx[2] = max(mx[2], k2);
+  double vx[kRounds], vy[kRounds], vz[kRounds];
+#pragma unroll
+  for (int r = 0; r < kRounds; r++) {
+    int i = r * kThreads + threadIdx.x;
+    if (i < c.len) {
+      vx[r] = X[c.start + i];
+      vy[r] = Y[c.start + i];
+      vz[r] = Z[c.start + i];
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < kRounds; r++) {
+    int i = r * kThreads + threadIdx.x;
+    if (i < c.len) {
+      unsigned long long k0 = okey(vx[r]), k1 = okey(vy[r]), k2 = okey(vz[r]);
+      mn[0] = min(mn[0], k0);
+      mx[0] = max(mx[0], k0);
+      mn[1] = min(mn[1], k1);
+      mx[1] = max(mx[1], k1);
+      mn[2] = min(mn[2], k2);
+      mx[2] = max(mx[2], k2);
+    }
   }
   __shared__ unsigned long long s[6][kThreads / 32];
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -204,9 +211,25 @@ __global__ void __launch_bounds__(kThreads) k_hist(const Chunk* __restrict__ chu
   __syncthreads();
   int d = s.dim;
   unsigned long long mask = s.mask, prefix = s.prefix;
-  for (int i = threadIdx.x; i < c.len; i += kThreads) {
-    unsigned long long key = okey(coord_of(X, Y, Z, d, c.start + i));
-    if ((key & mask) == prefix) atomicAdd(&h[(key >> shift) & 255], 1u);
+  const double* C = d == 0 ? X : (d == 1 ? Y : Z);
+  double v[kRounds];
+#pragma unroll
+  for (int r = 0; r < kRounds; r++) {
+    int i = r * kThreads + threadIdx.x;
+    if (i < c.len) v[r] = C[c.start + i];
+  }
+  // the keys of one node share their leading digits, so most lanes of a warp hit the same
+  // bin: lanes are grouped by digit and one atomic per distinct digit is issued
+#pragma unroll
+  for (int r = 0; r < kRounds; r++) {
+    int i = r * kThreads + threadIdx.x;
+    int digit = -1;
+    if (i < c.len) {
+      unsigned long long key = okey(v[r]);
+      if ((key & mask) == prefix) digit = (int)((key >> shift) & 255);
+    }
+    unsigned peers = __match_any_sync(0xffffffffu, digit);
+    if (digit >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&h[digit], __popc(peers));
   }
   __syncthreads();
   for (int i = threadIdx.x; i < 256; i += kThreads)
@@ -301,10 +324,20 @@ __global__ void __launch_bounds__(kThreads) k_count(const Chunk* __restrict__ ch
   const GNode& s = g[c.g];
   unsigned long long piv = s.prefix;
   unsigned a = 0, e = 0;
-  for (int i = threadIdx.x; i < c.len; i += kThreads) {
-    unsigned long long key = okey(coord_of(X, Y, Z, s.dim, c.start + i));
-    a += key < piv;
-    e += key == piv;
+  const double* C = s.dim == 0 ? X : (s.dim == 1 ? Y : Z);
+  double v[kRounds];
+#pragma unroll
+  for (int r = 0; r < kRounds; r++) {
+    int i = r * kThreads + threadIdx.x;
+    if (i < c.len) v[r] = C[c.start + i];
+  }
+#pragma unroll
+  for (int r = 0; r < kRounds; r++) {
+    if (r * kThreads + (int)threadIdx.x < c.len) {
+      unsigned long long key = okey(v[r]);
+      a += key < piv;
+      e += key == piv;
+    }
   }
   for (int o = 16; o > 0; o >>= 1) {
     a += __shfl_xor_sync(0xffffffffu, a, o);
@@ -365,9 +398,14 @@ __global__ void __launch_bounds__(kThreads) k_chunk_scan(GNode* g, const unsigne
 
 __global__ void __launch_bounds__(kThreads) k_scatter(const Chunk* __restrict__ chunks,
                                                       const GNode* __restrict__ g,
-                                                      const double* X, const double* Y,
-                                                      const double* Z, const int* ID, double* X2,
-                                                      double* Y2, double* Z2, int* ID2,
+                                                      const double* __restrict__ X,
+                                                      const double* __restrict__ Y,
+                                                      const double* __restrict__ Z,
+                                                      const int* __restrict__ ID,
+                                                      double* __restrict__ X2,
+                                                      double* __restrict__ Y2,
+                                                      double* __restrict__ Z2,
+                                                      int* __restrict__ ID2,
                                                       const unsigned* base_less,
                                                       const unsigned* base_eq, int* err) {
   __shared__ unsigned wsum[32];
@@ -380,52 +418,66 @@ __global__ void __launch_bounds__(kThreads) k_scatter(const Chunk* __restrict__ 
   int kleft = (s.size - 1) / 2 + 1;
   int right0 = s.start + kleft;
   int excess = s.total_eq - s.need_eq;
-  unsigned run_l = 0, run_e = 0, run_g = 0;
+  const double* C = s.dim == 0 ? X : (s.dim == 1 ? Y : Z);
+  // each thread owns kRounds consecutive particles, so one block scan of the packed
+  // (less, equal) counts orders the whole chunk stably; greater = position - less - equal
+  int i0 = threadIdx.x * kRounds;
+  unsigned cls = 0, nl = 0, ne = 0;
+#pragma unroll
   for (int r = 0; r < kRounds; r++) {
-    int i = r * kThreads + threadIdx.x;
-    bool valid = i < c.len;
-    unsigned long long key = 0;
-    int p = c.start + i;
-    if (valid) key = okey(coord_of(X, Y, Z, s.dim, p));
-    unsigned fl = valid && key < piv, fe = valid && key == piv, fg = valid && key > piv;
-    unsigned el = block_excl_scan(fl, &tot, wsum);
-    unsigned tl = tot;
-    unsigned ee = block_excl_scan(fe, &tot, wsum);
-    unsigned te = tot;
-    unsigned eg = block_excl_scan(fg, &tot, wsum);
-    unsigned tg = tot;
-    if (valid) {
-      int dst;
-      if (fl) {
-        dst = s.start + (int)(bl + run_l + el);
-      } else if (fe) {
-        int e = (int)(be + run_e + ee);
-        dst = e < s.need_eq ? s.start + s.n_less + e : right0 + (e - s.need_eq);
-      } else {
-        dst = right0 + excess + (int)(bg + run_g + eg);
-      }
-      if (dst < s.start || dst >= s.start + s.size) {  // selection inconsistent: report
-        atomicExch(err, 2);
-        dst = p;
-      }
-      X2[dst] = X[p];
-      Y2[dst] = Y[p];
-      Z2[dst] = Z[p];
-      ID2[dst] = ID[p];
+    int i = i0 + r;
+    unsigned k = 3;
+    if (i < c.len) {
+      unsigned long long key = okey(C[c.start + i]);
+      k = key < piv ? 0u : (key == piv ? 1u : 2u);
+      nl += k == 0;
+      ne += k == 1;
     }
-    run_l += tl;
-    run_e += te;
-    run_g += tg;
+    cls |= k << (2 * r);
+  }
+  unsigned pre = block_excl_scan(nl | (ne << 16), &tot, wsum);
+  unsigned rl = bl + (pre & 0xffffu), re = be + (pre >> 16);
+  unsigned rg = bg + (unsigned)min(i0, c.len) - (pre & 0xffffu) - (pre >> 16);
+#pragma unroll
+  for (int r = 0; r < kRounds; r++) {
+    unsigned k = (cls >> (2 * r)) & 3u;
+    if (k == 3) continue;
+    int p = c.start + i0 + r;
+    int dst;
+    if (k == 0) {
+      dst = s.start + (int)rl++;
+    } else if (k == 1) {
+      int e = (int)re++;
+      dst = e < s.need_eq ? s.start + s.n_less + e : right0 + (e - s.need_eq);
+    } else {
+      dst = right0 + excess + (int)rg++;
+    }
+    if (dst < s.start || dst >= s.start + s.size) {  // selection inconsistent: report
+      atomicExch(err, 2);
+      dst = p;
+    }
+    X2[dst] = X[p];
+    Y2[dst] = Y[p];
+    Z2[dst] = Z[p];
+    ID2[dst] = ID[p];
   }
 }
 
-// ---- phase 2: one CTA per subtree of at most kLocalMax particles
+// ---- phase 2: one CTA per subtree of at most kLocalMax particles.
+// The subtree is sorted once along x, y and z (key, then local index). No level sorts
+// again: a node's bounding box is the first and last entry of its segment in each sorted
+// list, its median along the split dimension is the middle entry of that list, and the
+// four index lists (the three sorted lists and the particle order) are split stably into
+// the children's segments with one block scan per level.
 struct LNode {
-  int start;  // local start
-  int size;
-  int h;      // heap index within the tree
-  int dim;    // -1 leaf
+  short start, size;  // local range
+  int h;              // heap index within the tree
+  short kl;           // particles that go left (split nodes)
+  short child;        // slot of the left child in the next level's list
+  int dim;            // -1 leaf
 };
+
+constexpr int kSortN = 3 * kLocalMax;
 
 __global__ void __launch_bounds__(kThreads) k_local_build(
     const LRoot* __restrict__ roots, const double* Xa, const double* Ya, const double* Za,
@@ -433,192 +485,247 @@ __global__ void __launch_bounds__(kThreads) k_local_build(
     const double* __restrict__ mass_in, const double* __restrict__ vel_in, int b,
     NodeRec* node, NodeX* nodex, P4* pos, float4* posf, V4* vel, int* perm, int* err, int p0) {
   extern __shared__ __align__(16) unsigned char smem[];
-  double* cx = (double*)smem;
+  double* cx = (double*)smem;                                         // [kLocalMax]
   double* cy = cx + kLocalMax;
   double* cz = cy + kLocalMax;
-  unsigned long long* skey = (unsigned long long*)(cz + kLocalMax);
-  int* id = (int*)(skey + kSortCap);
-  unsigned short* sidx = (unsigned short*)(id + kLocalMax);
-  unsigned short* src = sidx + kSortCap;
-  LNode* lv = (LNode*)(src + kLocalMax);
+  unsigned long long* skey = (unsigned long long*)(cz + kLocalMax);  // [kSortN], sort only
+  unsigned* sc01 = (unsigned*)skey;             // after the sort: packed scans of lists 0,1
+  unsigned* sc23 = sc01 + kLocalMax;            //                 and of lists 2,3
+  short* node_at = (short*)(sc23 + kLocalMax);  // level slot of each position, -1 finished
+  unsigned char* left = (unsigned char*)(node_at + kLocalMax);  // per particle
+  int* id = (int*)(skey + kSortN);                              // [kLocalMax]
+  unsigned short* sidx = (unsigned short*)(id + kLocalMax);     // [kSortN]
+  unsigned short* lst = sidx + kSortN;                          // [2][4][kLocalMax]
+  LNode* lv = (LNode*)(lst + 8 * kLocalMax);                    // [kLevelCap]
   LNode* lv2 = lv + kLevelCap;
-  __shared__ int n_cur, n_split, max_split;
+  __shared__ int n_cur, n_next;
+  __shared__ unsigned wsum[32], tot;
+  const int K = kLocalMax;
 
   const LRoot R = roots[blockIdx.x];
+  const int S = R.size;
   const double* X = R.buf ? Xb : Xa;
   const double* Y = R.buf ? Yb : Ya;
   const double* Z = R.buf ? Zb : Za;
   const int* I = R.buf ? IDb : IDa;
-  for (int e = threadIdx.x; e < R.size; e += kThreads) {
+  for (int e = threadIdx.x; e < S; e += kThreads) {
     cx[e] = X[R.start + e];
     cy[e] = Y[R.start + e];
     cz[e] = Z[R.start + e];
     id[e] = I[R.start + e];
   }
+  __syncthreads();
+  int P = 1;
+  while (P < S) P <<= 1;
+  const int total = 3 * P;
+  for (int t = threadIdx.x; t < total; t += kThreads) {
+    int d = t / P, r = t - d * P;
+    if (r < S) {
+      skey[t] = okey(d == 0 ? cx[r] : (d == 1 ? cy[r] : cz[r]));
+      sidx[t] = (unsigned short)r;
+    } else {
+      skey[t] = ~0ull;
+      sidx[t] = 0xffff;
+    }
+  }
+  __syncthreads();
+  // three segments of P sorted at once; every segment ascending by (key, local index)
+  for (int kk = 2; kk <= P; kk <<= 1) {
+    for (int jj = kk >> 1; jj > 0; jj >>= 1) {
+      for (int t = threadIdx.x; t < total; t += kThreads) {
+        int u = t ^ jj;
+        if (u > t) {
+          bool up = ((t & (P - 1)) & kk) == 0;
+          unsigned long long a = skey[t], c = skey[u];
+          unsigned short ia = sidx[t], ic = sidx[u];
+          bool gt = (a > c) || (a == c && ia > ic);
+          if (gt == up) {
+            skey[t] = c;
+            skey[u] = a;
+            sidx[t] = ic;
+            sidx[u] = ia;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  unsigned short* cur = lst;
+  unsigned short* nxt = lst + 4 * K;
+  for (int t = threadIdx.x; t < 3 * S; t += kThreads) {
+    int d = t / S, i = t - d * S;
+    unsigned short q = sidx[d * P + i];
+    if (q >= S) {  // a padding slot inside the sorted range: report, keep in bounds
+      atomicExch(err, 3);
+      q = (unsigned short)i;
+    }
+    cur[d * K + i] = q;
+  }
+  for (int i = threadIdx.x; i < S; i += kThreads) {
+    cur[3 * K + i] = (unsigned short)i;
+    node_at[i] = 0;
+  }
   if (threadIdx.x == 0) {
-    lv[0].start = 0;
-    lv[0].size = R.size;
-    lv[0].h = R.h;
-    lv[0].dim = -1;
+    LNode r0;
+    r0.start = 0;
+    r0.size = (short)S;
+    r0.h = R.h;
+    r0.kl = 0;
+    r0.child = 0;
+    r0.dim = -1;
+    lv[0] = r0;
     n_cur = 1;
   }
   __syncthreads();
-  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  while (true) {
-    // A: bounding box and split dimension of every node of this level (warp per node)
-    for (int j = warp; j < n_cur; j += kThreads / 32) {
+  for (int depth = 0; depth < 64; depth++) {
+    if (threadIdx.x == 0) n_next = 0;
+    __syncthreads();
+    // A: bounding box, split dimension and median of every node of this level
+    for (int j = threadIdx.x; j < n_cur; j += kThreads) {
       LNode nd = lv[j];
-      double lo[3] = {DBL_MAX, DBL_MAX, DBL_MAX}, hi[3] = {-DBL_MAX, -DBL_MAX, -DBL_MAX};
-      for (int e = nd.start + lane; e < nd.start + nd.size; e += 32) {
-        lo[0] = fmin(lo[0], cx[e]);
-        hi[0] = fmax(hi[0], cx[e]);
-        lo[1] = fmin(lo[1], cy[e]);
-        hi[1] = fmax(hi[1], cy[e]);
-        lo[2] = fmin(lo[2], cz[e]);
-        hi[2] = fmax(hi[2], cz[e]);
-      }
-      for (int d = 0; d < 3; d++) {
-        for (int o = 16; o > 0; o >>= 1) {
-          lo[d] = fmin(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
-          hi[d] = fmax(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
-        }
-      }
-      if (lane == 0) {
-        int dim = -1;
-        if (nd.size > b) {
-          dim = 0;
-          double cur = dsub(hi[0], lo[0]);
-          for (int d = 1; d < 3; d++) {
-            double sp = dsub(hi[d], lo[d]);
-            if (sp > cur) {
-              dim = d;
-              cur = sp;
-            }
+      int a0 = nd.start, a1 = nd.start + nd.size - 1;
+      double lo[3] = {cx[cur[a0]], cy[cur[K + a0]], cz[cur[2 * K + a0]]};
+      double hi[3] = {cx[cur[a1]], cy[cur[K + a1]], cz[cur[2 * K + a1]]};
+      int dim = -1;
+      double split = 0.0;
+      if (nd.size > b) {
+        // DetermineSplitDim: the first strictly larger FP64 spread wins
+        dim = 0;
+        double spread = dsub(hi[0], lo[0]);
+        for (int d = 1; d < 3; d++) {
+          double sp = dsub(hi[d], lo[d]);
+          if (sp > spread) {
+            dim = d;
+            spread = sp;
           }
         }
-        lv[j].dim = dim;
-        write_node(node, nodex, R.nbase + nd.h, lo, hi, p0 + R.start + nd.start, nd.size, dim,
-                   0.0);
-      }
-    }
-    if (threadIdx.x == 0) {
-      n_split = 0;
-      max_split = 0;
-    }
-    __syncthreads();
-    // compact the split nodes to the front of lv2 (order preserved) and size the network
-    if (threadIdx.x == 0) {
-      int ns = 0, mx = 0;
-      for (int j = 0; j < n_cur; j++)
-        if (lv[j].dim >= 0) {
-          lv2[ns++] = lv[j];
-          mx = max(mx, lv[j].size);
-        }
-      n_split = ns;
-      max_split = mx;
-    }
-    __syncthreads();
-    if (n_split == 0) break;
-    int P = 1;
-    while (P < max_split) P <<= 1;
-    int total = n_split * P;
-    // B: fill sort keys (split-dimension key, local index); pad with +inf
-    for (int t = threadIdx.x; t < total; t += kThreads) {
-      int j = t / P, r = t - j * P;
-      LNode nd = lv2[j];
-      if (r < nd.size) {
-        int e = nd.start + r;
-        double v = nd.dim == 0 ? cx[e] : (nd.dim == 1 ? cy[e] : cz[e]);
-        skey[t] = okey(v);
-        sidx[t] = (unsigned short)e;
-      } else {
-        skey[t] = ~0ull;
-        sidx[t] = 0xffff;
-      }
-    }
-    for (int e = threadIdx.x; e < R.size; e += kThreads) src[e] = (unsigned short)e;
-    __syncthreads();
-    for (int kk = 2; kk <= P; kk <<= 1) {
-      for (int jj = kk >> 1; jj > 0; jj >>= 1) {
-        for (int t = threadIdx.x; t < total; t += kThreads) {
-          int u = t ^ jj;
-          if (u > t) {
-            // direction from the position inside the P-segment: every segment ascending
-            bool up = ((t & (P - 1)) & kk) == 0;
-            unsigned long long a = skey[t], c = skey[u];
-            unsigned short ia = sidx[t], ic = sidx[u];
-            bool gt = (a > c) || (a == c && ia > ic);
-            if (gt == up) {
-              skey[t] = c;
-              skey[u] = a;
-              sidx[t] = ic;
-              sidx[u] = ia;
-            }
-          }
-        }
-        __syncthreads();
-      }
-    }
-    // C: new order inside each split node = sorted order
-    for (int t = threadIdx.x; t < total; t += kThreads) {
-      int j = t / P, r = t - j * P;
-      LNode nd = lv2[j];
-      if (r < nd.size) {
-        unsigned short sx = sidx[t];
-        if (sx >= R.size) {  // a padding slot inside the node: report, keep in bounds
-          atomicExch(err, 3);
-          sx = (unsigned short)(nd.start + r);
-        }
-        src[nd.start + r] = sx;
-      }
-    }
-    __syncthreads();
-    double* tmp = (double*)skey;  // keys are no longer needed
-    for (int a = 0; a < 3; a++) {
-      double* arr = a == 0 ? cx : (a == 1 ? cy : cz);
-      for (int e = threadIdx.x; e < R.size; e += kThreads) tmp[e] = arr[src[e]];
-      __syncthreads();
-      for (int e = threadIdx.x; e < R.size; e += kThreads) arr[e] = tmp[e];
-      __syncthreads();
-    }
-    {
-      int* itmp = (int*)skey;
-      for (int e = threadIdx.x; e < R.size; e += kThreads) itmp[e] = id[src[e]];
-      __syncthreads();
-      for (int e = threadIdx.x; e < R.size; e += kThreads) id[e] = itmp[e];
-      __syncthreads();
-    }
-    // D: split values and the next level
-    if (threadIdx.x == 0) {
-      int nn = 0;
-      for (int j = 0; j < n_split; j++) {
-        LNode nd = lv2[j];
         int kl = (nd.size - 1) / 2 + 1;
-        int m = nd.start + kl - 1;
-        double v = nd.dim == 0 ? cx[m] : (nd.dim == 1 ? cy[m] : cz[m]);
-        nodex[R.nbase + nd.h].split_val = v;
-        LNode l = {nd.start, kl, 2 * nd.h + 1, -1};
-        LNode r = {nd.start + kl, nd.size - kl, 2 * nd.h + 2, -1};
-        lv[nn++] = l;
-        lv[nn++] = r;
+        int q = cur[dim * K + nd.start + kl - 1];
+        split = dim == 0 ? cx[q] : (dim == 1 ? cy[q] : cz[q]);
+        int slot = atomicAdd(&n_next, 2);
+        if (slot + 2 <= kLevelCap) {
+          LNode l, r;
+          l.start = nd.start;
+          l.size = (short)kl;
+          l.h = 2 * nd.h + 1;
+          r.start = (short)(nd.start + kl);
+          r.size = (short)(nd.size - kl);
+          r.h = 2 * nd.h + 2;
+          l.kl = r.kl = 0;
+          l.child = r.child = 0;
+          l.dim = r.dim = -1;
+          lv2[slot] = l;
+          lv2[slot + 1] = r;
+        } else {
+          atomicExch(err, 4);
+        }
+        nd.kl = (short)kl;
+        nd.child = (short)slot;
       }
-      n_cur = nn;
+      nd.dim = dim;
+      lv[j] = nd;
+      write_node(node, nodex, R.nbase + nd.h, lo, hi, p0 + R.start + nd.start, nd.size, dim,
+                 split);
     }
+    __syncthreads();
+    if (n_next == 0 || n_next > kLevelCap) break;
+    // B: which particles go left, read off the list of their node's split dimension
+    for (int t = threadIdx.x; t < 3 * S; t += kThreads) {
+      int d = t / S, i = t - d * S;
+      int j = node_at[i];
+      if (j >= 0) {
+        LNode nd = lv[j];
+        if (nd.dim == d) left[cur[d * K + i]] = (i - nd.start) < nd.kl;
+      }
+    }
+    __syncthreads();
+    // C: exclusive scans of the left flags of the four lists (two packed per word); each
+    // thread covers four consecutive positions
+    {
+      unsigned f01[4], f23[4], s01 = 0, s23 = 0;
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        int i = 4 * threadIdx.x + u;
+        unsigned a = 0, c = 0;
+        if (i < S) {
+          int j = node_at[i];
+          if (j >= 0 && lv[j].dim >= 0) {
+            a = left[cur[i]] | ((unsigned)left[cur[K + i]] << 16);
+            c = left[cur[2 * K + i]] | ((unsigned)left[cur[3 * K + i]] << 16);
+          }
+        }
+        f01[u] = s01;
+        f23[u] = s23;
+        s01 += a;
+        s23 += c;
+      }
+      unsigned b01 = block_excl_scan(s01, &tot, wsum);
+      unsigned b23 = block_excl_scan(s23, &tot, wsum);
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        int i = 4 * threadIdx.x + u;
+        if (i < S) {
+          sc01[i] = b01 + f01[u];
+          sc23[i] = b23 + f23[u];
+        }
+      }
+    }
+    __syncthreads();
+    // D: stable split of every list inside its node; positions of leaves stay put
+    for (int i = threadIdx.x; i < S; i += kThreads) {
+      int j = node_at[i];
+      if (j < 0) {
+#pragma unroll
+        for (int l = 0; l < 4; l++) nxt[l * K + i] = cur[l * K + i];
+        continue;
+      }
+      LNode nd = lv[j];
+      if (nd.dim < 0) {
+#pragma unroll
+        for (int l = 0; l < 4; l++) nxt[l * K + i] = cur[l * K + i];
+        node_at[i] = -1;
+        continue;
+      }
+      int rel = i - nd.start;
+      unsigned v01 = sc01[i] - sc01[nd.start], v23 = sc23[i] - sc23[nd.start];
+#pragma unroll
+      for (int l = 0; l < 4; l++) {
+        unsigned v = l < 2 ? v01 : v23;
+        int before = (int)((l & 1) ? (v >> 16) : (v & 0xffffu));  // left entries before i
+        unsigned short q = cur[l * K + i];
+        int dst = left[q] ? nd.start + before : nd.start + nd.kl + (rel - before);
+        if (dst < nd.start || dst >= nd.start + nd.size) {  // inconsistent split: report
+          atomicExch(err, 3);
+          dst = i;
+        }
+        nxt[l * K + dst] = q;
+      }
+      node_at[i] = (short)(rel < nd.kl ? nd.child : nd.child + 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) n_cur = n_next;
+    unsigned short* t = cur;
+    cur = nxt;
+    nxt = t;
+    LNode* tl = lv;
+    lv = lv2;
+    lv2 = tl;
     __syncthreads();
   }
-  // final tree-order arrays
-  for (int e = threadIdx.x; e < R.size; e += kThreads) {
+  // final tree-order arrays: the particle-order list holds every leaf contiguously
+  for (int e = threadIdx.x; e < S; e += kThreads) {
+    int q = cur[3 * K + e];
     int t = p0 + R.start + e;  // absolute tree index
-    int ii = p0 + id[e];  // absolute input index
+    int ii = p0 + id[q];       // absolute input index
     double m = mass_in ? mass_in[ii] : 1.0;
     P4 p;
-    p.x = cx[e];
-    p.y = cy[e];
-    p.z = cz[e];
+    p.x = cx[q];
+    p.y = cy[q];
+    p.z = cz[q];
     p.m = m;
     pos[t] = p;
-    posf[t] = make_float4(__double2float_rn(cx[e]), __double2float_rn(cy[e]),
-                          __double2float_rn(cz[e]), 0.f);
+    posf[t] = make_float4(__double2float_rn(p.x), __double2float_rn(p.y),
+                          __double2float_rn(p.z), 0.f);
     perm[t] = ii;
     if (vel && vel_in) vel[t] = make_v4(vel_in[3 * ii], vel_in[3 * ii + 1], vel_in[3 * ii + 2], 0.0);
   }
@@ -636,8 +743,8 @@ int depth_of(int64_t n, int b) {
 }  // namespace
 
 size_t local_build_smem() {
-  return sizeof(double) * 3 * kLocalMax + sizeof(unsigned long long) * kSortCap +
-         sizeof(int) * kLocalMax + sizeof(unsigned short) * (kSortCap + kLocalMax) +
+  return sizeof(double) * 3 * kLocalMax + sizeof(unsigned long long) * kSortN +
+         sizeof(int) * kLocalMax + sizeof(unsigned short) * (kSortN + 8 * kLocalMax) +
          sizeof(LNode) * 2 * kLevelCap;
 }
 

@@ -338,17 +338,23 @@ __global__ void k_compress(int* parent, int n) {
   parent[i] = x;
 }
 
-__global__ void k_flatten_count(int* parent, int n, int* cnt) {
+__global__ void k_flatten_count(int* parent, int n, int* cnt, int* err) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  int x = i;
-  while (true) {
-    int p = parent[x];
-    if (p == x) break;
-    x = p;
+  bool valid = i < n;
+  int x = valid ? i : -1;
+  if (valid) {
+    int it = 0;
+    for (; it < kCap; it++) {
+      int p = parent[x];
+      if (p == x) break;
+      x = p;
+    }
+    if (it == kCap) atomicExch(err, kErrIterCap);
+    parent[i] = x;  // no concurrent writers remain; roots are untouched
   }
-  parent[i] = x;  // no concurrent writers remain; roots are untouched
-  atomicAdd(&cnt[x], 1);
+  // neighbouring particles mostly share a root: one atomic per distinct root in the warp
+  unsigned peers = __match_any_sync(0xffffffffu, x);
+  if (valid && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&cnt[x], __popc(peers));
 }
 
 __global__ void k_valid(const int* parent, const int* cnt, int n, int minnum, int* flag) {
@@ -482,7 +488,7 @@ int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tr
   }
   Phase ph_label("fof_label", st);
   NBK_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * n, st));
-  k_flatten_count<<<(n + 255) / 256, 256, 0, st>>>(a.parent, n, cnt); note_launch();
+  k_flatten_count<<<(n + 255) / 256, 256, 0, st>>>(a.parent, n, cnt, a.err); note_launch();
   k_valid<<<(n + 255) / 256, 256, 0, st>>>(a.parent, cnt, n, minnum, flag); note_launch();
   k_scan_blocks<<<nb, 1024, 0, st>>>(flag, lbl, bsum, n); note_launch();
   k_scan_sums<<<1, 1024, 0, st>>>(bsum, nb, d_total); note_launch();
