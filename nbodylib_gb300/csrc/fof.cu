@@ -91,16 +91,33 @@ __global__ void k_prelink(FofArgs a) {
   }
 }
 
-constexpr int kStack = 64;
+constexpr int kStack = 64;    // depth-first stack of the criterion search (one lane)
 constexpr int kWpb = 8;
+constexpr int kFStack = 512;  // frontier stack of the link search (one warp)
+constexpr int kBatchLimit = kFStack - 128;
 
 struct FofSmem {
   float4 sf[32];
   int par[32];  // parents of the staged leaf particles, read once per leaf
-  int stk[kStack];
+  int stk[kFStack];
 };
 
-__global__ void __launch_bounds__(32 * kWpb, 8) k_link(FofArgs a) {
+// Lower bound of the squared distance between two boxes (FP32, directed rounding).
+__device__ __forceinline__ float boxbox_d2_lo(const NodeRec& r, const float qlo[3],
+                                              const float qhi[3]) {
+  float g[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++)
+    g[d] = fmaxf(0.f, fmaxf(__fsub_rd(r.lo[d], qhi[d]), __fsub_rd(qlo[d], r.hi[d])));
+  return __fadd_rd(__fadd_rd(__fmul_rd(g[0], g[0]), __fmul_rd(g[1], g[1])), __fmul_rd(g[2], g[2]));
+}
+
+// 2. One warp links 32 consecutive particles. The traversal is frontier-parallel: each
+// step pops up to 32 nodes from the warp's stack, lane i loads node i, drops it when it
+// lies farther than ll from the box around all of the warp's query points, and for a
+// compact node chases its union-find root, so the dependent loads of up to 32 nodes
+// overlap. The surviving nodes are then tested against every lane's own query.
+__global__ void __launch_bounds__(32 * kWpb, 4) k_link(FofArgs a) {
   __shared__ FofSmem sm[kWpb];
   const unsigned FULL = 0xffffffffu;
   int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -127,49 +144,92 @@ __global__ void __launch_bounds__(32 * kWpb, 8) k_link(FofArgs a) {
     if (!__any_sync(FULL, active)) continue;
     float qx = __double2float_rn(xq[0]), qy = __double2float_rn(xq[1]),
           qz = __double2float_rn(xq[2]);
+    // box around the active lanes' query points, widened by eps
+    float qlo[3], qhi[3];
+    {
+      float v[3] = {qx, qy, qz};
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        float lo = active ? __fsub_rd(v[d], eps) : FLT_MAX;
+        float hi = active ? __fadd_ru(v[d], eps) : -FLT_MAX;
+        for (int o = 16; o > 0; o >>= 1) {
+          lo = fminf(lo, __shfl_xor_sync(FULL, lo, o));
+          hi = fmaxf(hi, __shfl_xor_sync(FULL, hi, o));
+        }
+        qlo[d] = lo;
+        qhi[d] = hi;
+      }
+    }
     int sp = 1;
     if (lane == 0) w.stk[0] = 0;
     __syncwarp();
-    while (sp > 0) {
-      int h = w.stk[sp - 1];
-      sp--;
-      __syncwarp();
-      NodeRec r = tv.node[tv.nbase + h];
-      bool need = active && box_d2_lo(qx, qy, qz, eps, r) < thr;
-      if (need && node_compact(r, ll2_lo)) {
-        // a compact node was prelinked: all its particles share one root. If that root is
-        // already ours nothing inside can add a link (the parallel form of the reference's
-        // BucketFlag, KDLeafNode.cxx:529-588); if the node lies wholly inside the ball,
-        // one union links all of it.
-        int rr = find_root(a.parent, r.start, a.err);
-        if (rr != myroot) myroot = find_root(a.parent, myroot, a.err);
-        if (rr == myroot) {
-          need = false;
-        } else if (box_far_d2_hi(qx, qy, qz, eps, r) < ll2_lo) {
-          unite(a.parent, self, r.start, a.err);
-          myroot = find_root(a.parent, self, a.err);
-          need = false;
-        }
+    for (int guard = 0; sp > 0 && guard < (1 << 26); guard++) {
+      // above kBatchLimit entries pop one node at a time: a depth-first descent from
+      // there adds at most the tree depth, so the stack never exceeds kFStack
+      int m = sp <= kBatchLimit ? min(32, sp) : 1;
+      int h = 0, root = -1;
+      NodeRec r;
+      bool keep = false, cpt = false;
+      if (lane < m) {
+        h = w.stk[sp - 1 - lane];
+        r = tv.node[tv.nbase + h];
+        keep = boxbox_d2_lo(r, qlo, qhi) < thr;
+        cpt = keep && node_compact(r, ll2_lo);
+        if (cpt) root = find_root(a.parent, r.start, a.err);
       }
-      if (!__any_sync(FULL, need)) continue;
-      if (r.count <= tv.b) {
-        for (int c0 = 0; c0 < r.count; c0 += 32) {
-          int m = min(32, r.count - c0);
-          if (lane < m) {
-            w.sf[lane] = tv.posf[r.start + c0 + lane];
-            w.par[lane] = ld_parent(a.parent, r.start + c0 + lane);
+      __syncwarp();
+      sp -= m;
+      unsigned todo = __ballot_sync(FULL, keep);
+      unsigned expand = 0;
+      while (todo) {
+        int j = __ffs(todo) - 1;
+        todo &= todo - 1;
+        NodeRec rj;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          rj.lo[d] = __shfl_sync(FULL, r.lo[d], j);
+          rj.hi[d] = __shfl_sync(FULL, r.hi[d], j);
+        }
+        rj.start = __shfl_sync(FULL, r.start, j);
+        rj.count = __shfl_sync(FULL, r.count, j);
+        int rootj = __shfl_sync(FULL, root, j);
+        bool need = active && box_d2_lo(qx, qy, qz, eps, rj) < thr;
+        if (need && rootj >= 0) {
+          // a compact node was prelinked: all its particles share one root. If that root
+          // is already ours nothing inside can add a link (the parallel form of the
+          // reference's BucketFlag, KDLeafNode.cxx:529-588); if the node lies wholly
+          // inside the ball, one union links all of it.
+          if (rootj != myroot) myroot = find_root(a.parent, myroot, a.err);
+          if (rootj == myroot) {
+            need = false;
+          } else if (box_far_d2_hi(qx, qy, qz, eps, rj) < ll2_lo) {
+            unite(a.parent, self, rj.start, a.err);
+            myroot = find_root(a.parent, self, a.err);
+            need = false;
+          }
+        }
+        if (!__any_sync(FULL, need)) continue;
+        if (rj.count > tv.b) {
+          expand |= 1u << j;
+          continue;
+        }
+        for (int c0 = 0; c0 < rj.count; c0 += 32) {
+          int mm = min(32, rj.count - c0);
+          if (lane < mm) {
+            w.sf[lane] = tv.posf[rj.start + c0 + lane];
+            w.par[lane] = ld_parent(a.parent, rj.start + c0 + lane);
           }
           __syncwarp();
           if (need) {
-            for (int j = 0; j < m; j++) {
-              int ti = r.start + c0 + j;
+            for (int jj = 0; jj < mm; jj++) {
+              int ti = rj.start + c0 + jj;
               // direct pass: the test is symmetric, so each pair is handled once
               if (pass == 0 && ti <= self) continue;
               // a staged parent equal to our root proves one component for good (links
               // and path halving never separate a component), so no root chase is needed
-              int pj = w.par[j];
+              int pj = w.par[jj];
               if (pj == myroot || ti == myroot) continue;
-              float4 cf = w.sf[j];
+              float4 cf = w.sf[jj];
               if (pair_d2_lo(qx, qy, qz, cf.x, cf.y, cf.z, two_eps) < thr) {
                 // decided in FP32 when the upper bound is already inside; only pairs
                 // within a few FP32 ulps of the linking length take the FP64 test
@@ -191,34 +251,22 @@ __global__ void __launch_bounds__(32 * kWpb, 8) k_link(FofArgs a) {
           }
           __syncwarp();
         }
-      } else {
-        int hl = 2 * h + 1, hr = 2 * h + 2;
-        NodeRec rl = tv.node[tv.nbase + hl], rr = tv.node[tv.nbase + hr];
-        float dl = need ? box_d2_lo(qx, qy, qz, eps, rl) : FLT_MAX;
-        float dr = need ? box_d2_lo(qx, qy, qz, eps, rr) : FLT_MAX;
-        bool anyl = __any_sync(FULL, dl < thr), anyr = __any_sync(FULL, dr < thr);
-        if (sp + 2 > kStack) {
-          if (lane == 0) atomicExch(a.err, kErrCapacity);
-          return;
-        }
-        // nearer child (for the first lane that needs this node) is opened first, so
-        // a particle joins its own neighbourhood's component early and later nodes are
-        // skipped by the root test
-        int leader = __ffs(__ballot_sync(FULL, need)) - 1;
-        bool left_first = __shfl_sync(FULL, dl, leader) <= __shfl_sync(FULL, dr, leader);
-        int first = left_first ? hr : hl, second = left_first ? hl : hr;
-        bool f_need = left_first ? anyr : anyl, s_need = left_first ? anyl : anyr;
-        if (f_need) {
-          if (lane == 0) w.stk[sp] = first;
-          sp++;
-        }
-        if (s_need) {
-          if (lane == 0) w.stk[sp] = second;
-          sp++;
-        }
-        __syncwarp();
       }
+      // children of the expanded nodes: lane i pushes those of its own node
+      int ne = __popc(expand);
+      if (sp + 2 * ne > kFStack) {
+        if (lane == 0) atomicExch(a.err, kErrCapacity);
+        return;
+      }
+      if ((expand >> lane) & 1u) {
+        int slot = sp + 2 * __popc(expand & ((1u << lane) - 1u));
+        w.stk[slot] = 2 * h + 2;
+        w.stk[slot + 1] = 2 * h + 1;
+      }
+      sp += 2 * ne;
+      __syncwarp();
     }
+    if (sp > 0 && lane == 0) atomicExch(a.err, kErrIterCap);
   }
 }
 
