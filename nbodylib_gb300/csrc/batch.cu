@@ -44,6 +44,7 @@ struct nbk_batch {
   int* d_err = nullptr;
   double* d_kernel = nullptr;
   std::vector<double> h_kernel;
+  std::vector<double> h_kernel_img;
   double kernnorm = 0;
   double* d_rho_tree = nullptr;
   double* d_rho_out = nullptr;
@@ -340,9 +341,10 @@ int nbk_batch_create(const double* pos, const double* mass, const int64_t* offse
     B->own_inputs = true;
   }
   kernel_table(B->kerntype, B->kernres, 3, B->h_kernel, B->kernnorm);
-  NBK_TRY(dev_malloc((void**)&B->d_kernel, sizeof(double) * B->kernres, st));
-  NBK_CUDA_TRY(cudaMemcpyAsync(B->d_kernel, B->h_kernel.data(), sizeof(double) * B->kernres,
-                               cudaMemcpyHostToDevice, st));
+  kernel_device_image(B->h_kernel, B->h_kernel_img);
+  NBK_TRY(dev_malloc((void**)&B->d_kernel, sizeof(double) * B->h_kernel_img.size(), st));
+  NBK_CUDA_TRY(cudaMemcpyAsync(B->d_kernel, B->h_kernel_img.data(),
+                               sizeof(double) * B->h_kernel_img.size(), cudaMemcpyHostToDevice, st));
   NBK_TRY(dev_malloc((void**)&B->d_counter, sizeof(int), st));
   NBK_TRY(dev_malloc((void**)&B->d_err, sizeof(int), st));
   NBK_CUDA_TRY(cudaMemsetAsync(B->d_err, 0, sizeof(int), st));

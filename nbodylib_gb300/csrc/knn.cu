@@ -31,8 +31,7 @@ template <int KMAX>
 struct WarpSmem {
   double hd[KMAX][32];
   int hi[KMAX][32];
-  float4 sf[32];
-  P4 sp[32];
+  float4 sf[32];  // FP32 copies of the staged leaf particles (the exact ones stay in L1)
   int stk[kStack];
 };
 
@@ -94,18 +93,15 @@ __device__ void traverse(const TreeView& tv, WarpSmem<KMAX>& w, int lane, bool a
     if (r.count <= tv.b) {
       for (int c0 = 0; c0 < r.count; c0 += 32) {
         int m = min(32, r.count - c0);
-        if (lane < m) {
-          w.sf[lane] = tv.posf[r.start + c0 + lane];
-          w.sp[lane] = tv.pos[r.start + c0 + lane];
-        }
+        if (lane < m) w.sf[lane] = tv.posf[r.start + c0 + lane];
         __syncwarp();
         if (need) {
           for (int j = 0; j < m; j++) {
             float4 cf = w.sf[j];
             if (pair_d2_lo(qx, qy, qz, cf.x, cf.y, cf.z, two_eps) < thr) {
-              P4 c = w.sp[j];
-              double d2 = dist2_exact(xq[0], xq[1], xq[2], c.x, c.y, c.z);
               int ti = r.start + c0 + j;
+              P4 c = tv.pos[ti];
+              double d2 = dist2_exact(xq[0], xq[1], xq[2], c.x, c.y, c.z);
               long long dk = dkey(d2);
               bool ok = dk < topk;  // d2 < top
               if (exclude_self) ok = ok && ti != self && dk != 0;
@@ -183,8 +179,7 @@ __device__ void run_warp(const KnnArgs& a, const TreeView& tv, WarpSmem<KMAX>& w
   if (!valid) return;
 
   const int kr = a.kernres;
-  const double delta = 2.0 / (double)(kr - 1);
-  const double inv_delta = 0.5 * (double)(kr - 1);  // exact
+  const double inv_delta = 0.5 * (double)(kr - 1);  // 1 / table step, exact
   if (EPI == kEpiNN) {
     int Kc = K;
     double d;
@@ -217,20 +212,16 @@ __device__ void run_warp(const KnnArgs& a, const TreeView& tv, WarpSmem<KMAX>& w
     double hh = 0.5 * __dsqrt_rn(top);
     double ih = 1.0 / hh;
     double norm = dmul(dmul(ih, ih), ih);  // 1 / h^3 (the reference takes pow(h, 3))
+    double wnorm = EPI == kEpiDensPart ? norm : 0.5 * norm;
     double acc = 0.0;
     for (int s = 0; s < K; s++) {
       double d2 = w.hd[s][lane];
       int j = w.hi[s][lane];
-      double rij = __dsqrt_rn(d2);
-      double q = dmul(rij, ih);
-      int ci = (int)dmul(dmul(q, 0.5), (double)(kr - 1));
-      double W = wsm_mul(q, ci, kr, delta, inv_delta, T);
+      double q = dmul(__dsqrt_rn(d2), ih);
+      double wij = dmul(wsm_line(q, kr, inv_delta, T), wnorm);
       double mj = tv.pos[j].m;
-      if (EPI == kEpiDensPart) {
-        acc = dadd(acc, dmul(dmul(W, norm), mj));
-      } else {
-        double wij = dmul(dmul(0.5, W), norm);
-        acc = dadd(acc, dmul(wij, mj));
+      acc = dadd(acc, dmul(wij, mj));
+      if (EPI != kEpiDensPart) {
         atomicAdd(&a.rho[j], dmul(wij, me.m));
         if (EPI == kEpiDensSave) a.nn[(size_t)(self - tv.pstart) * K + s] = j;
       }
@@ -266,10 +257,8 @@ __device__ void run_warp(const KnnArgs& a, const TreeView& tv, WarpSmem<KMAX>& w
     double norm = dmul(dmul(ih, ih), ih);
     double acc = 0.0;
     for (int s = 0; s < ns; s++) {
-      double rij = w.hd[s][lane];
-      double q = dmul(rij, ih);
-      int ci = (int)dmul(dmul(q, 0.5), (double)(kr - 1));
-      acc = dadd(acc, dmul(wsm_mul(q, ci, kr, delta, inv_delta, T), norm));
+      double q = dmul(w.hd[s][lane], ih);
+      acc = dadd(acc, dmul(wsm_line(q, kr, inv_delta, T), norm));
     }
     if (EPI == kEpiVelPart) a.vden[qi] = acc;
     else a.vden[self] = acc;

@@ -132,6 +132,7 @@ int run_density_adjoint(const TreeView& tv, int k, const int* d_nn, const double
                         double* d_gpos_tree, double* d_gmass_tree, cudaStream_t st);
 
 void kernel_table(int kerntype, int kernres, int nd, std::vector<double>& T, double& norm);
+void kernel_device_image(const std::vector<double>& T, std::vector<double>& img);
 
 // permutation helpers
 int scatter_to_input_order(const double* tree_vals, const int* perm, double* out, int64_t n,

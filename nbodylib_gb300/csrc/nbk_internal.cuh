@@ -210,17 +210,16 @@ __device__ __forceinline__ double wsm(double r, int i, int size, double delta, c
   }
   return x[i];
 }
-// The same interpolation with the division by delta replaced by a multiplication by
-// inv_delta = (size - 1) / 2, which is exact in FP64; the result differs from wsm() by a
-// few units in the last place (the interpolation is continuous across cells, so the
-// cell index may come from a quotient that differs in its last bit too).
-__device__ __forceinline__ double wsm_mul(double r, int i, int size, double delta,
-                                          double inv_delta, const double* x) {
-  if (i < size - 1) {
-    double xi = x[i], xj = x[i + 1];
-    return dadd(xi, dmul(dmul(dsub(xj, xi), dsub(r, dmul(delta, (double)i))), inv_delta));
-  }
-  return x[i];
+// The same interpolation from the table's device image [T | A | B]: on cell i the line
+// through T[i] and T[i+1] is A[i] + B[i] q, one FMA. The cell index is the reference's
+// (int)(q * 0.5 * (size - 1)); the result differs from wsm() by a few units in the last
+// place (the interpolant is continuous across cells, so a neighbouring cell gives the
+// same value up to rounding).
+__device__ __forceinline__ double wsm_line(double q, int size, double inv_delta,
+                                           const double* img) {
+  int i = (int)dmul(q, inv_delta);
+  if (i < size - 1) return __fma_rn(img[2 * size + i], q, img[size + i]);
+  return img[size - 1];
 }
 
 // ---- device error word: kernels report bounded-wait and capacity failures here
