@@ -9,9 +9,10 @@
 //
 // Phase 1 (levels whose nodes hold more than kLocalMax particles): for all nodes of a
 // level at once, over chunks of kChunk particles:
-//   bbox      segmented min/max of x, y, z (order-preserving uint64 keys, atomics)
-//   split     per node: spread, split dimension, target rank
-//   select    8 radix passes of 8 bits find the key of the median particle exactly
+//   bbox      segmented min/max of x, y, z (order-preserving uint64 keys, atomics); for
+//             the first level only, later levels get it from the partition above them
+//   select    6 radix passes (11, 11, 11, 11, 11, 9 bits) find the key of the median
+//             particle exactly; pass 0 also picks the split dimension from the box
 //   partition stable 3-way (less / equal / greater) scatter into the other buffer
 // Phase 2: one CTA per subtree of <= kLocalMax particles finishes it in shared memory:
 // one sort per dimension, then level by level stable splits of index lists; it writes
@@ -41,10 +42,17 @@ struct GNode {
   int total_eq;
   int first_chunk, nchunks;
   int first_diff;   // highest bit where the keys of the split dimension can differ
-  int pad;
+  unsigned done;    // blocks of this node finished in the current radix pass
+  int child[2];     // the children's slots in the next level's list (-1: per-CTA subtree)
   unsigned long long prefix, mask;
-  unsigned long long kmin[3], kmax[3];
+  unsigned long long kmin[3], kmax[3];  // node box as order keys (filled by the level above)
 };
+
+// Radix digits of the median selection, most significant first: 11+11+11+11+11+9 bits.
+constexpr int kPasses = 6;
+constexpr int kBins = 2048;
+__device__ __constant__ static const int kDigitShift[kPasses] = {53, 42, 31, 20, 9, 0};
+__device__ __constant__ static const int kDigitWidth[kPasses] = {11, 11, 11, 11, 11, 9};
 
 struct Chunk {
   int g;      // gnode index within the level
@@ -72,15 +80,6 @@ __global__ void k_init_soa(const double* __restrict__ pos_in, double* X, double*
   Y[i] = y;
   Z[i] = z;
   ID[i] = (int)i;
-}
-
-__global__ void k_gnode_reset(GNode* g, int ng) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= ng) return;
-  for (int d = 0; d < 3; d++) {
-    g[i].kmin[d] = ~0ull;
-    g[i].kmax[d] = 0ull;
-  }
 }
 
 __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
@@ -148,7 +147,7 @@ __global__ void __launch_bounds__(kThreads) k_bbox(const Chunk* __restrict__ chu
   }
 }
 
-__device__ void write_node(NodeRec* node, NodeX* nodex, int idx, const double lo[3],
+__device__ __forceinline__ void write_node(NodeRec* node, NodeX* nodex, int idx, const double lo[3],
                            const double hi[3], int start, int count, int dim, double split_val) {
   NodeRec r;
   NodeX x;
@@ -169,11 +168,7 @@ __device__ void write_node(NodeRec* node, NodeX* nodex, int idx, const double lo
 
 // DetermineSplitDim (KDTree.cxx:459-504): spread = max - min per dimension in FP64, the
 // first strictly larger spread wins.
-__global__ void k_gnode_split(GNode* g, int ng, NodeRec* node, NodeX* nodex, int p0) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= ng) return;
-  GNode s = g[i];
-  double lo[3], hi[3];
+__device__ __forceinline__ int split_dim_of(const GNode& s, double lo[3], double hi[3]) {
   for (int d = 0; d < 3; d++) {
     lo[d] = okey_inv(s.kmin[d]);
     hi[d] = okey_inv(s.kmax[d]);
@@ -187,107 +182,122 @@ __global__ void k_gnode_split(GNode* g, int ng, NodeRec* node, NodeX* nodex, int
       cur = sp;
     }
   }
-  s.dim = dim;
-  s.k = (s.size - 1) / 2;
-  s.n_less = 0;
-  s.prefix = 0;
-  s.mask = 0;
-  unsigned long long x = s.kmin[dim] ^ s.kmax[dim];
-  s.first_diff = x ? 63 - __clzll((long long)x) : -1;
-  g[i] = s;
-  // the split value is written once the median key is known (k_chunk_scan)
-  write_node(node, nodex, s.node, lo, hi, p0 + s.start, s.size, dim, 0.0);
+  return dim;
 }
 
-__global__ void __launch_bounds__(kThreads) k_hist(const Chunk* __restrict__ chunks,
-                                                   const GNode* __restrict__ g, const double* X,
-                                                   const double* Y, const double* Z,
-                                                   unsigned* hist, int shift) {
+__device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned* tot, unsigned* wsum);
+
+__device__ __forceinline__ unsigned long long sel3(unsigned long long a, unsigned long long b,
+                                                   unsigned long long c, int d) {
+  return d == 0 ? a : (d == 1 ? b : c);
+}
+
+// One radix pass of the median selection for every node of a level. Each block
+// histograms one chunk's digits; the last block of a node to finish (arrival counter,
+// no waiting) reads the node's histogram, narrows the rank to one digit and clears the
+// histogram for the next pass. Pass 0 also fixes the split dimension from the node box
+// (each block derives the same one) and writes the node's records.
+__global__ void __launch_bounds__(kThreads) k_radix(const Chunk* __restrict__ chunks, GNode* g,
+                                                    const double* X, const double* Y,
+                                                    const double* Z, unsigned* hist, int pass,
+                                                    NodeRec* node, NodeX* nodex, int p0) {
+  __shared__ unsigned h[kBins];
+  __shared__ unsigned wsum[32], tot;
+  __shared__ int s_last;
   Chunk c = chunks[blockIdx.x];
-  const GNode& s = g[c.g];
-  if (s.first_diff < shift) return;  // this byte is shared by every key of the node
-  __shared__ unsigned h[256];
-  for (int i = threadIdx.x; i < 256; i += kThreads) h[i] = 0;
-  __syncthreads();
-  int d = s.dim;
-  unsigned long long mask = s.mask, prefix = s.prefix;
-  const double* C = d == 0 ? X : (d == 1 ? Y : Z);
-  double v[kRounds];
-#pragma unroll
-  for (int r = 0; r < kRounds; r++) {
-    int i = r * kThreads + threadIdx.x;
-    if (i < c.len) v[r] = C[c.start + i];
+  const GNode s = g[c.g];
+  int dim, first_diff;
+  double lo[3], hi[3];
+  // (the node record stays in registers: no element of it is indexed at run time)
+  const unsigned long long kmin_d[3] = {s.kmin[0], s.kmin[1], s.kmin[2]};
+  if (pass == 0) {
+    dim = split_dim_of(s, lo, hi);
+    unsigned long long x = sel3(s.kmin[0], s.kmin[1], s.kmin[2], dim) ^
+                           sel3(s.kmax[0], s.kmax[1], s.kmax[2], dim);
+    first_diff = x ? 63 - __clzll((long long)x) : -1;
+  } else {
+    dim = s.dim;
+    first_diff = s.first_diff;
   }
-  // the keys of one node share their leading digits, so most lanes of a warp hit the same
-  // bin: lanes are grouped by digit and one atomic per distinct digit is issued
+  const int shift = kDigitShift[pass], width = kDigitWidth[pass];
+  const unsigned long long dmask = ((1ull << width) - 1ull) << shift;
+  const bool skip = first_diff < shift;  // every key of the node shares this digit
+  if (!skip) {
+    for (int i = threadIdx.x; i < kBins; i += kThreads) h[i] = 0;
+    __syncthreads();
+    const double* C = dim == 0 ? X : (dim == 1 ? Y : Z);
+    double v[kRounds];
 #pragma unroll
-  for (int r = 0; r < kRounds; r++) {
-    int i = r * kThreads + threadIdx.x;
-    int digit = -1;
-    if (i < c.len) {
-      unsigned long long key = okey(v[r]);
-      if ((key & mask) == prefix) digit = (int)((key >> shift) & 255);
+    for (int r = 0; r < kRounds; r++) {
+      int i = r * kThreads + threadIdx.x;
+      if (i < c.len) v[r] = C[c.start + i];
     }
-    unsigned peers = __match_any_sync(0xffffffffu, digit);
-    if (digit >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&h[digit], __popc(peers));
+    // the keys of one node share their leading digits, so most lanes of a warp hit the
+    // same bin: lanes are grouped by digit and one atomic per distinct digit is issued
+#pragma unroll
+    for (int r = 0; r < kRounds; r++) {
+      int i = r * kThreads + threadIdx.x;
+      int digit = -1;
+      if (i < c.len) {
+        unsigned long long key = okey(v[r]);
+        if ((key & s.mask) == s.prefix) digit = (int)((key & dmask) >> shift);
+      }
+      unsigned peers = __match_any_sync(0xffffffffu, digit);
+      if (digit >= 0 && (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&h[digit], __popc(peers));
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kBins; i += kThreads)
+      if (h[i]) atomicAdd(&hist[(size_t)c.g * kBins + i], h[i]);
   }
+  __threadfence();
   __syncthreads();
-  for (int i = threadIdx.x; i < 256; i += kThreads)
-    if (h[i]) atomicAdd(&hist[(size_t)c.g * 256 + i], h[i]);
-}
-
-// One warp per node: find the digit bucket that holds rank k.
-__global__ void k_select(GNode* g, int ng, unsigned* hist, int shift) {
-  int gi = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-  int lane = threadIdx.x & 31;
-  if (gi >= ng) return;
-  GNode s = g[gi];
-  unsigned long long byte_mask = 255ull << shift;
-  if (s.first_diff < shift) {
-    if (lane == 0) {
-      g[gi].prefix = s.prefix | (s.kmin[s.dim] & byte_mask);
-      g[gi].mask = s.mask | byte_mask;
+  if (threadIdx.x == 0) s_last = atomicAdd(&g[c.g].done, 1u) == (unsigned)s.nchunks - 1u;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  if (threadIdx.x == 0) {
+    g[c.g].done = 0u;
+    if (pass == 0) {
+      g[c.g].dim = dim;
+      g[c.g].first_diff = first_diff;
+      // the split value is written once the median key is known (k_chunk_scan)
+      write_node(node, nodex, s.node, lo, hi, p0 + s.start, s.size, dim, 0.0);
+    }
+  }
+  if (skip) {
+    if (threadIdx.x == 0) {
+      g[c.g].prefix = s.prefix | (sel3(kmin_d[0], kmin_d[1], kmin_d[2], dim) & dmask);
+      g[c.g].mask = s.mask | dmask;
     }
     return;
   }
-  unsigned* hh = hist + (size_t)gi * 256;
-  unsigned c[8];
-  unsigned sum = 0;
-  for (int j = 0; j < 8; j++) {
-    c[j] = hh[lane * 8 + j];
-    sum += c[j];
+  // the digit whose bin holds rank k: each thread owns kBins / kThreads consecutive bins
+  constexpr int kPer = kBins / kThreads;
+  unsigned* hh = hist + (size_t)c.g * kBins;
+  unsigned cnt[kPer], sum = 0;
+#pragma unroll
+  for (int e = 0; e < kPer; e++) {
+    cnt[e] = __ldcg(&hh[threadIdx.x * kPer + e]);
+    sum += cnt[e];
   }
-  unsigned incl = sum;
-  for (int o = 1; o < 32; o <<= 1) {
-    unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += v;
-  }
-  unsigned excl = incl - sum;
-  unsigned kk = (unsigned)s.k;
-  bool mine = (excl <= kk) && (kk < incl);
-  unsigned ballot = __ballot_sync(0xffffffffu, mine);
-  int owner = __ffs(ballot) - 1;
-  if (lane == owner) {
-    unsigned before = excl;
-    int digit = lane * 8;
-    for (int j = 0; j < 8; j++) {
-      if (kk < before + c[j]) {
-        digit = lane * 8 + j;
-        break;
+  unsigned before = block_excl_scan(sum, &tot, wsum);
+  unsigned k = (unsigned)s.k;
+  if (before <= k && k < before + sum) {
+    int digit = -1;
+#pragma unroll
+    for (int e = 0; e < kPer; e++) {
+      if (digit < 0) {
+        if (k < before + cnt[e]) digit = threadIdx.x * kPer + e;
+        else before += cnt[e];
       }
-      before += c[j];
     }
-    s.k = (int)(kk - before);
-    s.n_less += (int)before;
-    s.prefix |= ((unsigned long long)digit) << shift;
-    s.mask |= byte_mask;
-    g[gi].k = s.k;
-    g[gi].n_less = s.n_less;
-    g[gi].prefix = s.prefix;
-    g[gi].mask = s.mask;
+    g[c.g].k = (int)(k - before);
+    g[c.g].n_less = s.n_less + (int)before;
+    g[c.g].prefix = s.prefix | ((unsigned long long)digit << shift);
+    g[c.g].mask = s.mask | dmask;
   }
-  __syncwarp();
-  for (int j = 0; j < 8; j++) hh[lane * 8 + j] = 0;
+#pragma unroll
+  for (int e = 0; e < kPer; e++) hh[threadIdx.x * kPer + e] = 0u;
 }
 
 __device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned* tot, unsigned* wsum) {
@@ -396,6 +406,12 @@ __global__ void __launch_bounds__(kThreads) k_chunk_scan(GNode* g, const unsigne
   }
 }
 
+// Stable 3-way partition of every node of a level around its median key into the other
+// buffer. Each warp owns 256 consecutive particles of the chunk, taken 32 at a time, so
+// ballots give every particle its rank inside its class and the writes of one class are
+// contiguous across the warp; one block scan of the warps' (less, equal, valid) counts
+// orders the warps. The children's bounding boxes (order keys of x, y, z) are gathered on
+// the way and merged into the next level's nodes.
 __global__ void __launch_bounds__(kThreads) k_scatter(const Chunk* __restrict__ chunks,
                                                       const GNode* __restrict__ g,
                                                       const double* __restrict__ X,
@@ -407,59 +423,126 @@ __global__ void __launch_bounds__(kThreads) k_scatter(const Chunk* __restrict__ 
                                                       double* __restrict__ Z2,
                                                       int* __restrict__ ID2,
                                                       const unsigned* base_less,
-                                                      const unsigned* base_eq, int* err) {
-  __shared__ unsigned wsum[32];
-  __shared__ unsigned tot;
+                                                      const unsigned* base_eq, int* err,
+                                                      GNode* gnext) {
+  constexpr int kWarps = kThreads / 32, kPerWarp = kChunk / kWarps;
+  __shared__ unsigned wl[kWarps], we[kWarps], wv[kWarps];
+  __shared__ unsigned long long bb[kWarps][12];
   Chunk c = chunks[blockIdx.x];
   const GNode s = g[c.g];
-  unsigned long long piv = s.prefix;
-  unsigned bl = base_less[blockIdx.x], be = base_eq[blockIdx.x];
-  unsigned bg = (unsigned)c.off - bl - be;  // greater keys before this chunk
-  int kleft = (s.size - 1) / 2 + 1;
-  int right0 = s.start + kleft;
-  int excess = s.total_eq - s.need_eq;
+  const unsigned long long piv = s.prefix;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
   const double* C = s.dim == 0 ? X : (s.dim == 1 ? Y : Z);
-  // each thread owns kRounds consecutive particles, so one block scan of the packed
-  // (less, equal) counts orders the whole chunk stably; greater = position - less - equal
-  int i0 = threadIdx.x * kRounds;
-  unsigned cls = 0, nl = 0, ne = 0;
+  const int w0 = warp * kPerWarp;
+  unsigned cls = 0, nl = 0, ne = 0, nv = 0;
 #pragma unroll
-  for (int r = 0; r < kRounds; r++) {
-    int i = i0 + r;
+  for (int r = 0; r < kPerWarp / 32; r++) {
+    int i = w0 + r * 32 + lane;
     unsigned k = 3;
     if (i < c.len) {
       unsigned long long key = okey(C[c.start + i]);
       k = key < piv ? 0u : (key == piv ? 1u : 2u);
-      nl += k == 0;
-      ne += k == 1;
     }
     cls |= k << (2 * r);
+    nl += __popc(__ballot_sync(0xffffffffu, k == 0));
+    ne += __popc(__ballot_sync(0xffffffffu, k == 1));
+    nv += __popc(__ballot_sync(0xffffffffu, k != 3));
   }
-  unsigned pre = block_excl_scan(nl | (ne << 16), &tot, wsum);
-  unsigned rl = bl + (pre & 0xffffu), re = be + (pre >> 16);
-  unsigned rg = bg + (unsigned)min(i0, c.len) - (pre & 0xffffu) - (pre >> 16);
+  if (lane == 0) {
+    wl[warp] = nl;
+    we[warp] = ne;
+    wv[warp] = nv;
+  }
+  __syncthreads();
+  unsigned pl = 0, pe = 0, pv = 0;
+  for (int q = 0; q < warp; q++) {
+    pl += wl[q];
+    pe += we[q];
+    pv += wv[q];
+  }
+  const unsigned bl = base_less[blockIdx.x], be = base_eq[blockIdx.x];
+  const int kleft = (s.size - 1) / 2 + 1;
+  const int right0 = s.start + kleft;
+  const int excess = s.total_eq - s.need_eq;
+  unsigned rl = bl + pl, re = be + pe;
+  unsigned rg = ((unsigned)c.off - bl - be) + (pv - pl - pe);  // greater keys before this warp
+  unsigned long long mnl[3], mxl[3], mnr[3], mxr[3];  // left / right child boxes
 #pragma unroll
-  for (int r = 0; r < kRounds; r++) {
+  for (int d = 0; d < 3; d++) {
+    mnl[d] = mnr[d] = ~0ull;
+    mxl[d] = mxr[d] = 0ull;
+  }
+#pragma unroll
+  for (int r = 0; r < kPerWarp / 32; r++) {
     unsigned k = (cls >> (2 * r)) & 3u;
-    if (k == 3) continue;
-    int p = c.start + i0 + r;
-    int dst;
-    if (k == 0) {
-      dst = s.start + (int)rl++;
-    } else if (k == 1) {
-      int e = (int)re++;
-      dst = e < s.need_eq ? s.start + s.n_less + e : right0 + (e - s.need_eq);
-    } else {
-      dst = right0 + excess + (int)rg++;
+    unsigned bL = __ballot_sync(0xffffffffu, k == 0), bE = __ballot_sync(0xffffffffu, k == 1),
+             bG = __ballot_sync(0xffffffffu, k == 2);
+    if (k != 3) {
+      int p = c.start + w0 + r * 32 + lane;
+      int dst;
+      if (k == 0) {
+        dst = s.start + (int)(rl + __popc(bL & lt));
+      } else if (k == 1) {
+        int e = (int)(re + __popc(bE & lt));
+        dst = e < s.need_eq ? s.start + s.n_less + e : right0 + (e - s.need_eq);
+      } else {
+        dst = right0 + excess + (int)(rg + __popc(bG & lt));
+      }
+      if (dst < s.start || dst >= s.start + s.size) {  // selection inconsistent: report
+        atomicExch(err, 2);
+        dst = p;
+      }
+      double x = X[p], y = Y[p], z = Z[p];
+      X2[dst] = x;
+      Y2[dst] = y;
+      Z2[dst] = z;
+      ID2[dst] = ID[p];
+      unsigned long long kk[3] = {okey(x), okey(y), okey(z)};
+      if (dst < right0) {
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          mnl[d] = min(mnl[d], kk[d]);
+          mxl[d] = max(mxl[d], kk[d]);
+        }
+      } else {
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          mnr[d] = min(mnr[d], kk[d]);
+          mxr[d] = max(mxr[d], kk[d]);
+        }
+      }
     }
-    if (dst < s.start || dst >= s.start + s.size) {  // selection inconsistent: report
-      atomicExch(err, 2);
-      dst = p;
+    rl += __popc(bL);
+    re += __popc(bE);
+    rg += __popc(bG);
+  }
+  if (gnext == nullptr || (s.child[0] < 0 && s.child[1] < 0)) return;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    unsigned long long a = warp_min_u64(mnl[d]), b = warp_max_u64(mxl[d]);
+    unsigned long long a2 = warp_min_u64(mnr[d]), b2 = warp_max_u64(mxr[d]);
+    if (lane == 0) {
+      bb[warp][d] = a;
+      bb[warp][3 + d] = b;
+      bb[warp][6 + d] = a2;
+      bb[warp][9 + d] = b2;
     }
-    X2[dst] = X[p];
-    Y2[dst] = Y[p];
-    Z2[dst] = Z[p];
-    ID2[dst] = ID[p];
+  }
+  __syncthreads();
+  if (threadIdx.x < 12) {
+    int t = threadIdx.x / 6, e = threadIdx.x % 6;
+    int child = t == 0 ? s.child[0] : s.child[1];
+    if (child >= 0) {
+      bool is_min = e < 3;
+      unsigned long long v = is_min ? ~0ull : 0ull;
+      for (int q = 0; q < kWarps; q++) {
+        unsigned long long u = bb[q][threadIdx.x];
+        v = is_min ? min(v, u) : max(v, u);
+      }
+      if (is_min) atomicMin(&gnext[child].kmin[e], v);
+      else atomicMax(&gnext[child].kmax[e - 3], v);
+    }
   }
 }
 
@@ -813,6 +896,12 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
       g.start = (int)cur[i].start;
       g.size = (int)cur[i].size;
       g.node = cur[i].nbase + cur[i].h;
+      g.k = (int)((cur[i].size - 1) / 2);  // rank of the median inside the node
+      g.child[0] = g.child[1] = -1;
+      for (int d = 0; d < 3; d++) {
+        g.kmin[d] = ~0ull;  // boxes are merged in with atomics
+        g.kmax[d] = 0ull;
+      }
       g.first_chunk = (int)ch.size() - L.c0;
       int nc = (int)((cur[i].size + kChunk - 1) / kChunk);
       g.nchunks = nc;
@@ -828,13 +917,20 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
     max_ng = std::max(max_ng, L.ng);
     buf ^= 1;
     nxt.clear();
-    for (auto& c : cur) {
+    for (size_t i = 0; i < cur.size(); i++) {
+      const HN& c = cur[i];
       int64_t l = (c.size - 1) / 2 + 1;
       HN Lh = {c.start, l, 2 * c.h + 1, c.nbase};
       HN Rh = {c.start + l, c.size - l, 2 * c.h + 2, c.nbase};
+      int side = 0;
       for (HN x : {Lh, Rh}) {
-        if (x.size <= kLocalMax) lroots.push_back({(int)x.start, (int)x.size, x.nbase, x.h, buf, 0});
-        else nxt.push_back(x);
+        if (x.size <= kLocalMax) {
+          lroots.push_back({(int)x.start, (int)x.size, x.nbase, x.h, buf, 0});
+        } else {
+          gn[L.g0 + i].child[side] = (int)nxt.size();
+          nxt.push_back(x);
+        }
+        side++;
       }
     }
     cur.swap(nxt);
@@ -855,8 +951,8 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
   unsigned *d_hist = nullptr, *d_cl = nullptr, *d_ce = nullptr, *d_bl = nullptr, *d_be = nullptr;
   if (!levels.empty()) {
     size_t ncall = std::max<size_t>(ch.size(), 1);
-    NBK_TRY(alloc.get((void**)&d_hist, sizeof(unsigned) * 256 * max_ng));
-    NBK_CUDA_TRY(cudaMemsetAsync(d_hist, 0, sizeof(unsigned) * 256 * max_ng, st));
+    NBK_TRY(alloc.get((void**)&d_hist, sizeof(unsigned) * kBins * max_ng));
+    NBK_CUDA_TRY(cudaMemsetAsync(d_hist, 0, sizeof(unsigned) * kBins * max_ng, st));
     NBK_TRY(alloc.get((void**)&d_cl, sizeof(unsigned) * ncall));
     NBK_TRY(alloc.get((void**)&d_ce, sizeof(unsigned) * ncall));
     NBK_TRY(alloc.get((void**)&d_bl, sizeof(unsigned) * ncall));
@@ -865,8 +961,10 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
   k_init_soa<<<(unsigned)((ntot + 255) / 256), 256, 0, st>>>(d_pos_in + 3 * p0, Xa, Ya, Za, IDa, ntot,
                                                             d_err); note_launch();
   NBK_CUDA_TRY(cudaGetLastError());
-  for (const Level& L : levels) {
+  for (size_t li = 0; li < levels.size(); li++) {
+    const Level& L = levels[li];
     GNode* d_g = d_gall + L.g0;
+    GNode* d_gnext = li + 1 < levels.size() ? d_gall + levels[li + 1].g0 : nullptr;
     Chunk* d_c = d_call + L.c0;
     unsigned *cl = d_cl + L.c0, *ce = d_ce + L.c0, *bl = d_bl + L.c0, *be = d_be + L.c0;
     int ng = L.ng, nc = L.nc;
@@ -878,17 +976,18 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
     double* Y2 = L.buf ? Ya : Yb;
     double* Z2 = L.buf ? Za : Zb;
     int* I2 = L.buf ? IDa : IDb;
-    k_gnode_reset<<<(ng + 127) / 128, 128, 0, st>>>(d_g, ng); note_launch();
-    k_bbox<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z); note_launch();
-    k_gnode_split<<<(ng + 127) / 128, 128, 0, st>>>(d_g, ng, out.node, out.nodex, (int)p0); note_launch();
-    for (int pass = 0; pass < 8; pass++) {
-      int shift = 56 - 8 * pass;
-      k_hist<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, d_hist, shift); note_launch();
-      k_select<<<(ng + 3) / 4, 128, 0, st>>>(d_g, ng, d_hist, shift); note_launch();
+    // boxes of the first level's nodes; every later level gets them from the scatter above
+    if (li == 0) {
+      k_bbox<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z); note_launch();
+    }
+    for (int pass = 0; pass < kPasses; pass++) {
+      k_radix<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, d_hist, pass, out.node, out.nodex,
+                                       (int)p0); note_launch();
     }
     k_count<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, cl, ce); note_launch();
     k_chunk_scan<<<ng, kThreads, 0, st>>>(d_g, cl, ce, bl, be, out.nodex); note_launch();
-    k_scatter<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, I, X2, Y2, Z2, I2, bl, be, d_err); note_launch();
+    k_scatter<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, I, X2, Y2, Z2, I2, bl, be, d_err,
+                                       d_gnext); note_launch();
     NBK_CUDA_TRY(cudaGetLastError());
   }
   if (!lroots.empty()) {
