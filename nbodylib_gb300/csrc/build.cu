@@ -44,6 +44,8 @@ struct GNode {
   int first_diff;   // highest bit where the keys of the split dimension can differ
   unsigned done;    // blocks of this node finished in the current radix pass
   int child[2];     // the children's slots in the next level's list (-1: per-CTA subtree)
+  int ncand;        // keys in the current prefix class
+  unsigned nfill;   // keys of the class gathered so far (collect mode)
   unsigned long long prefix, mask;
   unsigned long long kmin[3], kmax[3];  // node box as order keys (filled by the level above)
 };
@@ -51,6 +53,7 @@ struct GNode {
 // Radix digits of the median selection, most significant first: 11+11+11+11+11+9 bits.
 constexpr int kPasses = 6;
 constexpr int kBins = 2048;
+constexpr int kCollect = kThreads;  // a class this small is gathered and ranked by one block
 __device__ __constant__ static const int kDigitShift[kPasses] = {53, 42, 31, 20, 9, 0};
 __device__ __constant__ static const int kDigitWidth[kPasses] = {11, 11, 11, 11, 11, 9};
 
@@ -199,13 +202,18 @@ __device__ __forceinline__ unsigned long long sel3(unsigned long long a, unsigne
 // (each block derives the same one) and writes the node's records.
 __global__ void __launch_bounds__(kThreads) k_radix(const Chunk* __restrict__ chunks, GNode* g,
                                                     const double* X, const double* Y,
-                                                    const double* Z, unsigned* hist, int pass,
-                                                    NodeRec* node, NodeX* nodex, int p0) {
-  __shared__ unsigned h[kBins];
+                                                    const double* Z, unsigned* hist,
+                                                    unsigned long long* cand, int pass,
+                                                    NodeRec* node, NodeX* nodex, int p0,
+                                                    int* err) {
+  static_assert(kCollect <= kBins / 2, "the gathered keys share the bins' shared memory");
+  __shared__ unsigned long long sk[kBins / 2];  // the bins, or the gathered keys
+  unsigned* h = reinterpret_cast<unsigned*>(sk);
   __shared__ unsigned wsum[32], tot;
   __shared__ int s_last;
   Chunk c = chunks[blockIdx.x];
   const GNode s = g[c.g];
+  if (s.mask == ~0ull) return;  // the median key of this node is already known
   int dim, first_diff;
   double lo[3], hi[3];
   // (the node record stays in registers: no element of it is indexed at run time)
@@ -222,7 +230,36 @@ __global__ void __launch_bounds__(kThreads) k_radix(const Chunk* __restrict__ ch
   const int shift = kDigitShift[pass], width = kDigitWidth[pass];
   const unsigned long long dmask = ((1ull << width) - 1ull) << shift;
   const bool skip = first_diff < shift;  // every key of the node shares this digit
-  if (!skip) {
+  const bool collect = !skip && s.ncand <= kCollect;
+  if (collect) {
+    // gather the class's keys into this node's slice of the candidate buffer
+    const double* C = dim == 0 ? X : (dim == 1 ? Y : Z);
+    double v[kRounds];
+#pragma unroll
+    for (int r = 0; r < kRounds; r++) {
+      int i = r * kThreads + threadIdx.x;
+      if (i < c.len) v[r] = C[c.start + i];
+    }
+    const unsigned lane = threadIdx.x & 31;
+#pragma unroll
+    for (int r = 0; r < kRounds; r++) {
+      int i = r * kThreads + threadIdx.x;
+      unsigned long long key = 0;
+      bool in = false;
+      if (i < c.len) {
+        key = okey(v[r]);
+        in = (key & s.mask) == s.prefix;
+      }
+      unsigned b = __ballot_sync(0xffffffffu, in);
+      if (b) {
+        unsigned base = 0;
+        if (lane == (unsigned)(__ffs(b) - 1)) base = atomicAdd(&g[c.g].nfill, (unsigned)__popc(b));
+        base = __shfl_sync(0xffffffffu, base, __ffs(b) - 1);
+        unsigned slot = base + __popc(b & ((1u << lane) - 1u));
+        if (in && slot < (unsigned)kCollect) cand[s.start + slot] = key;
+      }
+    }
+  } else if (!skip) {
     for (int i = threadIdx.x; i < kBins; i += kThreads) h[i] = 0;
     __syncthreads();
     const double* C = dim == 0 ? X : (dim == 1 ? Y : Z);
@@ -271,6 +308,30 @@ __global__ void __launch_bounds__(kThreads) k_radix(const Chunk* __restrict__ ch
     }
     return;
   }
+  if (collect) {
+    // the k-th smallest of the gathered keys is the median key: thread t holds key t and
+    // counts the keys below it and equal to it
+    int n = min(s.ncand, kCollect);
+    if (threadIdx.x == 0 && __ldcg(&g[c.g].nfill) != (unsigned)s.ncand) atomicExch(err, 5);
+    unsigned long long mine = ~0ull;
+    if ((int)threadIdx.x < n) mine = __ldcg(&cand[s.start + threadIdx.x]);
+    sk[threadIdx.x] = mine;
+    __syncthreads();
+    int below = 0, equal = 0;
+    for (int i = 0; i < n; i++) {
+      unsigned long long o = sk[i];
+      below += o < mine;
+      equal += o == mine;
+    }
+    int kr = min(max(s.k, 0), n - 1);
+    if ((int)threadIdx.x < n && below <= kr && kr < below + equal) {
+      // every holder of the k-th key writes the same value
+      g[c.g].prefix = mine;
+      g[c.g].mask = ~0ull;
+    }
+    if (threadIdx.x == 0) g[c.g].nfill = 0u;
+    return;
+  }
   // the digit whose bin holds rank k: each thread owns kBins / kThreads consecutive bins
   constexpr int kPer = kBins / kThreads;
   unsigned* hh = hist + (size_t)c.g * kBins;
@@ -293,6 +354,9 @@ __global__ void __launch_bounds__(kThreads) k_radix(const Chunk* __restrict__ ch
     }
     g[c.g].k = (int)(k - before);
     g[c.g].n_less = s.n_less + (int)before;
+#pragma unroll
+    for (int e = 0; e < kPer; e++)
+      if (threadIdx.x * kPer + e == digit) g[c.g].ncand = (int)cnt[e];
     g[c.g].prefix = s.prefix | ((unsigned long long)digit << shift);
     g[c.g].mask = s.mask | dmask;
   }
@@ -300,7 +364,8 @@ __global__ void __launch_bounds__(kThreads) k_radix(const Chunk* __restrict__ ch
   for (int e = 0; e < kPer; e++) hh[threadIdx.x * kPer + e] = 0u;
 }
 
-__device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned* tot, unsigned* wsum) {
+template <int NT>
+__device__ __forceinline__ unsigned block_excl_scan_t(unsigned v, unsigned* tot, unsigned* wsum) {
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   unsigned incl = v;
   for (int o = 1; o < 32; o <<= 1) {
@@ -310,19 +375,22 @@ __device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned* tot, u
   if (lane == 31) wsum[w] = incl;
   __syncthreads();
   if (w == 0) {
-    unsigned x = lane < kThreads / 32 ? wsum[lane] : 0;
+    unsigned x = lane < NT / 32 ? wsum[lane] : 0;
     unsigned xi = x;
     for (int o = 1; o < 32; o <<= 1) {
       unsigned t = __shfl_up_sync(0xffffffffu, xi, o);
       if (lane >= o) xi += t;
     }
-    if (lane < kThreads / 32) wsum[lane] = xi - x;
-    if (lane == kThreads / 32 - 1) *tot = xi;
+    if (lane < NT / 32) wsum[lane] = xi - x;
+    if (lane == NT / 32 - 1) *tot = xi;
   }
   __syncthreads();
   unsigned r = incl - v + wsum[w];
   __syncthreads();
   return r;
+}
+__device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned* tot, unsigned* wsum) {
+  return block_excl_scan_t<kThreads>(v, tot, wsum);
 }
 
 // Per chunk: how many keys are below / equal to the median key.
@@ -561,8 +629,9 @@ struct LNode {
 };
 
 constexpr int kSortN = 3 * kLocalMax;
+constexpr int kLocalThreads = 512;  // two CTAs of 16 warps per SM (shared memory bound)
 
-__global__ void __launch_bounds__(kThreads) k_local_build(
+__global__ void __launch_bounds__(kLocalThreads) k_local_build(
     const LRoot* __restrict__ roots, const double* Xa, const double* Ya, const double* Za,
     const int* IDa, const double* Xb, const double* Yb, const double* Zb, const int* IDb,
     const double* __restrict__ mass_in, const double* __restrict__ vel_in, int b,
@@ -591,7 +660,7 @@ __global__ void __launch_bounds__(kThreads) k_local_build(
   const double* Y = R.buf ? Yb : Ya;
   const double* Z = R.buf ? Zb : Za;
   const int* I = R.buf ? IDb : IDa;
-  for (int e = threadIdx.x; e < S; e += kThreads) {
+  for (int e = threadIdx.x; e < S; e += kLocalThreads) {
     cx[e] = X[R.start + e];
     cy[e] = Y[R.start + e];
     cz[e] = Z[R.start + e];
@@ -601,7 +670,7 @@ __global__ void __launch_bounds__(kThreads) k_local_build(
   int P = 1;
   while (P < S) P <<= 1;
   const int total = 3 * P;
-  for (int t = threadIdx.x; t < total; t += kThreads) {
+  for (int t = threadIdx.x; t < total; t += kLocalThreads) {
     int d = t / P, r = t - d * P;
     if (r < S) {
       skey[t] = okey(d == 0 ? cx[r] : (d == 1 ? cy[r] : cz[r]));
@@ -615,7 +684,7 @@ __global__ void __launch_bounds__(kThreads) k_local_build(
   // three segments of P sorted at once; every segment ascending by (key, local index)
   for (int kk = 2; kk <= P; kk <<= 1) {
     for (int jj = kk >> 1; jj > 0; jj >>= 1) {
-      for (int t = threadIdx.x; t < total; t += kThreads) {
+      for (int t = threadIdx.x; t < total; t += kLocalThreads) {
         int u = t ^ jj;
         if (u > t) {
           bool up = ((t & (P - 1)) & kk) == 0;
@@ -635,7 +704,7 @@ __global__ void __launch_bounds__(kThreads) k_local_build(
   }
   unsigned short* cur = lst;
   unsigned short* nxt = lst + 4 * K;
-  for (int t = threadIdx.x; t < 3 * S; t += kThreads) {
+  for (int t = threadIdx.x; t < 3 * S; t += kLocalThreads) {
     int d = t / S, i = t - d * S;
     unsigned short q = sidx[d * P + i];
     if (q >= S) {  // a padding slot inside the sorted range: report, keep in bounds
@@ -644,7 +713,7 @@ __global__ void __launch_bounds__(kThreads) k_local_build(
     }
     cur[d * K + i] = q;
   }
-  for (int i = threadIdx.x; i < S; i += kThreads) {
+  for (int i = threadIdx.x; i < S; i += kLocalThreads) {
     cur[3 * K + i] = (unsigned short)i;
     node_at[i] = 0;
   }
@@ -664,7 +733,7 @@ __global__ void __launch_bounds__(kThreads) k_local_build(
     if (threadIdx.x == 0) n_next = 0;
     __syncthreads();
     // A: bounding box, split dimension and median of every node of this level
-    for (int j = threadIdx.x; j < n_cur; j += kThreads) {
+    for (int j = threadIdx.x; j < n_cur; j += kLocalThreads) {
       LNode nd = lv[j];
       int a0 = nd.start, a1 = nd.start + nd.size - 1;
       double lo[3] = {cx[cur[a0]], cy[cur[K + a0]], cz[cur[2 * K + a0]]};
@@ -713,7 +782,7 @@ __global__ void __launch_bounds__(kThreads) k_local_build(
     __syncthreads();
     if (n_next == 0 || n_next > kLevelCap) break;
     // B: which particles go left, read off the list of their node's split dimension
-    for (int t = threadIdx.x; t < 3 * S; t += kThreads) {
+    for (int t = threadIdx.x; t < 3 * S; t += kLocalThreads) {
       int d = t / S, i = t - d * S;
       int j = node_at[i];
       if (j >= 0) {
@@ -723,12 +792,13 @@ __global__ void __launch_bounds__(kThreads) k_local_build(
     }
     __syncthreads();
     // C: exclusive scans of the left flags of the four lists (two packed per word); each
-    // thread covers four consecutive positions
+    // thread covers kPerT consecutive positions
     {
-      unsigned f01[4], f23[4], s01 = 0, s23 = 0;
+      constexpr int kPerT = kLocalMax / kLocalThreads;
+      unsigned f01[kPerT], f23[kPerT], s01 = 0, s23 = 0;
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
-        int i = 4 * threadIdx.x + u;
+      for (int u = 0; u < kPerT; u++) {
+        int i = kPerT * threadIdx.x + u;
         unsigned a = 0, c = 0;
         if (i < S) {
           int j = node_at[i];
@@ -742,11 +812,11 @@ __global__ void __launch_bounds__(kThreads) k_local_build(
         s01 += a;
         s23 += c;
       }
-      unsigned b01 = block_excl_scan(s01, &tot, wsum);
-      unsigned b23 = block_excl_scan(s23, &tot, wsum);
+      unsigned b01 = block_excl_scan_t<kLocalThreads>(s01, &tot, wsum);
+      unsigned b23 = block_excl_scan_t<kLocalThreads>(s23, &tot, wsum);
 #pragma unroll
-      for (int u = 0; u < 4; u++) {
-        int i = 4 * threadIdx.x + u;
+      for (int u = 0; u < kPerT; u++) {
+        int i = kPerT * threadIdx.x + u;
         if (i < S) {
           sc01[i] = b01 + f01[u];
           sc23[i] = b23 + f23[u];
@@ -755,7 +825,7 @@ __global__ void __launch_bounds__(kThreads) k_local_build(
     }
     __syncthreads();
     // D: stable split of every list inside its node; positions of leaves stay put
-    for (int i = threadIdx.x; i < S; i += kThreads) {
+    for (int i = threadIdx.x; i < S; i += kLocalThreads) {
       int j = node_at[i];
       if (j < 0) {
 #pragma unroll
@@ -796,7 +866,7 @@ __global__ void __launch_bounds__(kThreads) k_local_build(
     __syncthreads();
   }
   // final tree-order arrays: the particle-order list holds every leaf contiguously
-  for (int e = threadIdx.x; e < S; e += kThreads) {
+  for (int e = threadIdx.x; e < S; e += kLocalThreads) {
     int q = cur[3 * K + e];
     int t = p0 + R.start + e;  // absolute tree index
     int ii = p0 + id[q];       // absolute input index
@@ -897,6 +967,7 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
       g.size = (int)cur[i].size;
       g.node = cur[i].nbase + cur[i].h;
       g.k = (int)((cur[i].size - 1) / 2);  // rank of the median inside the node
+      g.ncand = (int)cur[i].size;
       g.child[0] = g.child[1] = -1;
       for (int d = 0; d < 3; d++) {
         g.kmin[d] = ~0ull;  // boxes are merged in with atomics
@@ -948,9 +1019,11 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
   GNode* d_gall = (GNode*)d_plan;
   Chunk* d_call = (Chunk*)(d_plan + bg);
   LRoot* d_r = (LRoot*)(d_plan + bg + bc);
+  unsigned long long* d_cand = nullptr;
   unsigned *d_hist = nullptr, *d_cl = nullptr, *d_ce = nullptr, *d_bl = nullptr, *d_be = nullptr;
   if (!levels.empty()) {
     size_t ncall = std::max<size_t>(ch.size(), 1);
+    NBK_TRY(alloc.get((void**)&d_cand, sizeof(unsigned long long) * ntot));
     NBK_TRY(alloc.get((void**)&d_hist, sizeof(unsigned) * kBins * max_ng));
     NBK_CUDA_TRY(cudaMemsetAsync(d_hist, 0, sizeof(unsigned) * kBins * max_ng, st));
     NBK_TRY(alloc.get((void**)&d_cl, sizeof(unsigned) * ncall));
@@ -981,8 +1054,8 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
       k_bbox<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z); note_launch();
     }
     for (int pass = 0; pass < kPasses; pass++) {
-      k_radix<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, d_hist, pass, out.node, out.nodex,
-                                       (int)p0); note_launch();
+      k_radix<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, d_hist, d_cand, pass, out.node,
+                                       out.nodex, (int)p0, d_err); note_launch();
     }
     k_count<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, cl, ce); note_launch();
     k_chunk_scan<<<ng, kThreads, 0, st>>>(d_g, cl, ce, bl, be, out.nodex); note_launch();
@@ -998,7 +1071,7 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
                                         (int)sm));
       attr_set = true;
     }
-    k_local_build<<<(unsigned)lroots.size(), kThreads, sm, st>>>(
+    k_local_build<<<(unsigned)lroots.size(), kLocalThreads, sm, st>>>(
         d_r, Xa, Ya, Za, IDa, Xb, Yb, Zb, IDb, d_mass_in, d_vel_in, b, out.node, out.nodex,
         out.pos, out.posf, out.vel, out.perm, d_err, (int)p0); note_launch();
     NBK_CUDA_TRY(cudaGetLastError());
