@@ -71,12 +71,19 @@ __global__ void __launch_bounds__(32 * kWpb) k_ball(BallArgs a) {
   long long r2k = a.r2 > 0.0 ? dkey(a.r2) : 0;  // nothing is inside r2 <= 0 or NaN
   float eps = tv.eps, two_eps = __fmul_ru(2.f, tv.eps);
   int npass = tv.periodic ? 8 : 1;
+  int near = 0;
+  if (tv.periodic && valid)
+    near = near_walls(make_float4(__double2float_rn(x0[0]), __double2float_rn(x0[1]),
+                                  __double2float_rn(x0[2]), 0.f),
+                      tv.period, eps, thr);
   for (int pass = 0; pass < npass; pass++) {
     double xq[3] = {x0[0], x0[1], x0[2]};
     bool active = valid;
     if (pass > 0) {
+      bool may = (kImageMask[pass] & ~near) == 0;
+      if (!__any_sync(0xffffffffu, may)) continue;
       double sval = reflect(x0, xq, tv.period, kImageMask[pass]);
-      active = active && (a.r2 > dmul(sval, sval));  // KDSplitNode.cxx:1356-1373
+      active = active && may && (a.r2 > dmul(sval, sval));  // KDSplitNode.cxx:1356-1373
     }
     if (!__any_sync(FULL, active)) continue;
     float qx = __double2float_rn(xq[0]), qy = __double2float_rn(xq[1]),

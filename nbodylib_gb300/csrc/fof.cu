@@ -134,12 +134,16 @@ __global__ void __launch_bounds__(32 * kWpb, 4) k_link(FofArgs a) {
   float eps = tv.eps, two_eps = __fmul_ru(2.f, tv.eps);
   int myroot = find_root(a.parent, self, a.err);  // cached; refreshed when it goes stale
   int npass = tv.periodic ? 8 : 1;
+  int near = tv.periodic && valid ? near_walls(tv.posf[self], tv.period, eps, thr) : 0;
   for (int pass = 0; pass < npass; pass++) {
     double xq[3] = {x0[0], x0[1], x0[2]};
     bool active = valid;
     if (pass > 0) {
+      // images no lane can open are skipped before any FP64 work
+      bool may = (kImageMask[pass] & ~near) == 0;
+      if (!__any_sync(FULL, may)) continue;
       double sval = reflect(x0, xq, tv.period, kImageMask[pass]);
-      active = active && (a.ll2 > dmul(sval, sval));  // KDSplitNode.cxx:1611
+      active = active && may && (a.ll2 > dmul(sval, sval));  // KDSplitNode.cxx:1611
     }
     if (!__any_sync(FULL, active)) continue;
     float qx = __double2float_rn(xq[0]), qy = __double2float_rn(xq[1]),

@@ -159,6 +159,7 @@ __device__ void run_warp(const KnnArgs& a, const TreeView& tv, WarpSmem<KMAX>& w
   double top = kMaxValue;
   __syncwarp();
   int npass = a.periodic ? 8 : 1;
+  int near_sq = 7, near_lin = 7;  // walls an image gate could still open across
   for (int pass = 0; pass < npass; pass++) {
     double xq[3];
     bool gate = valid;
@@ -167,11 +168,24 @@ __device__ void run_warp(const KnnArgs& a, const TreeView& tv, WarpSmem<KMAX>& w
       xq[1] = x0[1];
       xq[2] = x0[2];
     } else {
+      if (pass == 1 && valid) {
+        // top only shrinks from here on, so walls ruled out now stay ruled out: the
+        // sqrt(top) > sval gates need a wall closer than sqrt(top), the top > sval gates
+        // (2-D and 3-D images of the reference mode) one closer than top
+        float4 qf = make_float4(__double2float_rn(x0[0]), __double2float_rn(x0[1]),
+                                __double2float_rn(x0[2]), 0.f);
+        float top_hi = thresh_hi_bits(dkey(top));
+        near_sq = near_walls(qf, tv.period, tv.eps, top_hi);
+        near_lin = near_walls_lin(qf, tv.period, tv.eps, top_hi);
+      }
+      int m = kImageMask[pass];
+      bool may = (m & ~((pass <= 3 || a.min_image) ? near_sq : near_lin)) == 0;
+      if (!__any_sync(0xffffffffu, valid && may)) continue;
       double sval = reflect(x0, xq, tv.period, kImageMask[pass]);
       // KDSplitNode.cxx:1129 gates 1-D images with sqrt(top) > sval, :1134-1146 the 2-D
       // and 3-D images with top > sval.
       bool g = (pass <= 3 || a.min_image) ? (__dsqrt_rn(top) > sval) : (top > sval);
-      gate = gate && g;
+      gate = gate && may && g;
     }
     if (!__any_sync(0xffffffffu, gate)) continue;
     traverse<KMAX>(tv, w, lane, gate, xq, self, a.exclude_self && pass == 0, K, top, a.err);

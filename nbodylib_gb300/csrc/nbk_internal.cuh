@@ -82,13 +82,13 @@ __device__ __forceinline__ double dist2_exact(double ax, double ay, double az, d
 // Order-preserving map from FP64 to uint64 (-0.0 is folded onto +0.0 so that equal
 // values compare equal, as the reference's FP comparisons treat them).
 __host__ __device__ __forceinline__ uint64_t okey(double v) {
-  if (v == 0.0) v = 0.0;
 #ifdef __CUDA_ARCH__
   uint64_t u = (uint64_t)__double_as_longlong(v);
 #else
   uint64_t u;
   memcpy(&u, &v, 8);
 #endif
+  if (u == 0x8000000000000000ull) u = 0;  // -0.0 -> +0.0 (an integer test: no FP64 op)
   return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
 }
 __host__ __device__ __forceinline__ double okey_inv(uint64_t k) {
@@ -197,6 +197,34 @@ __device__ __forceinline__ double reflect(const double x0[3], double xp[3], cons
   }
   if (__popc(mask) == 1) return s1;
   return __dsqrt_rn(s);
+}
+// Dimensions in which the query (FP32 copy q, within eps of the exact position) may lie
+// closer than sqrt(r2_hi) to a periodic wall (bit k = dimension k). An image across the
+// walls of `mask` can only pass a gate "r2 > sval^2" when (mask & ~near) == 0, because
+// sval is at least the distance to each crossed wall; r2_hi is an FP32 value at or above r2.
+__device__ __forceinline__ int near_walls(float4 q, const double p[3], float eps, float r2_hi) {
+  const float v[3] = {q.x, q.y, q.z};
+  int near = 0;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    float pk = __double2float_rd(p[k]);
+    float d = fminf(__fsub_rd(v[k], eps), __fsub_rd(__fsub_rd(pk, v[k]), eps));
+    if (d <= 0.f || __fmul_rd(d, d) < r2_hi) near |= 1 << k;
+  }
+  return near;
+}
+// The same for a gate "t > sval" that compares a distance with t itself (t_hi >= t).
+__device__ __forceinline__ int near_walls_lin(float4 q, const double p[3], float eps,
+                                              float t_hi) {
+  const float v[3] = {q.x, q.y, q.z};
+  int near = 0;
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    float pk = __double2float_rd(p[k]);
+    float d = fminf(__fsub_rd(v[k], eps), __fsub_rd(__fsub_rd(pk, v[k]), eps));
+    if (d < t_hi) near |= 1 << k;
+  }
+  return near;
 }
 // The order in which the reference searches the images: x, y, z, xy, xz, yz, xyz
 // (KDSplitNode.cxx:1126-1147).
