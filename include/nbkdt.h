@@ -208,6 +208,64 @@ int nbk_veldensity_particles(nbk_tree* tree, const int32_t* targets, int64_t nta
                              int nsmooth, int nsearch, double* out);
 
 /*
+ * SPH smoothing over the Nsmooth nearest neighbours (KDCalcSmoothQuantities.cxx). In all
+ * of them rho holds the particles' densities in input order (the reference's
+ * densityset = 1: what CalcDensity stored in the particles), or is NULL to run
+ * CalcDensity(Nsmooth) first (densityset != 1). Searches ignore the period, as the
+ * reference's. Every-particle outputs are in input order; the targets are tree indices and
+ * the points (nq, 3) coordinates; their outputs follow the query order. Matrices are 3x3
+ * row-major (element (k, l) at 3k + l).
+ */
+/* KDTree::CalcSmoothVel (KDCalcSmoothQuantities.cxx:480-540). smvel: [n][3]. */
+int nbk_smooth_vel(nbk_tree* tree, int nsmooth, const double* rho, double* smvel);
+/* KDTree::CalcSmoothVelDisp (:542-615), meanvelset = 1. smvel [n][3] in, disp [n][9] out. */
+int nbk_smooth_vel_disp(nbk_tree* tree, int nsmooth, const double* rho, const double* smvel,
+                        double* disp);
+/* KDTree::CalcSmoothVelSkew (:617-690), meanvelset = veldispset = 1. skew: [n][3]. */
+int nbk_smooth_vel_skew(nbk_tree* tree, int nsmooth, const double* rho, const double* smvel,
+                        const double* disp, double* skew);
+/* KDTree::CalcSmoothVelKurtosis (:692-766), the reference's per-neighbour "- 3" included. */
+int nbk_smooth_vel_kurtosis(nbk_tree* tree, int nsmooth, const double* rho, const double* smvel,
+                            const double* disp, double* kurt);
+/* KDTree::CalcVelDensityWithPhysDensity (:393-478). Its physical smoothing length is half
+   the largest squared distance, as the reference computes it (:428); where that sends the
+   kernel-table index past the table (neighbour distances below 1), the reference reads
+   past its table and this call uses the table's last entry. vden: [n]. */
+int nbk_veldensity_physdensity(nbk_tree* tree, int nsmooth, int nsearch, const double* rho,
+                               double* vden);
+/* KDTree::CalcVelDensityWithPhysDensityParticle (:922-990). */
+int nbk_veldensity_physdensity_particles(nbk_tree* tree, const int32_t* targets, int64_t ntargets,
+                                         int nsmooth, int nsearch, const double* rho,
+                                         double* vden);
+/* KDTree::CalcSmoothVelParticle (:992-1036) / CalcSmoothVelPosition (:1209-1253). [nq][3]. */
+int nbk_smooth_vel_particles(nbk_tree* tree, const int32_t* targets, int64_t ntargets,
+                             int nsmooth, const double* rho, double* smvel);
+int nbk_smooth_vel_points(nbk_tree* tree, const double* x, int64_t nq, int nsmooth,
+                          const double* rho, double* smvel);
+/* KDTree::CalcSmoothVelDispParticle (:1038-1090) / CalcSmoothVelDispPosition (:1255-1305).
+   smvel: [nq][3] (the mean velocity of each query), disp: [nq][9]. */
+int nbk_smooth_vel_disp_particles(nbk_tree* tree, const int32_t* targets, int64_t ntargets,
+                                  int nsmooth, const double* rho, const double* smvel,
+                                  double* disp);
+int nbk_smooth_vel_disp_points(nbk_tree* tree, const double* x, int64_t nq, int nsmooth,
+                               const double* rho, const double* smvel, double* disp);
+/* KDTree::CalcSmoothLocalMeanParticle (:1539-1577) / CalcSmoothLocalMeanPosition
+   (:1619-1655). weight: [n] in input order; mean: [nq]. */
+int nbk_smooth_local_mean_particles(nbk_tree* tree, const int32_t* targets, int64_t ntargets,
+                                    int nsmooth, const double* rho, const double* weight,
+                                    double* mean);
+int nbk_smooth_local_mean_points(nbk_tree* tree, const double* x, int64_t nq, int nsmooth,
+                                 const double* rho, const double* weight, double* mean);
+/* KDTree::CalcSmoothLocalDispParticle (:1579-1617) / CalcSmoothLocalDispPosition
+   (:1657-1693). mean: [nq] (the local mean of each query), disp: [nq]. */
+int nbk_smooth_local_disp_particles(nbk_tree* tree, const int32_t* targets, int64_t ntargets,
+                                    int nsmooth, const double* rho, const double* weight,
+                                    const double* mean, double* disp);
+int nbk_smooth_local_disp_points(nbk_tree* tree, const double* x, int64_t nq, int nsmooth,
+                                 const double* rho, const double* weight, const double* mean,
+                                 double* disp);
+
+/*
  * Fixed-radius search around particles. Replaces KDTree::SearchBallPosTagged(Int_t tt,
  * Double_t fdist2) (KDFindNearest.cxx:618-626, 664-672) for a batch of targets (tree
  * indices): every particle with d2 < fdist2, excluding the target itself; periodic trees

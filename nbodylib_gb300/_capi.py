@@ -46,6 +46,21 @@ SIGNATURES = {
     "nbk_veldensity": (c_int, [c_vp, c_int, c_int, c_vp]),
     "nbk_density_veldensity": (c_int, [c_vp, c_int, c_int, c_vp, c_vp]),
     "nbk_veldensity_particles": (c_int, [c_vp, c_vp, c_i64, c_int, c_int, c_vp]),
+    "nbk_smooth_vel": (c_int, [c_vp, c_int, c_vp, c_vp]),
+    "nbk_smooth_vel_disp": (c_int, [c_vp, c_int, c_vp, c_vp, c_vp]),
+    "nbk_smooth_vel_skew": (c_int, [c_vp, c_int, c_vp, c_vp, c_vp, c_vp]),
+    "nbk_smooth_vel_kurtosis": (c_int, [c_vp, c_int, c_vp, c_vp, c_vp, c_vp]),
+    "nbk_veldensity_physdensity": (c_int, [c_vp, c_int, c_int, c_vp, c_vp]),
+    "nbk_veldensity_physdensity_particles": (c_int, [c_vp, c_vp, c_i64, c_int, c_int, c_vp, c_vp]),
+    "nbk_smooth_vel_particles": (c_int, [c_vp, c_vp, c_i64, c_int, c_vp, c_vp]),
+    "nbk_smooth_vel_points": (c_int, [c_vp, c_vp, c_i64, c_int, c_vp, c_vp]),
+    "nbk_smooth_vel_disp_particles": (c_int, [c_vp, c_vp, c_i64, c_int, c_vp, c_vp, c_vp]),
+    "nbk_smooth_vel_disp_points": (c_int, [c_vp, c_vp, c_i64, c_int, c_vp, c_vp, c_vp]),
+    "nbk_smooth_local_mean_particles": (c_int, [c_vp, c_vp, c_i64, c_int, c_vp, c_vp, c_vp]),
+    "nbk_smooth_local_mean_points": (c_int, [c_vp, c_vp, c_i64, c_int, c_vp, c_vp, c_vp]),
+    "nbk_smooth_local_disp_particles": (c_int, [c_vp, c_vp, c_i64, c_int, c_vp, c_vp, c_vp,
+                                                c_vp]),
+    "nbk_smooth_local_disp_points": (c_int, [c_vp, c_vp, c_i64, c_int, c_vp, c_vp, c_vp, c_vp]),
     "nbk_ball_tagged": (c_int, [c_vp, c_vp, c_i64, c_dbl, c_vp, c_vp, c_i64, c_i64p]),
     "nbk_ball_tagged_points": (c_int, [c_vp, c_vp, c_i64, c_dbl, c_vp, c_vp, c_i64, c_i64p]),
     "nbk_ball_mark": (c_int, [c_vp, ctypes.c_int32, c_dbl, ctypes.c_int32, c_vp, c_vp]),

@@ -298,6 +298,10 @@ int check_err(nbk_tree* t, const char* what) {
     set_error(std::string(what) + ": fewer than k neighbours were found for some particle");
     return NBK_ERR_TOO_FEW;
   }
+  if (h == kErrTarget) {
+    set_error(std::string(what) + ": a target index is outside the tree");
+    return NBK_ERR_INVALID;
+  }
   if (h) {
     set_error(std::string(what) + ": device bound exceeded (code " + std::to_string(h) + ")");
     return NBK_ERR_DEVICE;
@@ -823,6 +827,225 @@ static int particles_common(nbk_tree* t, const int32_t* targets, int64_t nt, int
   NBK_TRY(S.finish());
   if (!t->dev()) NBK_TRY(check_err(t, "particle density"));
   return NBK_OK;
+}
+
+// The SPH smoothing family (KDCalcSmoothQuantities.cxx). qmode 0: every particle,
+// 2: targets (tree indices, as the reference's bucket index), 1: coordinates. rho: the
+// particles' densities in input order (the reference's densityset = 1), or null to run
+// CalcDensity(nsmooth) first (densityset != 1).
+static int smooth_common(nbk_tree* t, int which, int qmode, const int32_t* targets,
+                         const double* points, int64_t nq, int nsmooth, int nsearch,
+                         const double* rho, const double* smvel, const double* disp,
+                         const double* weight, const double* mean, double* out) {
+  if (!out || nsmooth < 1 || (qmode == 2 && !targets) || (qmode == 1 && !points) || nq < 0) {
+    set_error("smoothing: invalid argument");
+    return NBK_ERR_INVALID;
+  }
+  if (which == kSmVelPhys) {
+    if (nsearch < 1) {
+      set_error("smoothing: nsearch must be >= 1");
+      return NBK_ERR_INVALID;
+    }
+    if (nsmooth > nsearch) nsmooth = nsearch;  // KDCalcSmoothQuantities.cxx:404-407
+  }
+  bool needs_vel = which != kSmMeanOne && which != kSmDispOne;
+  if (needs_vel && !t->has_vel) {
+    set_error("smoothing: this quantity needs velocities at nbk_create");
+    return NBK_ERR_INVALID;
+  }
+  if (((which == kSmVelDisp || which == kSmVelSkew || which == kSmVelKurt ||
+        which == kSmVelDispOne) && !smvel) ||
+      ((which == kSmVelSkew || which == kSmVelKurt) && !disp) ||
+      ((which == kSmMeanOne || which == kSmDispOne) && !weight) ||
+      (which == kSmDispOne && !mean)) {
+    set_error("smoothing: a required input array is null");
+    return NBK_ERR_INVALID;
+  }
+  int K = which == kSmVelPhys ? nsearch : nsmooth;
+  if (K > t->n - (qmode == 1 ? 0 : 1)) {
+    set_error("smoothing: " + std::to_string(K) + " neighbours requested from a tree of " +
+              std::to_string(t->n) + " particles");
+    return NBK_ERR_TOO_FEW;
+  }
+  if (qmode == 0) nq = t->n;
+  if (qmode == 2 && !t->dev()) {
+    for (int64_t i = 0; i < nq; i++)
+      if (targets[i] < 0 || targets[i] >= t->n) {
+        set_error("smoothing: target index out of range");
+        return NBK_ERR_INVALID;
+      }
+  }
+  if (nq == 0) return NBK_OK;
+  const int width = (which == kSmVelDisp || which == kSmVelDispOne) ? 9
+                    : (which == kSmVelPhys || which == kSmMeanOne || which == kSmDispOne) ? 1 : 3;
+  Stage S(t);
+  const int32_t* dt = nullptr;
+  const double *dx = nullptr, *drho = nullptr, *dsv = nullptr, *ddisp = nullptr, *dw = nullptr,
+               *dmean = nullptr;
+  double* dout = nullptr;
+  if (qmode == 2) NBK_TRY(S.in(targets, nq, &dt));
+  if (qmode == 1) NBK_TRY(S.in(points, 3 * nq, &dx));
+  if (rho) {
+    NBK_TRY(S.in(rho, t->n, &drho));
+  } else {
+    double *scratch, *r;
+    NBK_TRY(S.alloc.get((void**)&scratch, sizeof(double) * t->n));
+    NBK_TRY(S.alloc.get((void**)&r, sizeof(double) * t->n));
+    NBK_TRY(density_into_scratch(t, nsmooth, scratch, r));
+    drho = r;
+  }
+  if (smvel) NBK_TRY(S.in(smvel, 3 * (qmode == 0 ? t->n : nq), &dsv));
+  if (disp) NBK_TRY(S.in(disp, 9 * t->n, &ddisp));
+  if (weight) NBK_TRY(S.in(weight, t->n, &dw));
+  if (mean) NBK_TRY(S.in(mean, nq, &dmean));
+  NBK_TRY(S.out(out, (size_t)width * nq, &dout));
+  if (qmode == 0 && which != kSmVelPhys)
+    NBK_CUDA_TRY(cudaMemsetAsync(dout, 0, sizeof(double) * width * nq, t->st));
+  NBK_TRY(clear_err(t));
+  KnnArgs a = base_args(t);
+  a.tv.periodic = 0;  // the smoothing functions search without images, as CalcDensity
+  a.kheap = K;
+  a.kout = K;
+  a.exclude_self = qmode != 1;
+  a.qmode = qmode;
+  a.qidx = dt;
+  a.qx = dx;
+  a.nq = (int)nq;
+  a.nsmooth = nsmooth;
+  SmoothArgs sa{a, nsmooth, drho, dsv, ddisp, dw, dmean, dout};
+  NBK_TRY(launch_smooth(sa, which, t->st));
+  NBK_TRY(S.finish());
+  if (!t->dev()) NBK_TRY(check_err(t, "smoothing"));
+  return NBK_OK;
+}
+
+int nbk_smooth_vel(nbk_tree* t, int nsmooth, const double* rho, double* smvel) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return smooth_common(t, kSmVel, 0, nullptr, nullptr, 0, nsmooth, 0, rho, nullptr, nullptr,
+                       nullptr, nullptr, smvel);
+  API_END
+}
+
+int nbk_smooth_vel_disp(nbk_tree* t, int nsmooth, const double* rho, const double* smvel,
+                        double* disp) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return smooth_common(t, kSmVelDisp, 0, nullptr, nullptr, 0, nsmooth, 0, rho, smvel, nullptr,
+                       nullptr, nullptr, disp);
+  API_END
+}
+
+int nbk_smooth_vel_skew(nbk_tree* t, int nsmooth, const double* rho, const double* smvel,
+                        const double* disp, double* skew) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return smooth_common(t, kSmVelSkew, 0, nullptr, nullptr, 0, nsmooth, 0, rho, smvel, disp,
+                       nullptr, nullptr, skew);
+  API_END
+}
+
+int nbk_smooth_vel_kurtosis(nbk_tree* t, int nsmooth, const double* rho, const double* smvel,
+                            const double* disp, double* kurt) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return smooth_common(t, kSmVelKurt, 0, nullptr, nullptr, 0, nsmooth, 0, rho, smvel, disp,
+                       nullptr, nullptr, kurt);
+  API_END
+}
+
+int nbk_veldensity_physdensity(nbk_tree* t, int nsmooth, int nsearch, const double* rho,
+                               double* vden) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return smooth_common(t, kSmVelPhys, 0, nullptr, nullptr, 0, nsmooth, nsearch, rho, nullptr,
+                       nullptr, nullptr, nullptr, vden);
+  API_END
+}
+
+int nbk_veldensity_physdensity_particles(nbk_tree* t, const int32_t* targets, int64_t nt,
+                                         int nsmooth, int nsearch, const double* rho,
+                                         double* vden) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return smooth_common(t, kSmVelPhys, 2, targets, nullptr, nt, nsmooth, nsearch, rho, nullptr,
+                       nullptr, nullptr, nullptr, vden);
+  API_END
+}
+
+int nbk_smooth_vel_particles(nbk_tree* t, const int32_t* targets, int64_t nt, int nsmooth,
+                             const double* rho, double* smvel) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return smooth_common(t, kSmVelOne, 2, targets, nullptr, nt, nsmooth, 0, rho, nullptr, nullptr,
+                       nullptr, nullptr, smvel);
+  API_END
+}
+
+int nbk_smooth_vel_points(nbk_tree* t, const double* x, int64_t nq, int nsmooth,
+                          const double* rho, double* smvel) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return smooth_common(t, kSmVelOne, 1, nullptr, x, nq, nsmooth, 0, rho, nullptr, nullptr,
+                       nullptr, nullptr, smvel);
+  API_END
+}
+
+int nbk_smooth_vel_disp_particles(nbk_tree* t, const int32_t* targets, int64_t nt, int nsmooth,
+                                  const double* rho, const double* smvel, double* disp) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return smooth_common(t, kSmVelDispOne, 2, targets, nullptr, nt, nsmooth, 0, rho, smvel,
+                       nullptr, nullptr, nullptr, disp);
+  API_END
+}
+
+int nbk_smooth_vel_disp_points(nbk_tree* t, const double* x, int64_t nq, int nsmooth,
+                               const double* rho, const double* smvel, double* disp) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return smooth_common(t, kSmVelDispOne, 1, nullptr, x, nq, nsmooth, 0, rho, smvel, nullptr,
+                       nullptr, nullptr, disp);
+  API_END
+}
+
+int nbk_smooth_local_mean_particles(nbk_tree* t, const int32_t* targets, int64_t nt,
+                                    int nsmooth, const double* rho, const double* weight,
+                                    double* mean) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return smooth_common(t, kSmMeanOne, 2, targets, nullptr, nt, nsmooth, 0, rho, nullptr,
+                       nullptr, weight, nullptr, mean);
+  API_END
+}
+
+int nbk_smooth_local_mean_points(nbk_tree* t, const double* x, int64_t nq, int nsmooth,
+                                 const double* rho, const double* weight, double* mean) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return smooth_common(t, kSmMeanOne, 1, nullptr, x, nq, nsmooth, 0, rho, nullptr, nullptr,
+                       weight, nullptr, mean);
+  API_END
+}
+
+int nbk_smooth_local_disp_particles(nbk_tree* t, const int32_t* targets, int64_t nt,
+                                    int nsmooth, const double* rho, const double* weight,
+                                    const double* mean, double* disp) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return smooth_common(t, kSmDispOne, 2, targets, nullptr, nt, nsmooth, 0, rho, nullptr,
+                       nullptr, weight, mean, disp);
+  API_END
+}
+
+int nbk_smooth_local_disp_points(nbk_tree* t, const double* x, int64_t nq, int nsmooth,
+                                 const double* rho, const double* weight, const double* mean,
+                                 double* disp) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return smooth_common(t, kSmDispOne, 1, nullptr, x, nq, nsmooth, 0, rho, nullptr, nullptr,
+                       weight, mean, disp);
+  API_END
 }
 
 int nbk_density_particles(nbk_tree* t, const int32_t* targets, int64_t nt, int k, double* out) {

@@ -92,6 +92,30 @@ struct KnnArgs {
 };
 int launch_knn(const KnnArgs& a, int epi, cudaStream_t st);
 
+// ---- SPH smoothing over the nearest neighbours (smooth.cu)
+enum Smooth : int {
+  kSmVel = 0,          // CalcSmoothVel (symmetric, every particle)
+  kSmVelDisp = 1,      // CalcSmoothVelDisp
+  kSmVelSkew = 2,      // CalcSmoothVelSkew
+  kSmVelKurt = 3,      // CalcSmoothVelKurtosis
+  kSmVelPhys = 4,      // CalcVelDensityWithPhysDensity[Particle]
+  kSmVelOne = 5,       // CalcSmoothVel{Particle,Position}
+  kSmVelDispOne = 6,   // CalcSmoothVelDisp{Particle,Position}
+  kSmMeanOne = 7,      // CalcSmoothLocalMean{Particle,Position}
+  kSmDispOne = 8,      // CalcSmoothLocalDisp{Particle,Position}
+};
+struct SmoothArgs {
+  KnnArgs k;              // the search: queries, heap size (Nsmooth, or Nsearch for kSmVelPhys)
+  int nsmooth;
+  const double* rho;      // densities, input order
+  const double* smvel;    // input order [n][3] (every-particle forms) or query order [nq][3]
+  const double* disp;     // input order [n][9]
+  const double* weight;   // input order [n]
+  const double* mean;     // query order [nq]
+  double* out;            // input order (every-particle forms, zeroed) or query order
+};
+int launch_smooth(const SmoothArgs& s, int which, cudaStream_t st);
+
 // ---- batched path: many trees, one persistent launch
 struct WorkItem {
   int tree, q0, count, pad;  // queries [q0, q0+count) of tree `tree`

@@ -256,6 +256,7 @@ enum DeviceErr : int {
   kErrIterCap = 1,   // a union-find or queue loop exceeded its iteration cap
   kErrCapacity = 2,  // an output or stack capacity was exceeded
   kErrTooFew = 3,    // fewer than k neighbours found
+  kErrTarget = 4,    // a target index outside the tree (the query is skipped)
 };
 
 }  // namespace nbk

@@ -180,6 +180,124 @@ class KDTree:
                                                        nsmooth, nsearch, _ptr(out)))
         return out
 
+    # ---- SPH smoothing (KDCalcSmoothQuantities.cxx:393-766, 922-1091, 1209-1306,
+    # 1539-1700). rho: densities in input order (the reference's densityset = 1, i.e. what
+    # CalcDensity returned), or None to compute CalcDensity(Nsmooth) first. Targets are
+    # tree indices, points an (nq, 3) array; matrices come back as (.., 3, 3).
+    def _vec(self, a, shape):
+        if a is None:
+            return None
+        if self.device:
+            return a.to(self._torch.float64).contiguous()
+        return np.ascontiguousarray(a, np.float64).reshape(shape)
+
+    def _pts(self, x):
+        if self.device:
+            return x.to(self._torch.float64).contiguous()
+        return np.ascontiguousarray(x, np.float64).reshape(-1, 3)
+
+    def CalcSmoothVel(self, Nsmooth=64, rho=None):
+        out = self._empty((self.n, 3), np.float64)
+        _capi.check(self._lib.nbk_smooth_vel(self._h, Nsmooth, _ptr(self._vec(rho, (-1,))),
+                                             _ptr(out)))
+        return out
+
+    def CalcSmoothVelDisp(self, smvel, Nsmooth=64, rho=None):
+        out = self._empty((self.n, 3, 3), np.float64)
+        _capi.check(self._lib.nbk_smooth_vel_disp(self._h, Nsmooth, _ptr(self._vec(rho, (-1,))),
+                                                  _ptr(self._vec(smvel, (-1, 3))), _ptr(out)))
+        return out
+
+    def _moment(self, fn, smvel, smveldisp, Nsmooth, rho):
+        out = self._empty((self.n, 3), np.float64)
+        _capi.check(fn(self._h, Nsmooth, _ptr(self._vec(rho, (-1,))),
+                       _ptr(self._vec(smvel, (-1, 3))), _ptr(self._vec(smveldisp, (-1, 9))),
+                       _ptr(out)))
+        return out
+
+    def CalcSmoothVelSkew(self, smvel, smveldisp, Nsmooth=64, rho=None):
+        return self._moment(self._lib.nbk_smooth_vel_skew, smvel, smveldisp, Nsmooth, rho)
+
+    def CalcSmoothVelKurtosis(self, smvel, smveldisp, Nsmooth=64, rho=None):
+        return self._moment(self._lib.nbk_smooth_vel_kurtosis, smvel, smveldisp, Nsmooth, rho)
+
+    def CalcVelDensityWithPhysDensity(self, Nsmooth=64, Nsearch=64, rho=None):
+        out = self._empty(self.n, np.float64)
+        _capi.check(self._lib.nbk_veldensity_physdensity(self._h, Nsmooth, Nsearch,
+                                                         _ptr(self._vec(rho, (-1,))), _ptr(out)))
+        return out
+
+    def CalcVelDensityWithPhysDensityParticle(self, targets, Nsmooth=64, Nsearch=64, rho=None):
+        targets = self._targets(targets)
+        out = self._empty(len(targets), np.float64)
+        _capi.check(self._lib.nbk_veldensity_physdensity_particles(
+            self._h, _ptr(targets), len(targets), Nsmooth, Nsearch, _ptr(self._vec(rho, (-1,))),
+            _ptr(out)))
+        return out
+
+    def CalcSmoothVelParticle(self, targets, Nsmooth=64, rho=None):
+        targets = self._targets(targets)
+        out = self._empty((len(targets), 3), np.float64)
+        _capi.check(self._lib.nbk_smooth_vel_particles(self._h, _ptr(targets), len(targets),
+                                                       Nsmooth, _ptr(self._vec(rho, (-1,))),
+                                                       _ptr(out)))
+        return out
+
+    def CalcSmoothVelPosition(self, x, Nsmooth=64, rho=None):
+        x = self._pts(x)
+        out = self._empty((x.shape[0], 3), np.float64)
+        _capi.check(self._lib.nbk_smooth_vel_points(self._h, _ptr(x), x.shape[0], Nsmooth,
+                                                    _ptr(self._vec(rho, (-1,))), _ptr(out)))
+        return out
+
+    def CalcSmoothVelDispParticle(self, targets, smvel, Nsmooth=64, rho=None):
+        targets = self._targets(targets)
+        out = self._empty((len(targets), 3, 3), np.float64)
+        _capi.check(self._lib.nbk_smooth_vel_disp_particles(
+            self._h, _ptr(targets), len(targets), Nsmooth, _ptr(self._vec(rho, (-1,))),
+            _ptr(self._vec(smvel, (-1, 3))), _ptr(out)))
+        return out
+
+    def CalcSmoothVelDispPosition(self, x, smvel, Nsmooth=64, rho=None):
+        x = self._pts(x)
+        out = self._empty((x.shape[0], 3, 3), np.float64)
+        _capi.check(self._lib.nbk_smooth_vel_disp_points(
+            self._h, _ptr(x), x.shape[0], Nsmooth, _ptr(self._vec(rho, (-1,))),
+            _ptr(self._vec(smvel, (-1, 3))), _ptr(out)))
+        return out
+
+    def CalcSmoothLocalMeanParticle(self, targets, weight, Nsmooth=64, rho=None):
+        targets = self._targets(targets)
+        out = self._empty(len(targets), np.float64)
+        _capi.check(self._lib.nbk_smooth_local_mean_particles(
+            self._h, _ptr(targets), len(targets), Nsmooth, _ptr(self._vec(rho, (-1,))),
+            _ptr(self._vec(weight, (-1,))), _ptr(out)))
+        return out
+
+    def CalcSmoothLocalMeanPosition(self, x, weight, Nsmooth=64, rho=None):
+        x = self._pts(x)
+        out = self._empty(x.shape[0], np.float64)
+        _capi.check(self._lib.nbk_smooth_local_mean_points(
+            self._h, _ptr(x), x.shape[0], Nsmooth, _ptr(self._vec(rho, (-1,))),
+            _ptr(self._vec(weight, (-1,))), _ptr(out)))
+        return out
+
+    def CalcSmoothLocalDispParticle(self, targets, weight, mean, Nsmooth=64, rho=None):
+        targets = self._targets(targets)
+        out = self._empty(len(targets), np.float64)
+        _capi.check(self._lib.nbk_smooth_local_disp_particles(
+            self._h, _ptr(targets), len(targets), Nsmooth, _ptr(self._vec(rho, (-1,))),
+            _ptr(self._vec(weight, (-1,))), _ptr(self._vec(mean, (-1,))), _ptr(out)))
+        return out
+
+    def CalcSmoothLocalDispPosition(self, x, weight, mean, Nsmooth=64, rho=None):
+        x = self._pts(x)
+        out = self._empty(x.shape[0], np.float64)
+        _capi.check(self._lib.nbk_smooth_local_disp_points(
+            self._h, _ptr(x), x.shape[0], Nsmooth, _ptr(self._vec(rho, (-1,))),
+            _ptr(self._vec(weight, (-1,))), _ptr(self._vec(mean, (-1,))), _ptr(out)))
+        return out
+
     def _targets(self, targets):
         if self.device:
             return targets.to(self._torch.int32).contiguous()

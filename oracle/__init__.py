@@ -72,6 +72,13 @@ def _lib(backend: str) -> ctypes.CDLL:
         "ball_tagged_pos": (ctypes.c_int, [vp, _c_dbl_p, ctypes.c_double, _c_int_p]),
         "ball_mark": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, _c_int_p,
                                      _c_dbl_p]),
+        "smooth_vel_moments": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, _c_dbl_p, _c_dbl_p,
+                                              _c_dbl_p, _c_dbl_p]),
+        "veldensity_phys": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, _c_dbl_p, _c_dbl_p]),
+        "veldensity_phys_particle": (ctypes.c_double, [vp, ctypes.c_int, ctypes.c_int,
+                                                       ctypes.c_int, _c_dbl_p]),
+        "smooth_one": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, _c_dbl_p, ctypes.c_int,
+                                      _c_dbl_p, _c_dbl_p, _c_dbl_p, ctypes.c_double, _c_dbl_p]),
     }
     if backend == "port":
         sig["knn_pos"] = (ctypes.c_int, [vp, _c_dbl_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -194,6 +201,45 @@ class OracleTree:
             return (rho, nn) if return_nn else rho
         self._f("density")(self._h, k, _dp(rho))
         return rho
+
+    # ---- SPH smoothing (KDCalcSmoothQuantities.cxx). rho=None: CalcDensity(nsmooth) first.
+    def _arr(self, a, shape):
+        return None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(shape)
+
+    def smooth_vel_moments(self, which, nsmooth, rho=None, smvel=None, disp=None):
+        """which 0: CalcSmoothVel (n,3); 1: CalcSmoothVelDisp (n,3,3); 2: Skew; 3: Kurtosis."""
+        out = np.empty((self.n, 9 if which == 1 else 3), np.float64)
+        st = self._f("smooth_vel_moments")(self._h, which, nsmooth,
+                                           _dp(self._arr(rho, (self.n,))),
+                                           _dp(self._arr(smvel, (self.n, 3))),
+                                           _dp(self._arr(disp, (self.n, 9))), _dp(out))
+        if st:
+            raise RuntimeError("smoothing: fewer than nsmooth neighbours")
+        return out.reshape(self.n, 3, 3) if which == 1 else out
+
+    def veldensity_phys(self, nsmooth, nsearch, rho=None):
+        out = np.empty(self.n, np.float64)
+        st = self._f("veldensity_phys")(self._h, nsmooth, nsearch,
+                                        _dp(self._arr(rho, (self.n,))), _dp(out))
+        if st:
+            raise RuntimeError("CalcVelDensityWithPhysDensity: fewer than nsearch neighbours")
+        return out
+
+    def veldensity_phys_particle(self, pid, nsmooth, nsearch, rho=None):
+        return self._f("veldensity_phys_particle")(self._h, int(pid), nsmooth, nsearch,
+                                                   _dp(self._arr(rho, (self.n,))))
+
+    def smooth_one(self, which, nsmooth, pid=-1, x=None, rho=None, smvel=None, weight=None,
+                   mean=0.0):
+        """which 0: CalcSmoothVel{Particle,Position} (3); 1: ..VelDisp.. (3,3);
+        4: CalcSmoothLocalMean{..}; 5: CalcSmoothLocalDisp{..}."""
+        out = np.empty(9 if which == 1 else (3 if which == 0 else 1), np.float64)
+        st = self._f("smooth_one")(self._h, which, int(pid), _dp(self._arr(x, (3,))), nsmooth,
+                                   _dp(self._arr(rho, (self.n,))), _dp(self._arr(smvel, (3,))),
+                                   _dp(self._arr(weight, (self.n,))), float(mean), _dp(out))
+        if st:
+            raise RuntimeError("smoothing: fewer than nsmooth neighbours")
+        return out.reshape(3, 3) if which == 1 else (out if which == 0 else float(out[0]))
 
     def veldensity(self, nsmooth, nsearch):
         out = np.empty(self.n, np.float64)

@@ -1223,6 +1223,241 @@ int pt_density_frozen(PTree* t, int k, const int* nn, const double* pos0, const 
     return 0;
 }
 
+/* ------------------------------------------------------------ SPH smoothing */
+/* The densities the smoothing functions divide by: the caller's (densityset = 1) or
+   CalcDensity(nsmooth) (KDCalcSmoothQuantities.cxx:408, 493, 561, ...). */
+static int sm_density(PTree* t, int nsmooth, const double* rho) {
+    if (rho) {
+        for (int i = 0; i < t->n; i++) t->p[i].rho = rho[t->p[i].id];
+        return 0;
+    }
+    double* tmp = (double*)malloc(sizeof(double) * (size_t)(t->n > 0 ? t->n : 1));
+    int s = pt_density(t, nsmooth, tmp, NULL);
+    free(tmp);
+    return s;
+}
+
+/* Wsm for an index that may pass the end of the table: the reference reads past its table
+   there (only CalcVelDensityWithPhysDensity, whose h comes from a squared distance); this
+   restatement returns the last entry instead. */
+static inline double wsm_end(double r, int i, int size, double delta, const double* x) {
+    if (i >= size) return x[size - 1];
+    return wsm(r, i, size, delta, x);
+}
+
+/* CalcSmoothVel / CalcSmoothVelDisp / CalcSmoothVelSkew / CalcSmoothVelKurtosis
+   (KDCalcSmoothQuantities.cxx:480-766): symmetric SPH sums over the Nsmooth nearest. */
+int pt_smooth_vel_moments(PTree* t, int which, int nsmooth, const double* rho,
+                          const double* smvel, const double* disp, double* out) {
+    int n = t->n, nd = t->nd;
+    int width = which == 1 ? 9 : 3;
+    int status = sm_density(t, nsmooth, rho);
+    if (status) return status;
+    for (size_t i = 0; i < (size_t)n * width; i++) out[i] = 0;
+    PQ pq;
+    pq_init(&pq, nsmooth);
+    double delta = 2.0 / (double)(t->kernres - 1);
+    for (int i = 0; i < n && !status; i++) {
+        pq.n = 0;
+        for (int j = 0; j < nsmooth; j++) pq_push(&pq, -1, MAXVALUE);
+        double off[6] = {0, 0, 0, 0, 0, 0};
+        double xt[6] = {0, 0, 0, 0, 0, 0};
+        tvec(t, &t->p[i], xt);
+        knn_target(t, 0, 0.0, &pq, off, i, xt);
+        double hi = 0.5 * sqrt(pq_top(&pq));
+        double norm = 1.0 / pow(hi, (double)(nd * 1.));
+        for (int j = 0; j < nsmooth; j++) {
+            if (pq_topq(&pq) == -1) {
+                status = 6;
+                break;
+            }
+            double rij = sqrt(pq_top(&pq));
+            double wij = 0.5 * wsm(rij / hi, (int)(rij / hi * 0.5 * (t->kernres - 1)), t->kernres,
+                                   delta, t->kernel) *
+                         norm;
+            int index = pq_topq(&pq);
+            int id1 = t->p[i].id, id2 = t->p[index].id;
+            const PPart* a = &t->p[index]; /* the neighbour, summed into id1 */
+            const PPart* b = &t->p[i];     /* the target, summed into id2 */
+            for (int side = 0; side < 2; side++) {
+                const PPart* src = side == 0 ? a : b;
+                int dst = side == 0 ? id1 : id2;
+                double temp = wij / src->rho * src->mass;
+                if (which == 0) {
+                    for (int k = 0; k < 3; k++) out[(size_t)dst * 3 + k] += temp * src->vel[k];
+                } else if (which == 1) {
+                    for (int k = 0; k < 3; k++)
+                        for (int l = 0; l < 3; l++) {
+                            double dv1 = src->vel[k] - smvel[(size_t)dst * 3 + k];
+                            double dv2 = src->vel[l] - smvel[(size_t)dst * 3 + l];
+                            out[(size_t)dst * 9 + k * 3 + l] += temp * dv1 * dv2;
+                        }
+                } else if (which == 2) {
+                    for (int k = 0; k < 3; k++) {
+                        double dv1 = src->vel[k] - smvel[(size_t)dst * 3 + k];
+                        out[(size_t)dst * 3 + k] +=
+                            temp * dv1 * dv1 * dv1 / pow(disp[(size_t)dst * 9 + k * 4], (double)1.5);
+                    }
+                } else {
+                    for (int k = 0; k < 3; k++) {
+                        double dv1 = src->vel[k] - smvel[(size_t)dst * 3 + k];
+                        double dkk = disp[(size_t)dst * 9 + k * 4];
+                        out[(size_t)dst * 3 + k] += temp * dv1 * dv1 * dv1 * dv1 / (dkk * dkk) - 3.;
+                    }
+                }
+            }
+            pq_pop(&pq);
+        }
+    }
+    pq_free(&pq);
+    return status;
+}
+
+/* CalcVelDensityWithPhysDensity[Particle] (KDCalcSmoothQuantities.cxx:393-478, 922-990):
+   the physical h is half the largest squared distance, as the reference computes it. */
+static double veldensity_phys_one(PTree* t, int i, int nsmooth, int nsearch, PQ* pq, PQ* pq2,
+                                  int* nnids, double* vdist, int* status) {
+    int nd = t->nd;
+    double delta = 2.0 / (double)(t->kernres - 1);
+    pq->n = 0;
+    for (int j = 0; j < nsearch; j++) pq_push(pq, -1, MAXVALUE);
+    double off[6] = {0, 0, 0, 0, 0, 0};
+    double xt[6] = {0, 0, 0, 0, 0, 0};
+    tvec(t, &t->p[i], xt);
+    knn_target(t, 0, 0.0, pq, off, i, xt);
+    double hi = 0.5 * pq_top(pq);
+    double norm = 1.0 / pow(hi, (double)(nd * 1.));
+    for (int j = 0; j < nsearch; j++) {
+        if (pq_topq(pq) == -1) {
+            *status = 6;
+            return 0;
+        }
+        nnids[j] = pq_topq(pq);
+        vdist[j] = sqrt(dist2_n(t->p[i].vel, t->p[nnids[j]].vel, 3));
+        pq_pop(pq);
+    }
+    pq2->n = 0;
+    for (int j = 0; j < nsmooth; j++) pq_push(pq2, -1, MAXVALUE);
+    for (int j = 0; j < nsearch; j++)
+        if (vdist[j] < pq_top(pq2)) {
+            pq_pop(pq2);
+            pq_push(pq2, nnids[j], vdist[j]);
+        }
+    double vhi = 0.5 * pq_top(pq2);
+    double vnorm = 1.0 / pow(vhi, (double)(nd * 1.));
+    double vden = 0;
+    for (int j = 0; j < nsmooth; j++) {
+        double vij = pq_top(pq2);
+        int id2 = pq_topq(pq2);
+        double rij = sqrt(dist2_n(t->p[i].pos, t->p[id2].pos, 3));
+        double vwij = wsm_end(vij / vhi, (int)(vij / vhi * 0.5 * (t->kernres - 1)), t->kernres,
+                              delta, t->kernel) *
+                      vnorm;
+        double wij = wsm_end(rij / hi, (int)(rij / hi * 0.5 * (t->kernres - 1)), t->kernres, delta,
+                             t->kernel) *
+                     norm;
+        vden += vwij * (wij / t->p[i].rho * t->p[i].mass);
+        pq_pop(pq2);
+    }
+    return vden;
+}
+
+int pt_veldensity_phys(PTree* t, int nsmooth, int nsearch, const double* rho, double* out) {
+    if (nsmooth > nsearch) nsmooth = nsearch;
+    int status = sm_density(t, nsmooth, rho);
+    if (status) return status;
+    PQ pq, pq2;
+    pq_init(&pq, nsearch);
+    pq_init(&pq2, nsmooth);
+    int* nnids = (int*)malloc(sizeof(int) * (size_t)nsearch);
+    double* vdist = (double*)malloc(sizeof(double) * (size_t)nsearch);
+    for (int i = 0; i < t->n; i++) out[i] = 0;
+    for (int i = 0; i < t->n && !status; i++)
+        out[t->p[i].id] += veldensity_phys_one(t, i, nsmooth, nsearch, &pq, &pq2, nnids, vdist, &status);
+    free(nnids);
+    free(vdist);
+    pq_free(&pq);
+    pq_free(&pq2);
+    return status;
+}
+
+double pt_veldensity_phys_particle(PTree* t, int id, int nsmooth, int nsearch, const double* rho) {
+    if (nsmooth > nsearch) nsmooth = nsearch;
+    int status = sm_density(t, nsmooth, rho);
+    if (status) return NAN;
+    PQ pq, pq2;
+    pq_init(&pq, nsearch);
+    pq_init(&pq2, nsmooth);
+    int* nnids = (int*)malloc(sizeof(int) * (size_t)nsearch);
+    double* vdist = (double*)malloc(sizeof(double) * (size_t)nsearch);
+    double v = veldensity_phys_one(t, t->tree_of_id[id], nsmooth, nsearch, &pq, &pq2, nnids, vdist,
+                                   &status);
+    free(nnids);
+    free(vdist);
+    pq_free(&pq);
+    pq_free(&pq2);
+    return status ? NAN : v;
+}
+
+/* CalcSmoothVel{Particle,Position}, CalcSmoothVelDisp{Particle,Position},
+   CalcSmoothLocalMean{Particle,Position}, CalcSmoothLocalDisp{Particle,Position}
+   (KDCalcSmoothQuantities.cxx:992-1091, 1209-1306, 1539-1700): one-sided sums. */
+int pt_smooth_one(PTree* t, int which, int id, const double* x, int nsmooth, const double* rho,
+                  const double* smvel, const double* weight, double mean, double* out) {
+    int nd = t->nd;
+    int status = sm_density(t, nsmooth, rho);
+    if (status) return status;
+    int width = which == 1 ? 9 : (which == 0 ? 3 : 1);
+    for (int k = 0; k < width; k++) out[k] = 0;
+    PQ pq;
+    pq_init(&pq, nsmooth);
+    for (int j = 0; j < nsmooth; j++) pq_push(&pq, -1, MAXVALUE);
+    double off[6] = {0, 0, 0, 0, 0, 0};
+    if (x) {
+        double xq[6] = {0, 0, 0, 0, 0, 0};
+        for (int j = 0; j < nd; j++) xq[j] = x[j];
+        knn_coord(t, 0, 0.0, &pq, off, xq);
+    } else {
+        int i = t->tree_of_id[id];
+        double xt[6] = {0, 0, 0, 0, 0, 0};
+        tvec(t, &t->p[i], xt);
+        knn_target(t, 0, 0.0, &pq, off, i, xt);
+    }
+    double delta = 2.0 / (double)(t->kernres - 1);
+    double hi = 0.5 * sqrt(pq_top(&pq));
+    double norm = 1.0 / pow(hi, (double)(nd * 1.));
+    for (int j = 0; j < nsmooth; j++) {
+        if (pq_topq(&pq) == -1) {
+            status = 6;
+            break;
+        }
+        double rij = sqrt(pq_top(&pq));
+        double wij = wsm(rij / hi, (int)(rij / hi * 0.5 * (t->kernres - 1)), t->kernres, delta,
+                         t->kernel) *
+                     norm;
+        const PPart* a = &t->p[pq_topq(&pq)];
+        double temp = wij / a->rho * a->mass;
+        if (which == 0) {
+            for (int k = 0; k < 3; k++) out[k] += temp * a->vel[k];
+        } else if (which == 1) {
+            for (int k = 0; k < 3; k++)
+                for (int l = 0; l < 3; l++) {
+                    double dv1 = a->vel[k] - smvel[k];
+                    double dv2 = a->vel[l] - smvel[l];
+                    out[k * 3 + l] += temp * dv1 * dv2;
+                }
+        } else if (which == 4) {
+            out[0] += temp * weight[a->id];
+        } else {
+            double dl = (weight[a->id] - mean);
+            out[0] += temp * dl * dl;
+        }
+        pq_pop(&pq);
+    }
+    pq_free(&pq);
+    return status;
+}
+
 int pt_density_adjoint(PTree* t, int k, const int* nn, const double* pos, const double* mass,
                        const double* wts, double* rho, double* gpos, double* gmass) {
     int n = t->n;

@@ -48,6 +48,23 @@ int pt_ball_tagged(PTree* t, int id, double fdist2, int* out_ids);
 int pt_ball_tagged_pos(PTree* t, const double* x, double fdist2, int* out_ids);
 int pt_ball_mark(PTree* t, int id, double fdist2, int imark, int* mark, double* dist2);
 
+/* SPH smoothing over the Nsmooth nearest neighbours (KDCalcSmoothQuantities.cxx).
+   rho: the particles' densities in ID order (the reference's densityset = 1), or NULL to
+   run CalcDensity(nsmooth) first (densityset != 1). Outputs in ID order.
+   which: 0 CalcSmoothVel (out n*3), 1 CalcSmoothVelDisp (n*9, row-major (k,l); needs
+   smvel n*3), 2 CalcSmoothVelSkew (n*3; needs smvel, disp), 3 CalcSmoothVelKurtosis. */
+int pt_smooth_vel_moments(PTree* t, int which, int nsmooth, const double* rho,
+                          const double* smvel, const double* disp, double* out);
+/* CalcVelDensityWithPhysDensity (all particles, ID order) and its Particle form. */
+int pt_veldensity_phys(PTree* t, int nsmooth, int nsearch, const double* rho, double* out);
+double pt_veldensity_phys_particle(PTree* t, int id, int nsmooth, int nsearch, const double* rho);
+/* Single-particle (x == NULL, target id) and position (x) forms:
+   which 0 CalcSmoothVel{Particle,Position} (out 3), 1 CalcSmoothVelDisp{..} (out 9, needs
+   smvel 3), 4 CalcSmoothLocalMean{..} (out 1, needs weight in ID order),
+   5 CalcSmoothLocalDisp{..} (out 1, needs weight and mean). */
+int pt_smooth_one(PTree* t, int which, int id, const double* x, int nsmooth, const double* rho,
+                  const double* smvel, const double* weight, double mean, double* out);
+
 /* Density adjoint (no reference counterpart): L = sum_i w_i log rho_i with rho from
    CalcDensity(k), neighbour lists nn_ids (ID rows of k, any order) and kernel-table cells
    frozen. Inputs/outputs in ID order; pos is (n,3) row-major. */

@@ -221,4 +221,90 @@ int ref_ball_mark(void* h, int id, double fdist2, int imark, int* mark, double* 
     return 0;
 }
 
+// ---- SPH smoothing (KDCalcSmoothQuantities.cxx:393-766, 922-1091, 1209-1306, 1539-1700).
+// rho != NULL: set the particles' densities and pass densityset = 1; otherwise the
+// reference computes CalcDensity(Nsmooth) itself (densityset = 0).
+static int set_rho(RefTree* r, const double* rho) {
+    if (!rho) return 0;
+    for (int t = 0; t < r->n; t++) r->parts[t].SetDensity(rho[r->parts[t].GetID()]);
+    return 1;
+}
+
+int ref_smooth_vel_moments(void* h, int which, int nsmooth, const double* rho,
+                           const double* smvel, const double* disp, double* out) {
+    RefTree* r = (RefTree*)h;
+    int ds = set_rho(r, rho);
+    int n = r->n;
+    Coordinate* sv = nullptr;
+    Matrix* dm = nullptr;
+    if (which >= 1) {
+        sv = new Coordinate[n];
+        for (int i = 0; i < n; i++) sv[i] = Coordinate(smvel[3 * (size_t)i], smvel[3 * (size_t)i + 1], smvel[3 * (size_t)i + 2]);
+    }
+    if (which >= 2) {
+        dm = new Matrix[n];
+        for (int i = 0; i < n; i++) dm[i] = Matrix(&disp[9 * (size_t)i]);
+    }
+    if (which == 1) {
+        Matrix* m = r->tree->CalcSmoothVelDisp(sv, nsmooth, ds, 1);
+        for (int i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++)
+                for (int l = 0; l < 3; l++) out[9 * (size_t)i + 3 * k + l] = m[i](k, l);
+        delete[] m;
+    } else {
+        Coordinate* c = which == 0 ? r->tree->CalcSmoothVel(nsmooth, ds)
+                      : which == 2 ? r->tree->CalcSmoothVelSkew(sv, dm, nsmooth, ds, 1, 1)
+                                   : r->tree->CalcSmoothVelKurtosis(sv, dm, nsmooth, ds, 1, 1);
+        for (int i = 0; i < n; i++)
+            for (int k = 0; k < 3; k++) out[3 * (size_t)i + k] = c[i][k];
+        delete[] c;
+    }
+    delete[] sv;
+    delete[] dm;
+    return 0;
+}
+
+int ref_veldensity_phys(void* h, int nsmooth, int nsearch, const double* rho, double* out) {
+    RefTree* r = (RefTree*)h;
+    int ds = set_rho(r, rho);
+    Double_t* v = r->tree->CalcVelDensityWithPhysDensity(nsmooth, nsearch, ds);
+    for (int i = 0; i < r->n; i++) out[i] = v[i];
+    delete[] v;
+    return 0;
+}
+
+double ref_veldensity_phys_particle(void* h, int id, int nsmooth, int nsearch, const double* rho) {
+    RefTree* r = (RefTree*)h;
+    int ds = set_rho(r, rho);
+    return r->tree->CalcVelDensityWithPhysDensityParticle(r->tree_of_id[id], nsmooth, nsearch, ds);
+}
+
+int ref_smooth_one(void* h, int which, int id, const double* x, int nsmooth, const double* rho,
+                   const double* smvel, const double* weight, double mean, double* out) {
+    RefTree* r = (RefTree*)h;
+    int ds = set_rho(r, rho);
+    Double_t xx[3] = {0, 0, 0};
+    if (x) for (int k = 0; k < 3; k++) xx[k] = x[k];
+    int t = x ? -1 : r->tree_of_id[id];
+    Double_t* w = const_cast<Double_t*>(weight);
+    if (which == 0) {
+        Coordinate c = x ? r->tree->CalcSmoothVelPosition(xx, nsmooth, ds)
+                         : r->tree->CalcSmoothVelParticle(t, nsmooth, ds);
+        for (int k = 0; k < 3; k++) out[k] = c[k];
+    } else if (which == 1) {
+        Coordinate sv(smvel[0], smvel[1], smvel[2]);
+        Matrix m = x ? r->tree->CalcSmoothVelDispPosition(xx, sv, nsmooth, ds)
+                     : r->tree->CalcSmoothVelDispParticle(t, sv, nsmooth, ds);
+        for (int k = 0; k < 3; k++)
+            for (int l = 0; l < 3; l++) out[3 * k + l] = m(k, l);
+    } else if (which == 4) {
+        out[0] = x ? r->tree->CalcSmoothLocalMeanPosition(xx, w, nsmooth, ds)
+                   : r->tree->CalcSmoothLocalMeanParticle(t, w, nsmooth, ds);
+    } else {
+        out[0] = x ? r->tree->CalcSmoothLocalDispPosition(xx, w, mean, nsmooth, ds)
+                   : r->tree->CalcSmoothLocalDispParticle(t, w, mean, nsmooth, ds);
+    }
+    return 0;
+}
+
 }  // extern "C"

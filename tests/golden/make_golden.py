@@ -127,10 +127,57 @@ def tiny_periodic():
                 d2_findnearest=d2, nn_findnearestpos=nnp, d2_findnearestpos=d2p)
 
 
-def main():
+def smoothing():
+    """The SPH smoothing family (KDCalcSmoothQuantities.cxx) on clustered particles with
+    velocities, densities computed by the reference (densityset != 1), k = 24; the
+    Particle forms for a few particles (stored by ID) and the Position forms at a few
+    points; CalcVelDensityWithPhysDensity on widely spaced particles (every neighbour
+    distance above 1, where the reference stays inside its kernel table)."""
+    pos, mass, vel = syn.clustered_box(2500, 50.0, seed=21, velocities=True)
+    t = ref_tree(pos, vel, mass, 16, 0, None)
+    k = 24
+    rho = t.density(k)
+    sv = t.smooth_vel_moments(0, k, None)
+    dp = t.smooth_vel_moments(1, k, None, sv).reshape(-1, 9)
+    skew = t.smooth_vel_moments(2, k, None, sv, dp)
+    kurt = t.smooth_vel_moments(3, k, None, sv, dp)
+    rng = np.random.default_rng(22)
+    weight = rng.random(len(mass))
+    ids = np.array([0, 5, 911, 1700, len(mass) - 1], np.int32)
+    pts = pos[ids] + rng.normal(scale=0.05, size=(len(ids), 3))
+    one = {}
+    for tag, kw in (("id", [dict(pid=int(i)) for i in ids]), ("pt", [dict(x=x) for x in pts])):
+        one[f"vel_{tag}"] = np.array([t.smooth_one(0, k, rho=None, **a) for a in kw])
+        one[f"veldisp_{tag}"] = np.array([t.smooth_one(1, k, rho=None, smvel=sv[j], **a)
+                                          for j, a in zip(ids, kw)])
+        one[f"mean_{tag}"] = np.array([t.smooth_one(4, k, rho=None, weight=weight, **a)
+                                       for a in kw])
+        one[f"disp_{tag}"] = np.array([t.smooth_one(5, k, rho=None, weight=weight, mean=0.4, **a)
+                                       for a in kw])
+    prng = np.random.default_rng(23)
+    ppos = prng.random((3000, 3)) * 200.0
+    pvel = prng.normal(size=(3000, 3))
+    pmass = prng.random(3000) + 0.5
+    tp = ref_tree(ppos, pvel, pmass, 16, 0, None)
+    vphys = tp.veldensity_phys(16, 32, None)
+    vphys_id = np.array([tp.veldensity_phys_particle(int(i), 16, 32, None) for i in ids])
+    return dict(pos=pos, vel=vel, mass=mass, b=16, k=k, rho=rho, smvel=sv, veldisp=dp,
+                velskew=skew, velkurt=kurt, weight=weight, ids=ids, points=pts, mean_ref=0.4,
+                phys_pos=ppos, phys_vel=pvel, phys_mass=pmass, phys_nsmooth=16,
+                phys_nsearch=32, veldensity_phys=vphys, veldensity_phys_id=vphys_id, **one)
+
+
+FIXTURES = [("uniform_periodic", uniform_periodic), ("clustered", clustered),
+            ("nonperiodic", nonperiodic), ("tiny_periodic", tiny_periodic),
+            ("smoothing", smoothing)]
+
+
+def main(names=None):
+    """Writes the named fixtures (all of them without names)."""
     oracle.build(ref=True)
-    for name, fn in [("uniform_periodic", uniform_periodic), ("clustered", clustered),
-                     ("nonperiodic", nonperiodic), ("tiny_periodic", tiny_periodic)]:
+    for name, fn in FIXTURES:
+        if names and name not in names:
+            continue
         d = fn()
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **{k: np.asarray(v) for k, v in d.items()})
@@ -138,4 +185,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -150,3 +150,76 @@ def test_adjoint_restatement_finite_differences(port_built):
     g = gp[coords[:, 0], coords[:, 1]]
     rel = np.abs(fd - g) / np.maximum(np.abs(g), 1e-3 * np.abs(gp).max())
     assert rel.max() <= 1e-6, rel.max()
+
+
+def _smoothing_inputs():
+    pos, mass, vel = syn.clustered_box(2500, 50.0, seed=21, velocities=True)
+    return pos, mass, vel
+
+
+@pytest.mark.parametrize("given_rho", [False, True])
+def test_port_smoothing_matches_reference(ref_built, given_rho):
+    """CalcSmoothVel / VelDisp / VelSkew / VelKurtosis and the Particle / Position forms of
+    CalcSmoothVel, CalcSmoothVelDisp, CalcSmoothLocalMean, CalcSmoothLocalDisp: the
+    restatement is bit-identical to the compiled reference, with the densities computed
+    inside (densityset != 1) or given (densityset = 1)."""
+    pos, mass, vel = _smoothing_inputs()
+    R = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, None, backend="ref")
+    P = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, None, backend="port")
+    k = 24
+    rho = R.density(k) * 1.25 if given_rho else None
+    sv = R.smooth_vel_moments(0, k, rho)
+    dp = R.smooth_vel_moments(1, k, rho, sv).reshape(-1, 9)
+    for which in range(4):
+        a = R.smooth_vel_moments(which, k, rho, sv, dp)
+        b = P.smooth_vel_moments(which, k, rho, sv, dp)
+        assert np.array_equal(a, b), f"moment {which}"
+    w = np.random.default_rng(2).random(len(mass))
+    for pid in (0, 911, len(mass) - 1):
+        for which in (0, 1, 4, 5):
+            args = dict(rho=rho, smvel=sv[pid], weight=w, mean=0.4)
+            assert np.array_equal(R.smooth_one(which, k, pid=pid, **args),
+                                  P.smooth_one(which, k, pid=pid, **args)), (which, pid)
+            x = pos[pid] + 0.013
+            assert np.array_equal(R.smooth_one(which, k, x=x, **args),
+                                  P.smooth_one(which, k, x=x, **args)), (which, pid, "position")
+
+
+def test_port_veldensity_phys_matches_reference(ref_built):
+    """CalcVelDensityWithPhysDensity[Particle], whose physical h is half the largest squared
+    distance (KDCalcSmoothQuantities.cxx:428): compared where every neighbour distance is
+    above 1, so the reference's table index stays inside its table."""
+    rng = np.random.default_rng(11)
+    n = 3000
+    pos = rng.random((n, 3)) * 200.0
+    vel = rng.normal(size=(n, 3))
+    mass = rng.random(n) + 0.5
+    R = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, None, backend="ref")
+    P = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, None, backend="port")
+    for rho in (None, R.density(16) * 1.3):
+        a = R.veldensity_phys(16, 32, rho)
+        assert np.array_equal(a, P.veldensity_phys(16, 32, rho))
+        for pid in (0, 17, n - 1):
+            assert R.veldensity_phys_particle(pid, 16, 32, rho) == \
+                P.veldensity_phys_particle(pid, 16, 32, rho)
+
+
+def test_port_matches_golden_smoothing(port_built):
+    """The restatement reproduces the reference's smoothing outputs stored in the fixture."""
+    g = golden("smoothing")
+    P = oracle.OracleTree(g["pos"], g["vel"], g["mass"], int(g["b"]), 0, 0, 1000, None,
+                          backend="port")
+    k = int(g["k"])
+    assert np.array_equal(P.smooth_vel_moments(0, k), g["smvel"])
+    assert np.array_equal(P.smooth_vel_moments(1, k, None, g["smvel"]).reshape(-1, 9), g["veldisp"])
+    assert np.array_equal(P.smooth_vel_moments(2, k, None, g["smvel"], g["veldisp"]), g["velskew"])
+    assert np.array_equal(P.smooth_vel_moments(3, k, None, g["smvel"], g["veldisp"]), g["velkurt"])
+    for n, i in enumerate(g["ids"]):
+        assert np.array_equal(P.smooth_one(0, k, pid=int(i)), g["vel_id"][n])
+        assert np.array_equal(P.smooth_one(4, k, pid=int(i), weight=g["weight"]), g["mean_id"][n])
+        assert np.array_equal(P.smooth_one(5, k, x=g["points"][n], weight=g["weight"],
+                                           mean=float(g["mean_ref"])), g["disp_pt"][n])
+    Q = oracle.OracleTree(g["phys_pos"], g["phys_vel"], g["phys_mass"], 16, 0, 0, 1000, None,
+                          backend="port")
+    assert np.array_equal(Q.veldensity_phys(int(g["phys_nsmooth"]), int(g["phys_nsearch"])),
+                          g["veldensity_phys"])
