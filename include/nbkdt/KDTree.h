@@ -22,6 +22,7 @@
 #define NBKDT_KDTREE_H
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -211,6 +212,144 @@ class KDTree {
     return out;
   }
 
+  // ---- SPH smoothing (KDTree.h:413-464, KDCalcSmoothQuantities.cxx). densityset == 1 uses
+  // the densities stored in the particles (by CalcDensity), as the reference does; any
+  // other value computes CalcDensity(Nsmooth) first. Arrays returned with new[] are indexed
+  // by ID, as the reference's. With meanvelset / veldispset != 1 the mean velocities /
+  // dispersions are computed here; unlike the reference, the caller's arrays are not deleted.
+  Double_t* CalcVelDensityWithPhysDensity(Int_t Nsmooth = 64, Int_t Nsearch = 64,
+                                          int densityset = 1) {
+    std::vector<double> rho = densities(densityset);
+    Double_t* out = new Double_t[numparts_];
+    nbkdt::check(nbk_veldensity_physdensity(tree_, Nsmooth, Nsearch, rho_or_null(rho), out));
+    return out;
+  }
+  Coordinate* CalcSmoothVel(Int_t Nsmooth = 64, int densityset = 1) {
+    std::vector<double> rho = densities(densityset), v(3 * (size_t)numparts_);
+    nbkdt::check(nbk_smooth_vel(tree_, Nsmooth, rho_or_null(rho), v.data()));
+    Coordinate* out = new Coordinate[numparts_];
+    for (Int_t i = 0; i < numparts_; i++) out[i] = Coordinate(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+    return out;
+  }
+  Matrix* CalcSmoothVelDisp(Coordinate* smvel, Int_t Nsmooth = 64, int densityset = 1,
+                            int meanvelset = 1) {
+    std::vector<double> rho = densities(densityset);
+    std::vector<double> sv = mean_velocities(smvel, meanvelset, Nsmooth, rho), d(9 * (size_t)numparts_);
+    nbkdt::check(nbk_smooth_vel_disp(tree_, Nsmooth, rho_or_null(rho), sv.data(), d.data()));
+    return to_matrices(d, numparts_);
+  }
+  Coordinate* CalcSmoothVelSkew(Coordinate* smvel, Matrix* smveldisp, Int_t Nsmooth = 64,
+                                int densityset = 1, int meanvelset = 1, int veldispset = 1) {
+    return moment(smvel, smveldisp, Nsmooth, densityset, meanvelset, veldispset, false);
+  }
+  Coordinate* CalcSmoothVelKurtosis(Coordinate* smvel, Matrix* smveldisp, Int_t Nsmooth = 64,
+                                    int densityset = 1, int meanvelset = 1, int veldispset = 1) {
+    return moment(smvel, smveldisp, Nsmooth, densityset, meanvelset, veldispset, true);
+  }
+  Double_t CalcVelDensityWithPhysDensityParticle(Int_t target, Int_t Nsmooth = 64,
+                                                 Int_t Nsearch = 64, int densityset = 1) {
+    std::vector<double> rho = densities(densityset);
+    int32_t t = (int32_t)target;
+    double out = 0;
+    nbkdt::check(nbk_veldensity_physdensity_particles(tree_, &t, 1, Nsmooth, Nsearch,
+                                                      rho_or_null(rho), &out));
+    return out;
+  }
+  Coordinate CalcSmoothVelParticle(Int_t target, Int_t Nsmooth = 64, int densityset = 1) {
+    std::vector<double> rho = densities(densityset);
+    int32_t t = (int32_t)target;
+    double v[3];
+    nbkdt::check(nbk_smooth_vel_particles(tree_, &t, 1, Nsmooth, rho_or_null(rho), v));
+    return Coordinate(v[0], v[1], v[2]);
+  }
+  Coordinate CalcSmoothVelPosition(Double_t* x, Int_t Nsmooth = 64, int densityset = 1) {
+    std::vector<double> rho = densities(densityset);
+    double v[3];
+    nbkdt::check(nbk_smooth_vel_points(tree_, x, 1, Nsmooth, rho_or_null(rho), v));
+    return Coordinate(v[0], v[1], v[2]);
+  }
+  Coordinate CalcSmoothVelPosition(Coordinate x, Int_t Nsmooth = 64, int densityset = 1) {
+    return CalcSmoothVelPosition(x.GetCoord(), Nsmooth, densityset);
+  }
+  Matrix CalcSmoothVelDispParticle(Int_t target, Coordinate smvel, Int_t Nsmooth = 64,
+                                   int densityset = 1) {
+    std::vector<double> rho = densities(densityset);
+    int32_t t = (int32_t)target;
+    double sv[3] = {smvel[0], smvel[1], smvel[2]}, d[9];
+    nbkdt::check(nbk_smooth_vel_disp_particles(tree_, &t, 1, Nsmooth, rho_or_null(rho), sv, d));
+    return Matrix(d);
+  }
+  Matrix CalcSmoothVelDispPosition(Double_t* x, Coordinate smvel, Int_t Nsmooth = 64,
+                                   int densityset = 1) {
+    std::vector<double> rho = densities(densityset);
+    double sv[3] = {smvel[0], smvel[1], smvel[2]}, d[9];
+    nbkdt::check(nbk_smooth_vel_disp_points(tree_, x, 1, Nsmooth, rho_or_null(rho), sv, d));
+    return Matrix(d);
+  }
+  Matrix CalcSmoothVelDispPosition(Coordinate x, Coordinate smvel, Int_t Nsmooth = 64,
+                                   int densityset = 1) {
+    return CalcSmoothVelDispPosition(x.GetCoord(), smvel, Nsmooth, densityset);
+  }
+  Double_t CalcSmoothLocalMeanParticle(Int_t target, Double_t* weight, Int_t Nsmooth = 64,
+                                       int densityset = 1) {
+    std::vector<double> rho = densities(densityset);
+    int32_t t = (int32_t)target;
+    double out = 0;
+    nbkdt::check(nbk_smooth_local_mean_particles(tree_, &t, 1, Nsmooth, rho_or_null(rho),
+                                                 weight, &out));
+    return out;
+  }
+  Double_t CalcSmoothLocalMeanPosition(Double_t* x, Double_t* weight, Int_t Nsmooth = 64,
+                                       int densityset = 1) {
+    std::vector<double> rho = densities(densityset);
+    double out = 0;
+    nbkdt::check(nbk_smooth_local_mean_points(tree_, x, 1, Nsmooth, rho_or_null(rho), weight, &out));
+    return out;
+  }
+  Double_t CalcSmoothLocalMeanPosition(Coordinate x, Double_t* weight, Int_t Nsmooth = 64,
+                                       int densityset = 1) {
+    return CalcSmoothLocalMeanPosition(x.GetCoord(), weight, Nsmooth, densityset);
+  }
+  Double_t CalcSmoothLocalDispParticle(Int_t target, Double_t* weight, Double_t mean,
+                                       Int_t Nsmooth = 64, int densityset = 1) {
+    std::vector<double> rho = densities(densityset);
+    int32_t t = (int32_t)target;
+    double out = 0;
+    nbkdt::check(nbk_smooth_local_disp_particles(tree_, &t, 1, Nsmooth, rho_or_null(rho), weight,
+                                                 &mean, &out));
+    return out;
+  }
+  Double_t CalcSmoothLocalDispPosition(Double_t* x, Double_t* weight, Double_t mean,
+                                       Int_t Nsmooth = 64, int densityset = 1) {
+    std::vector<double> rho = densities(densityset);
+    double out = 0;
+    nbkdt::check(nbk_smooth_local_disp_points(tree_, x, 1, Nsmooth, rho_or_null(rho), weight,
+                                              &mean, &out));
+    return out;
+  }
+  Double_t CalcSmoothLocalDispPosition(Coordinate x, Double_t* weight, Double_t localmean,
+                                       Int_t Nsmooth = 64, int densityset = 1) {
+    return CalcSmoothLocalDispPosition(x.GetCoord(), weight, localmean, Nsmooth, densityset);
+  }
+  // CalcSmoothLocalValue(Nsmooth, dist, weight) (KDCalcSmoothQuantities.cxx:1721-1736): the
+  // kernel sum over caller-given distances (dist[0] the largest), on the host.
+  Double_t CalcSmoothLocalValue(Int_t Nsmooth, Double_t* dist, Double_t* weight) {
+    std::vector<double> table(kernres_);
+    double norm = 0;
+    nbkdt::check(nbk_get_kernel(tree_, table.data(), &norm));
+    double hi = 0.5 * dist[0];
+    double hnorm = 1.0 / std::pow(hi, 3.0);
+    double delta = 2.0 / (double)(kernres_ - 1), value = 0;
+    for (Int_t j = 0; j < Nsmooth; j++) {
+      double q = dist[j] / hi;
+      int i = (int)(q * 0.5 * (kernres_ - 1));
+      double w = i < kernres_ - 1 ? table[i] + (table[i + 1] - table[i]) * (q - delta * i) / delta
+                                  : table[kernres_ - 1];
+      value += w * hnorm * weight[j];
+    }
+    return value;
+  }
+
   // ---- FOF (KDTree.h:480-503). Returns new Int_t[numparts] indexed by ID.
   Int_t* FOF(Double_t fdist, Int_t& numgroup, Int_t minnum = 8, int order = 0,
              Int_t* pHead = NULL, Int_t* pNext = NULL, Int_t* pTail = NULL, Int_t* pLen = NULL,
@@ -263,6 +402,7 @@ class KDTree {
     b_ = b;
     treetype_ = treetype;
     kerntype_ = kerntype;
+    kernres_ = kernres < 100 ? 100 : kernres;  // KDTree.cxx:1145-1148
     if (metric || keep_input_order || rdist_adapt > 0 || adaptive_fac > 0)
       throw nbkdt::Error(NBK_ERR_UNSUPPORTED,
                          "KDTree: metric, keep-input-order and adaptive trees are not supported");
@@ -318,10 +458,60 @@ class KDTree {
     return std::vector<Int_t>(out.begin(), out.begin() + total);
   }
 
+  // densities for the smoothing calls: the particles' own (densityset == 1), in ID order,
+  // or none (the call computes CalcDensity(Nsmooth) first)
+  std::vector<double> densities(int densityset) const {
+    std::vector<double> rho;
+    if (densityset == 1) {
+      rho.resize(numparts_);
+      for (Int_t i = 0; i < numparts_; i++) rho[bucket_[i].GetID()] = bucket_[i].GetDensity();
+    }
+    return rho;
+  }
+  static const double* rho_or_null(const std::vector<double>& rho) {
+    return rho.empty() ? nullptr : rho.data();
+  }
+  std::vector<double> mean_velocities(const Coordinate* smvel, int meanvelset, Int_t Nsmooth,
+                                      const std::vector<double>& rho) {
+    std::vector<double> sv(3 * (size_t)numparts_);
+    if (meanvelset == 1 && smvel) {
+      for (Int_t i = 0; i < numparts_; i++)
+        for (int k = 0; k < 3; k++) sv[3 * (size_t)i + k] = smvel[i][k];
+    } else {
+      nbkdt::check(nbk_smooth_vel(tree_, Nsmooth, rho_or_null(rho), sv.data()));
+    }
+    return sv;
+  }
+  static Matrix* to_matrices(const std::vector<double>& d, Int_t n) {
+    Matrix* out = new Matrix[n];
+    for (Int_t i = 0; i < n; i++)
+      for (int k = 0; k < 3; k++)
+        for (int l = 0; l < 3; l++) out[i](k, l) = d[9 * (size_t)i + 3 * k + l];
+    return out;
+  }
+  Coordinate* moment(const Coordinate* smvel, const Matrix* smveldisp, Int_t Nsmooth,
+                     int densityset, int meanvelset, int veldispset, bool kurtosis) {
+    std::vector<double> rho = densities(densityset);
+    std::vector<double> sv = mean_velocities(smvel, meanvelset, Nsmooth, rho);
+    std::vector<double> d(9 * (size_t)numparts_), v(3 * (size_t)numparts_);
+    if (veldispset == 1 && smveldisp) {
+      for (Int_t i = 0; i < numparts_; i++)
+        for (int k = 0; k < 3; k++)
+          for (int l = 0; l < 3; l++) d[9 * (size_t)i + 3 * k + l] = smveldisp[i](k, l);
+    } else {
+      nbkdt::check(nbk_smooth_vel_disp(tree_, Nsmooth, rho_or_null(rho), sv.data(), d.data()));
+    }
+    nbkdt::check((kurtosis ? nbk_smooth_vel_kurtosis : nbk_smooth_vel_skew)(
+        tree_, Nsmooth, rho_or_null(rho), sv.data(), d.data(), v.data()));
+    Coordinate* out = new Coordinate[numparts_];
+    for (Int_t i = 0; i < numparts_; i++) out[i] = Coordinate(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+    return out;
+  }
+
   nbk_tree* tree_ = nullptr;
   Particle* bucket_ = nullptr;
   Int_t numparts_ = 0, b_ = 16;
-  int treetype_ = 0, kerntype_ = 0;
+  int treetype_ = 0, kerntype_ = 0, kernres_ = 1000;
   int64_t numnodes_ = 0, numleaves_ = 0;
   Double_t kernnorm_ = 0;
   Double_t period_[3] = {0, 0, 0};

@@ -1,5 +1,5 @@
-// Test stand-in for NBodylib's NBody.h: just enough of NBody::Particle, NBody::System and
-// NBody::Coordinate (the accessors include/nbkdt/KDTree.h uses) to compile and run the
+// Test stand-in for NBodylib's NBody.h: just enough of NBody::Particle, NBody::System,
+// NBody::Coordinate and NBody::Matrix (the accessors include/nbkdt/KDTree.h uses) to compile and run the
 // drop-in KDTree where NBodylib itself is not installed. The member layout follows the
 // reference's default Particle (88 bytes: mass, position[3], velocity[3], pid, id, type,
 // rho, phi).
@@ -24,6 +24,21 @@ class Coordinate {
 
  private:
   Double_t c_[3];
+};
+
+class Matrix {
+ public:
+  Matrix() {
+    for (int i = 0; i < 9; i++) m_[i] = 0;
+  }
+  explicit Matrix(const Double_t m[9]) {
+    for (int i = 0; i < 9; i++) m_[i] = m[i];
+  }
+  Double_t& operator()(int i, int j) { return m_[j + 3 * i]; }
+  const Double_t& operator()(int i, int j) const { return m_[j + 3 * i]; }
+
+ private:
+  Double_t m_[9];
 };
 
 class Particle {

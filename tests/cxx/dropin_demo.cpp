@@ -8,7 +8,8 @@
 //   out.bin: int32 n, int32 numnodes, int32 numleaves, int32 ngroup,
 //            n x int32 group (by ID), n x double rho (by ID, CalcDensity(32)),
 //            n x 16 int32 FindNearest IDs (row by ID), n x 16 double d2,
-//            int32 ball count, ball IDs, double rho after the destructor (input order)
+//            int32 ball count, ball IDs, double rho after the destructor (input order),
+//            n x 3 double CalcSmoothVel(32) with the stored densities (by ID)
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -40,7 +41,7 @@ int main(int argc, char** argv) {
   fclose(f);
   double period[3] = {box, box, box};
   std::vector<int> group(n), nnid((size_t)n * 16), ballid;
-  std::vector<double> rho(n), d2((size_t)n * 16), rho_after(n);
+  std::vector<double> rho(n), d2((size_t)n * 16), rho_after(n), smvel(3 * (size_t)n);
   int numnodes, numleaves, ngroup = 0;
   {
     KDTree tree(parts.data(), n, 16, KDTree::TPHYS, KDTree::KSPH, 1000, 0, 0, 0,
@@ -53,6 +54,11 @@ int main(int argc, char** argv) {
     delete[] g;
     tree.CalcDensity(32);
     for (int t = 0; t < n; t++) rho[parts[t].GetID()] = parts[t].GetDensity();
+    // densityset = 1: the densities CalcDensity stored in the particles
+    Coordinate* sv = tree.CalcSmoothVel(32, 1);
+    for (int i = 0; i < n; i++)
+      for (int k = 0; k < 3; k++) smvel[3 * (size_t)i + k] = sv[i][k];
+    delete[] sv;
     std::vector<Int_t> nn(16);
     std::vector<Double_t> dd(16);
     for (int t = 0; t < n; t++) {
@@ -84,6 +90,7 @@ int main(int argc, char** argv) {
   fwrite(&nb, 4, 1, o);
   fwrite(ballid.data(), 4, nb, o);
   fwrite(rho_after.data(), 8, n, o);
+  fwrite(smvel.data(), 8, 3 * (size_t)n, o);
   fclose(o);
   printf("dropin ok: n=%d nodes=%d groups=%d\n", n, numnodes, ngroup);
   return 0;

@@ -73,6 +73,7 @@ def test_dropin_runs_like_the_reference(gpu, port_built, tmp_path, periodic):
     nb = take(np.int32, 1)[0]
     ball = take(np.int32, nb)
     rho_after = take(np.float64, n)
+    smvel = take(np.float64, 3 * n).reshape(n, 3)
     per = [box] * 3 if periodic else None
     o = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, per, backend="port")
     assert nodes == o.num_nodes and leaves == o.num_leaves
@@ -85,3 +86,8 @@ def test_dropin_runs_like_the_reference(gpu, port_built, tmp_path, periodic):
     assert_density_close(rho, ro, "drop-in CalcDensity")
     assert_density_close(rho_after, ro, "input order restored by the destructor")
     np.testing.assert_array_equal(np.sort(ball), o.ball_tagged(0, 4 * ll * ll))
+    # CalcSmoothVel with the stored densities (FP64 sums in another order: 1e-12 of the
+    # largest magnitude)
+    want = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, per,
+                             backend="port").smooth_vel_moments(0, 32, ro)
+    assert np.max(np.abs(smvel - want)) <= 1e-12 * np.max(np.abs(want))
