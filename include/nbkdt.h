@@ -312,6 +312,25 @@ int nbk_fof(nbk_tree* tree, double fdist, int32_t minnum, int order, int32_t* gr
 int nbk_fof_criterion(nbk_tree* tree, int comparator, const double* params, int32_t minnum,
                       int order, int32_t* group, int32_t* ngroup);
 
+/* Friends-of-friends over given neighbour lists. Replaces KDTree::FOFNNCriterion
+   (KDFOF.cxx:380-506): nn holds numnn tree indices per particle, rows by tree index (as
+   FindNearest gives them); particle t is linked with each nn[t][j] the comparator accepts.
+   The groups are the connected components of those links; groups below minnum are dropped
+   and the rest numbered 1..G by decreasing size (equal sizes by their first member in tree
+   order; the reference's order among equal sizes follows its priority queue). group: n, in
+   input order. */
+int nbk_fof_nn_criterion(nbk_tree* tree, int comparator, const double* params, int numnn,
+                         const int32_t* nn, int32_t minnum, int32_t* group, int32_t* ngroup);
+/* KDTree::FOFNNDistCriterion (KDFOF.cxx:507-640): as nbk_fof_nn_criterion, with
+   params[pidx[k]] (k < npc <= 8, pidx[k] <= 7) replaced for each particle t by values[t]
+   (tree order) before its comparisons: the value the reference takes from
+   distfunc(numNN, dist2[t]), which the caller evaluates (the drop-in class calls the
+   caller's function on the host). */
+int nbk_fof_nn_dist_criterion(nbk_tree* tree, int comparator, const double* params, int numnn,
+                              const int32_t* nn, const double* values, int npc,
+                              const int32_t* pidx, int32_t minnum, int32_t* group,
+                              int32_t* ngroup);
+
 /*
  * Density adjoint (no reference counterpart; the reference has no gradients).
  * Forward: rho = nbk_density(k). Loss L = sum_i w_i log rho_i. With the neighbour sets

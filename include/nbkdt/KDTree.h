@@ -383,6 +383,21 @@ class KDTree {
     return out;
   }
 
+  // FOF over the caller's neighbour lists (KDTree.h:509-515, KDFOF.cxx:380-640): nnIDs rows
+  // by tree index with numNN tree indices each (as FindNearest fills them); groups come back
+  // ID-indexed and numbered by decreasing size.
+  Int_t* FOFNNCriterion(FOFcompfunc p, Double_t* params, Int_t numNN, Int_t** nnIDs,
+                        Int_t& numgroups, Int_t minnum = 8) {
+    return fof_nn(p, params, numNN, nnIDs, nullptr, nullptr, 0, nullptr, numgroups, minnum);
+  }
+  // As FOFNNCriterion with params[npca[k]] = distfunc(numNN, dist2[t]) for each target t:
+  // the caller's function runs here on the host, once per particle, before the GPU pass.
+  Int_t* FOFNNDistCriterion(FOFcompfunc p, Double_t* params, Int_t numNN, Int_t** nnIDs,
+                            Double_t** dist2, Double_t distfunc(Int_t, Double_t*), Int_t npc,
+                            Int_t* npca, Int_t& numgroup, Int_t minnum = 8) {
+    return fof_nn(p, params, numNN, nnIDs, dist2, distfunc, npc, npca, numgroup, minnum);
+  }
+
   // ---- ordering (KDTree.h:522-524, KDTree.cxx:1358-1362)
   void OverWriteInputOrder() {
     iresetorder_ = false;
@@ -456,6 +471,36 @@ class KDTree {
     nbkdt::check(target ? nbk_ball_tagged(tree_, target, 1, fdist2, off, out.data(), total, &total)
                         : nbk_ball_tagged_points(tree_, x, 1, fdist2, off, out.data(), total, &total));
     return std::vector<Int_t>(out.begin(), out.begin() + total);
+  }
+
+  Int_t* fof_nn(FOFcompfunc p, Double_t* params, Int_t numNN, Int_t** nnIDs, Double_t** dist2,
+                Double_t (*distfunc)(Int_t, Double_t*), Int_t npc, Int_t* npca, Int_t& numgroups,
+                Int_t minnum) {
+    int cmp = p == &FOF3d ? NBK_FOF3D : (p == &FOFVel ? NBK_FOFVEL : (p == &FOF6d ? NBK_FOF6D : -1));
+    if (cmp < 0)
+      throw nbkdt::Error(NBK_ERR_UNSUPPORTED,
+                         "FOFNNCriterion: only FOF3d, FOFVel and FOF6d run on the GPU");
+    std::vector<int32_t> nn((size_t)numparts_ * numNN), g(numparts_), pidx;
+    for (Int_t t = 0; t < numparts_; t++)
+      for (Int_t j = 0; j < numNN; j++) nn[(size_t)t * numNN + j] = (int32_t)nnIDs[t][j];
+    std::vector<double> values;
+    if (distfunc) {
+      values.resize(numparts_);
+      for (Int_t t = 0; t < numparts_; t++) values[t] = distfunc(numNN, dist2[t]);
+      for (Int_t k = 0; k < npc; k++) pidx.push_back((int32_t)npca[k]);
+    }
+    int32_t ng = 0;
+    if (distfunc)
+      nbkdt::check(nbk_fof_nn_dist_criterion(tree_, cmp, params, (int)numNN, nn.data(),
+                                             values.data(), (int)npc, pidx.data(),
+                                             (int32_t)minnum, g.data(), &ng));
+    else
+      nbkdt::check(nbk_fof_nn_criterion(tree_, cmp, params, (int)numNN, nn.data(),
+                                        (int32_t)minnum, g.data(), &ng));
+    numgroups = ng;
+    Int_t* out = new Int_t[numparts_];
+    for (Int_t i = 0; i < numparts_; i++) out[i] = g[i];
+    return out;
   }
 
   // densities for the smoothing calls: the particles' own (densityset == 1), in ID order,

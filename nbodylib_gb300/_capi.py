@@ -66,6 +66,10 @@ SIGNATURES = {
     "nbk_ball_mark": (c_int, [c_vp, ctypes.c_int32, c_dbl, ctypes.c_int32, c_vp, c_vp]),
     "nbk_fof": (c_int, [c_vp, c_dbl, ctypes.c_int32, c_int, c_vp, c_i32p]),
     "nbk_fof_criterion": (c_int, [c_vp, c_int, c_vp, ctypes.c_int32, c_int, c_vp, c_i32p]),
+    "nbk_fof_nn_criterion": (c_int, [c_vp, c_int, c_vp, c_int, c_vp, ctypes.c_int32, c_vp,
+                                     c_i32p]),
+    "nbk_fof_nn_dist_criterion": (c_int, [c_vp, c_int, c_vp, c_int, c_vp, c_vp, c_int, c_vp,
+                                          ctypes.c_int32, c_vp, c_i32p]),
     "nbk_density_adjoint": (c_int, [c_vp, c_int, c_vp, c_vp, c_vp, c_vp]),
     "nbk_batch_create": (c_int, [c_vp, c_vp, c_vp, c_i64, c_int, c_int, c_int, ctypes.c_uint,
                                  ctypes.POINTER(c_vp)]),

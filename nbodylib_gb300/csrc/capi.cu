@@ -1222,6 +1222,93 @@ int nbk_fof_criterion(nbk_tree* t, int comparator, const double* params, int32_t
   API_END
 }
 
+// FOF over given neighbour lists: nn rows by tree index, numnn tree indices per row;
+// values (tree order) replace params[pidx[k]] per target for the distance form.
+static int fof_nn_common(nbk_tree* t, int comparator, const double* params, int numnn,
+                         const int32_t* nn, const double* values, int npc, const int32_t* pidx,
+                         int32_t minnum, int32_t* group, int32_t* ngroup) {
+  if (!group || !ngroup || !params || !nn || numnn < 0 || npc < 0 || npc > 8 ||
+      (npc > 0 && (!values || !pidx))) {
+    set_error("nbk_fof_nn_criterion: invalid argument");
+    return NBK_ERR_INVALID;
+  }
+  if (comparator < NBK_FOF3D || comparator > NBK_FOF6D) {
+    set_error("nbk_fof_nn_criterion: only the FOF3d, FOFVel and FOF6d comparators run on the GPU");
+    return NBK_ERR_UNSUPPORTED;
+  }
+  if (comparator != NBK_FOF3D && !t->has_vel) {
+    set_error("nbk_fof_nn_criterion: FOFVel and FOF6d need velocities at nbk_create");
+    return NBK_ERR_INVALID;
+  }
+  double p[8];
+  int32_t pi[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (t->dev()) {
+    NBK_CUDA_TRY(cudaMemcpy(p, params, sizeof(p), cudaMemcpyDeviceToHost));
+    if (npc) NBK_CUDA_TRY(cudaMemcpy(pi, pidx, sizeof(int32_t) * npc, cudaMemcpyDeviceToHost));
+  } else {
+    memcpy(p, params, sizeof(p));
+    if (npc) memcpy(pi, pidx, sizeof(int32_t) * npc);
+  }
+  for (int k = 0; k < npc; k++)
+    if (pi[k] < 0 || pi[k] > 7) {
+      set_error("nbk_fof_nn_dist_criterion: parameter index outside params[0..7]");
+      return NBK_ERR_INVALID;
+    }
+  Stage S(t);
+  const int32_t* dnn;
+  const double* dval = nullptr;
+  int* dg;
+  NBK_TRY(S.in(nn, (size_t)t->n * numnn, &dnn));
+  if (npc) NBK_TRY(S.in(values, t->n, &dval));
+  NBK_TRY(S.out(group, t->n, &dg));
+  int *parent, *gtree;
+  NBK_TRY(S.alloc.get((void**)&parent, sizeof(int) * t->n));
+  NBK_TRY(S.alloc.get((void**)&gtree, sizeof(int) * t->n));
+  NBK_TRY(clear_err(t));
+  FofArgs a{};
+  a.tv = t->view();
+  a.crit = 2;
+  a.cmp = comparator;
+  for (int i = 0; i < 8; i++) a.params[i] = p[i];
+  a.parent = parent;
+  a.err = t->d_err;
+  a.nn = dnn;
+  a.numnn = numnn;
+  a.pval = dval;
+  a.npc = npc;
+  for (int k = 0; k < npc; k++) a.pidx[k] = pi[k];
+  int ng = 0;
+  // groups are numbered by decreasing size, as the reference's (KDFOF.cxx:493-503)
+  NBK_TRY(run_fof(a, (int)t->nslots, minnum, 1, gtree, &ng, S.alloc, t->st));
+  k_scatter_i<<<(unsigned)((t->n + 255) / 256), 256, 0, t->st>>>(gtree, t->arr.perm, dg, t->n);
+  note_launch();
+  NBK_CUDA_TRY(cudaGetLastError());
+  NBK_TRY(S.finish());
+  NBK_TRY(check_err(t, "nbk_fof_nn_criterion"));
+  *ngroup = ng;
+  return NBK_OK;
+}
+
+int nbk_fof_nn_criterion(nbk_tree* t, int comparator, const double* params, int numnn,
+                         const int32_t* nn, int32_t minnum, int32_t* group, int32_t* ngroup) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return fof_nn_common(t, comparator, params, numnn, nn, nullptr, 0, nullptr, minnum, group,
+                       ngroup);
+  API_END
+}
+
+int nbk_fof_nn_dist_criterion(nbk_tree* t, int comparator, const double* params, int numnn,
+                              const int32_t* nn, const double* values, int npc,
+                              const int32_t* pidx, int32_t minnum, int32_t* group,
+                              int32_t* ngroup) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return fof_nn_common(t, comparator, params, numnn, nn, values, npc, pidx, minnum, group,
+                       ngroup);
+  API_END
+}
+
 int nbk_density_adjoint(nbk_tree* t, int k, const double* w, double* rho, double* grad_pos,
                         double* grad_mass) {
   API_BEGIN

@@ -312,6 +312,45 @@ __device__ __forceinline__ double crit_invscaling(const double* p, int cd) {
   return 1.0;
 }
 
+// ---- FOFNNCriterion / FOFNNDistCriterion (KDFOF.cxx:380-506, 507-640). The reference
+// grows groups breadth-first, testing each member t against its listed neighbours
+// nn[t][j] with the comparator; every particle ends up tested, and merges join whole
+// groups, so its groups are the connected components of the accepted (t, nn[t][j]) edges.
+// One thread per particle unites it with each accepted neighbour. For the distance form,
+// params[pidx[k]] take the particle's own value before its comparisons, as the reference
+// sets them from distfunc(numNN, dist2[t]).
+__global__ void __launch_bounds__(256) k_nn_link(FofArgs a) {
+  const TreeView& tv = a.tv;
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= tv.n) return;
+  int self = tv.pstart + q;
+  P4 me = tv.pos[self];
+  V4 mv = tv.vel ? tv.vel[self] : make_v4(0, 0, 0, 0);
+  double x0[3] = {me.x, me.y, me.z};
+  double p[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) p[k] = a.params[k];
+  if (a.pval)
+    for (int k = 0; k < a.npc; k++) {
+      double v = a.pval[q];
+#pragma unroll
+      for (int m = 0; m < 8; m++)
+        if (m == a.pidx[k]) p[m] = v;  // static indices keep p in registers
+    }
+  const int* row = a.nn + (size_t)q * a.numnn;
+  for (int j = 0; j < a.numnn; j++) {
+    int b = row[j];
+    if (b < 0 || b >= tv.n) {
+      if (b >= tv.n) atomicExch(a.err, kErrTarget);
+      continue;
+    }
+    if (b == q) continue;
+    int bi = tv.pstart + b;
+    V4 vb = tv.vel ? tv.vel[bi] : make_v4(0, 0, 0, 0);
+    if (crit_cmp(a.cmp, p, x0, mv, tv.pos[bi], vb)) unite(a.parent, self, bi, a.err);
+  }
+}
+
 __global__ void __launch_bounds__(128) k_crit_link(FofArgs a) {
   const TreeView& tv = a.tv;
   int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -531,7 +570,10 @@ int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tr
     k_compress<<<(n + 255) / 256, 256, 0, st>>>(a.parent, n); note_launch();
   }
   int warps = (n + 31) / 32;
-  if (a.crit) {
+  if (a.crit == 2) {
+    Phase ph("fof_nn_link", st);
+    k_nn_link<<<(n + 255) / 256, 256, 0, st>>>(a); note_launch();
+  } else if (a.crit) {
     Phase ph("fof_criterion_link", st);
     k_crit_link<<<(n + 127) / 128, 128, 0, st>>>(a); note_launch();
   } else {

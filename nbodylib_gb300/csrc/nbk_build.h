@@ -136,11 +136,16 @@ int launch_knn_batch(const KnnArgs& a, const BatchArgs& b, cudaStream_t st);
 struct FofArgs {
   TreeView tv;
   double ll2;          // linking length squared
-  int crit;            // 0: plain FOF, 1: FOFCriterion
+  int crit;            // 0: plain FOF, 1: FOFCriterion, 2: FOFNN[Dist]Criterion
   int cmp;             // comparator for crit
   double params[8];
   int* parent;         // tree order union-find forest
   int* err;
+  const int* nn;       // crit 2: neighbour lists, [n][numnn] tree indices (row = tree index)
+  int numnn;
+  const double* pval;  // crit 2, FOFNNDistCriterion: per-particle value (tree order) for
+  int npc;             //   params[pidx[0..npc)]
+  int pidx[8];
 };
 int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tree,
             int* h_ngroup, DevAlloc& alloc, cudaStream_t st);

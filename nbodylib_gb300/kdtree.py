@@ -351,6 +351,43 @@ class KDTree:
                                                 int(order), _ptr(group), ctypes.byref(ng)))
         return group, ng.value
 
+    # ---- FOF over given neighbour lists (KDTree.h:497-515, KDFOF.cxx:380-640)
+    def FOFNNCriterion(self, comparator, params, nn, minnum=8):
+        """nn: (n, numNN) tree indices, rows by tree index (as FindNearest returns them).
+        Returns (group[n] in input order, numbered by decreasing size, ngroup)."""
+        return self._fof_nn(comparator, params, nn, None, None, minnum)
+
+    def FOFNNDistCriterion(self, comparator, params, nn, values, pidx, minnum=8):
+        """As FOFNNCriterion, with params[pidx[k]] replaced per particle by values (tree
+        order): the values the reference takes from distfunc(numNN, dist2[t])."""
+        return self._fof_nn(comparator, params, nn, values, pidx, minnum)
+
+    def _fof_nn(self, comparator, params, nn, values, pidx, minnum):
+        p = np.zeros(8)
+        p[: min(8, len(params))] = np.asarray(params, np.float64)[:8]
+        if self.device:
+            p = self._torch.from_numpy(p).cuda()
+            nn = nn.to(self._torch.int32).contiguous()
+            vals = None if values is None else values.to(self._torch.float64).contiguous()
+            pi = None if pidx is None else self._torch.as_tensor(
+                np.asarray(pidx, np.int32)).cuda()
+        else:
+            nn = np.ascontiguousarray(nn, np.int32)
+            vals = None if values is None else np.ascontiguousarray(values, np.float64)
+            pi = None if pidx is None else np.ascontiguousarray(pidx, np.int32)
+        numnn = nn.shape[1]
+        group = self._empty(self.n, np.int32)
+        ng = ctypes.c_int32()
+        if vals is None:
+            _capi.check(self._lib.nbk_fof_nn_criterion(self._h, int(comparator), _ptr(p), numnn,
+                                                       _ptr(nn), int(minnum), _ptr(group),
+                                                       ctypes.byref(ng)))
+        else:
+            _capi.check(self._lib.nbk_fof_nn_dist_criterion(
+                self._h, int(comparator), _ptr(p), numnn, _ptr(nn), _ptr(vals), len(pi), _ptr(pi),
+                int(minnum), _ptr(group), ctypes.byref(ng)))
+        return group, ng.value
+
     # ---- adjoint (no reference counterpart)
     def DensityAdjoint(self, k, w):
         w = w if self.device else np.ascontiguousarray(w, np.float64)

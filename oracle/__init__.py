@@ -72,6 +72,8 @@ def _lib(backend: str) -> ctypes.CDLL:
         "ball_tagged_pos": (ctypes.c_int, [vp, _c_dbl_p, ctypes.c_double, _c_int_p]),
         "ball_mark": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, _c_int_p,
                                      _c_dbl_p]),
+        "fof_nn": (ctypes.c_int, [vp, ctypes.c_int, _c_dbl_p, ctypes.c_int, _c_int_p, _c_dbl_p,
+                                  ctypes.c_int, _c_int_p, ctypes.c_int, _c_int_p, _c_int_p]),
         "smooth_vel_moments": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, _c_dbl_p, _c_dbl_p,
                                               _c_dbl_p, _c_dbl_p]),
         "veldensity_phys": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, _c_dbl_p, _c_dbl_p]),
@@ -265,6 +267,38 @@ class OracleTree:
         ng = ctypes.c_int(0)
         self._f("fof_criterion")(self._h, cmp, _dp(p), minnum, order, _ip(g), ctypes.byref(ng))
         return g, ng.value
+
+    def fof_nn(self, cmp, params, nn, minnum=8, values=None, pidx=None, dist2=None):
+        """FOFNNCriterion over lists nn (rows by this tree's index, tree indices). The
+        restatement takes per-target values (tree order) with parameter indices pidx; the
+        reference takes the lists' dist2 and uses the row maximum as its distfunc."""
+        p = np.zeros(20)
+        p[:len(params)] = params
+        nn = np.ascontiguousarray(nn, np.int32)
+        numnn = nn.shape[1]
+        group = np.empty(self.n, np.int32)
+        ng = ctypes.c_int()
+        pi = None if pidx is None else np.ascontiguousarray(pidx, np.int32)
+        npc = 0 if pi is None else len(pi)
+        if self.backend == "port":
+            vals = None if values is None else np.ascontiguousarray(values, np.float64)
+            self._f("fof_nn")(self._h, cmp, _dp(p), numnn, _ip(nn), _dp(vals), npc, _ip(pi),
+                              minnum, _ip(group), ctypes.byref(ng))
+        else:
+            d2 = None if dist2 is None else np.ascontiguousarray(dist2, np.float64)
+            self._f("fof_nn")(self._h, cmp, _dp(p), numnn, _ip(nn), _dp(d2), npc, _ip(pi),
+                              minnum, _ip(group), ctypes.byref(ng))
+        return group, ng.value
+
+    def tree_knn(self, k):
+        """FindNearest rows by this tree's index holding tree indices (the lists
+        FOFNNCriterion takes), with their d2."""
+        nn, d2 = self.knn(k, method=0)  # rows by ID, IDs
+        ids = self.ids()  # tree index -> ID
+        tree_of = np.empty_like(ids)
+        tree_of[ids] = np.arange(len(ids))
+        return (np.ascontiguousarray(tree_of[nn[ids]], np.int32),
+                np.ascontiguousarray(d2[ids]))
 
     def ball_tagged(self, pid, fdist2):
         out = np.empty(8 * self.n + 16, np.int32)

@@ -1156,6 +1156,135 @@ int pt_fof_criterion(PTree* t, int cmp, const double* params, int minnum, int or
     return fof_driver(t, 1, 0.0, cmp, params, minnum, order, group, ngroup);
 }
 
+/* ------------------------------------------------------- FOF over given lists */
+/* FOF comparators (FOFFunc.h:30-55) between two particles. */
+static int nn_cmp(int cmp, const double* params, const PPart* a, const PPart* b) {
+    double total = 0;
+    if (cmp == 0) {
+        for (int j = 0; j < 3; j++) total += (a->pos[j] - b->pos[j]) * (a->pos[j] - b->pos[j]) / params[6];
+    } else if (cmp == 1) {
+        for (int j = 0; j < 3; j++) total += (a->vel[j] - b->vel[j]) * (a->vel[j] - b->vel[j]) / params[6];
+    } else {
+        for (int j = 0; j < 3; j++) {
+            total += (a->pos[j] - b->pos[j]) * (a->pos[j] - b->pos[j]) / params[6];
+            total += (a->vel[j] - b->vel[j]) * (a->vel[j] - b->vel[j]) / params[7];
+        }
+    }
+    return (total < 1);
+}
+
+/* KDTree::FOFNNCriterion / FOFNNDistCriterion (KDFOF.cxx:380-640). Groups grow breadth
+   first in tree order; each member is tested against its listed neighbours; a neighbour
+   already in an older group brings that whole group in (its member list is spliced onto
+   the current one); groups below minnum are cleared and the rest numbered by size through
+   the max-heap. With values, params[pidx[k]] take values[target] before each target's
+   comparisons (the reference's distfunc(numNN, dist2[target])). */
+int pt_fof_nn(PTree* t, int cmp, const double* params_in, int numnn, const int* nn,
+              const double* values, int npc, const int* pidx, int minnum, int* group,
+              int* ngroup) {
+    int n = t->n;
+    double params[20];
+    for (int k = 0; k < 20; k++) params[k] = params_in[k];
+    int* head_of = (int*)malloc(sizeof(int) * (size_t)(n + 1)); /* first member of each group */
+    int* fifo = (int*)malloc(sizeof(int) * (size_t)n);
+    int* phead = (int*)malloc(sizeof(int) * (size_t)n);
+    int* ptail = (int*)malloc(sizeof(int) * (size_t)n);
+    int* pnext = (int*)malloc(sizeof(int) * (size_t)n);
+    int* plen = (int*)malloc(sizeof(int) * (size_t)(n + 1));
+    for (int i = 0; i < n; i++) {
+        group[i] = 0;
+        phead[i] = ptail[i] = i;
+        pnext[i] = -1;
+    }
+    int ig = 0, qh = 0, qt = 0;
+    for (int i = 0; i < n; i++) {
+        if (group[t->p[i].id] != 0) continue;
+        group[t->p[i].id] = ++ig;
+        plen[ig] = 1;
+        head_of[ig] = i;
+        fifo[qt++] = i;
+        if (qt == n) qt = 0;
+        while (qh != qt) {
+            int target = fifo[qh++];
+            if (qh == n) qh = 0;
+            if (values)
+                for (int k = 0; k < npc; k++) params[pidx[k]] = values[target];
+            for (int j = 0; j < numnn; j++) {
+                int nb = nn[(size_t)target * numnn + j];
+                int nid = t->p[nb].id;
+                if (group[nid] == ig) continue;
+                if (!nn_cmp(cmp, params, &t->p[target], &t->p[nb])) continue;
+                if (group[nid] > 0) {
+                    int old = group[nid], oh = head_of[old], otail = ptail[oh];
+                    int ctail = ptail[head_of[ig]];
+                    int m = oh;
+                    do {
+                        group[t->p[m].id] = ig;
+                        phead[m] = head_of[ig];
+                    } while ((m = pnext[m]) != -1);
+                    m = ctail;
+                    do {
+                        ptail[m] = otail;
+                    } while ((m = pnext[m]) != -1);
+                    plen[ig] += plen[old];
+                    plen[old] = -1;
+                    pnext[ctail] = oh;
+                    ptail[head_of[ig]] = otail;
+                    phead[oh] = head_of[ig];
+                } else {
+                    group[nid] = ig;
+                    fifo[qt++] = nb;
+                    plen[ig]++;
+                    pnext[ptail[head_of[ig]]] = nb;
+                    ptail[head_of[ig]] = nb;
+                    phead[nb] = head_of[ig];
+                    if (qt == n) qt = 0;
+                }
+            }
+        }
+    }
+    /* members of each live group in tree order, then the minnum cut and the size order */
+    int** plist = (int**)malloc(sizeof(int*) * (size_t)(ig + 1));
+    int* pcount = (int*)calloc((size_t)ig + 1, sizeof(int));
+    for (int g = 1; g <= ig; g++) plist[g] = plen[g] > 0 ? (int*)malloc(sizeof(int) * plen[g]) : NULL;
+    for (int i = 0; i < n; i++) {
+        int gid = group[t->p[i].id];
+        if (gid > 0 && plen[gid] > 0) plist[gid][pcount[gid]++] = i;
+    }
+    int total = ig, live = ig;
+    for (int g = 1; g <= total; g++) {
+        if (plen[g] < minnum) {
+            if (plen[g] > 0)
+                for (int j = 0; j < plen[g]; j++) group[t->p[plist[g][j]].id] = 0;
+            plen[g] = 0;
+            live--;
+        }
+    }
+    if (live) {
+        PQ pq;
+        pq_init(&pq, live);
+        for (int g = 1; g <= total; g++)
+            if (plen[g] > 0) pq_push(&pq, g, plen[g]);
+        for (int r = 1; r <= live; r++) {
+            int gid = pq_topq(&pq), size = (int)pq_top(&pq);
+            pq_pop(&pq);
+            for (int j = 0; j < size; j++) group[t->p[plist[gid][j]].id] = r;
+        }
+        pq_free(&pq);
+    }
+    for (int g = 1; g <= total; g++) free(plist[g]);
+    free(plist);
+    free(pcount);
+    free(head_of);
+    free(fifo);
+    free(phead);
+    free(ptail);
+    free(pnext);
+    free(plen);
+    *ngroup = live;
+    return 0;
+}
+
 /* ---------------------------------------------------------------- adjoint */
 /* Frozen density model shared by the adjoint and the finite-difference check.
    rho_i = sum_{j in N(i)} w_ij m_j + sum_{l : i in N(l)} w_li m_l,

@@ -44,6 +44,11 @@ int pt_fof(PTree* t, double ll, int minnum, int order, int* group, int* ngroup);
 /* cmp: 0 FOF3d, 1 FOFVel, 2 FOF6d (src/KDTree/FOFFunc.h:30-55). params as the reference. */
 int pt_fof_criterion(PTree* t, int cmp, const double* params, int minnum, int order, int* group,
                      int* ngroup);
+/* FOFNNCriterion / FOFNNDistCriterion over lists nn (rows by tree index, tree indices);
+   values (tree order) with npc parameter indices pidx, or NULL. group in ID order. */
+int pt_fof_nn(PTree* t, int cmp, const double* params, int numnn, const int* nn,
+              const double* values, int npc, const int* pidx, int minnum, int* group,
+              int* ngroup);
 int pt_ball_tagged(PTree* t, int id, double fdist2, int* out_ids);
 int pt_ball_tagged_pos(PTree* t, const double* x, double fdist2, int* out_ids);
 int pt_ball_mark(PTree* t, int id, double fdist2, int imark, int* mark, double* dist2);

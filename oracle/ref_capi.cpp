@@ -221,6 +221,44 @@ int ref_ball_mark(void* h, int id, double fdist2, int imark, int* mark, double* 
     return 0;
 }
 
+// ---- FOFNNCriterion / FOFNNDistCriterion (KDFOF.cxx:380-640). nn rows by tree index.
+// The distance form uses distfunc = the largest squared distance of the row.
+static Double_t row_max(Int_t num, Double_t* d2) {
+    Double_t m = d2[0];
+    for (Int_t j = 1; j < num; j++) m = d2[j] > m ? d2[j] : m;
+    return m;
+}
+
+int ref_fof_nn(void* h, int cmp, const double* params, int numnn, const int* nn,
+               const double* dist2, int npc, const int* pidx, int minnum, int* group,
+               int* ngroup) {
+    RefTree* r = (RefTree*)h;
+    double p[20];
+    for (int i = 0; i < 20; i++) p[i] = params[i];
+    FOFcompfunc f = cmp == 0 ? FOF3d : (cmp == 1 ? FOFVel : FOF6d);
+    std::vector<Int_t*> rows(r->n);
+    std::vector<Double_t*> drows(r->n);
+    std::vector<Int_t> flat((size_t)r->n * numnn);
+    std::vector<Double_t> dflat((size_t)r->n * numnn);
+    for (int i = 0; i < r->n; i++) {
+        rows[i] = &flat[(size_t)i * numnn];
+        drows[i] = &dflat[(size_t)i * numnn];
+        for (int j = 0; j < numnn; j++) {
+            rows[i][j] = nn[(size_t)i * numnn + j];
+            if (dist2) drows[i][j] = dist2[(size_t)i * numnn + j];
+        }
+    }
+    std::vector<Int_t> npca(pidx ? pidx : (const int*)nullptr, pidx ? pidx + npc : nullptr);
+    Int_t ng = 0;
+    Int_t* g = dist2 ? r->tree->FOFNNDistCriterion(f, p, numnn, rows.data(), drows.data(), row_max,
+                                                    npc, npca.data(), ng, minnum)
+                     : r->tree->FOFNNCriterion(f, p, numnn, rows.data(), ng, minnum);
+    std::memcpy(group, g, sizeof(int) * r->n);
+    delete[] g;
+    *ngroup = ng;
+    return 0;
+}
+
 // ---- SPH smoothing (KDCalcSmoothQuantities.cxx:393-766, 922-1091, 1209-1306, 1539-1700).
 // rho != NULL: set the particles' densities and pass densityset = 1; otherwise the
 // reference computes CalcDensity(Nsmooth) itself (densityset = 0).

@@ -9,7 +9,8 @@
 //            n x int32 group (by ID), n x double rho (by ID, CalcDensity(32)),
 //            n x 16 int32 FindNearest IDs (row by ID), n x 16 double d2,
 //            int32 ball count, ball IDs, double rho after the destructor (input order),
-//            n x 3 double CalcSmoothVel(32) with the stored densities (by ID)
+//            n x 3 double CalcSmoothVel(32) with the stored densities (by ID),
+//            int32 ngroup_nn, n x int32 FOFNNCriterion(FOF3d, 16 lists) groups (by ID)
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -40,7 +41,8 @@ int main(int argc, char** argv) {
   }
   fclose(f);
   double period[3] = {box, box, box};
-  std::vector<int> group(n), nnid((size_t)n * 16), ballid;
+  std::vector<int> group(n), nnid((size_t)n * 16), ballid, group_nn(n);
+  int ngroup_nn = 0;
   std::vector<double> rho(n), d2((size_t)n * 16), rho_after(n), smvel(3 * (size_t)n);
   int numnodes, numleaves, ngroup = 0;
   {
@@ -61,14 +63,24 @@ int main(int argc, char** argv) {
     delete[] sv;
     std::vector<Int_t> nn(16);
     std::vector<Double_t> dd(16);
+    std::vector<Int_t> flat((size_t)n * 16);
+    std::vector<Int_t*> rows(n);
     for (int t = 0; t < n; t++) {
       tree.FindNearest(t, nn.data(), dd.data(), 16);
       int id = parts[t].GetID();
+      rows[t] = &flat[(size_t)t * 16];
       for (int j = 0; j < 16; j++) {
         nnid[(size_t)id * 16 + j] = parts[nn[j]].GetID();
         d2[(size_t)id * 16 + j] = dd[j];
+        rows[t][j] = nn[j];  // tree indices, as the reference's lists
       }
     }
+    Double_t fof_params[8] = {0, 0, 0, 0, 0, 0, 0.35, 0};
+    Int_t ngn = 0;
+    Int_t* gn = tree.FOFNNCriterion(FOF3d, fof_params, 16, rows.data(), ngn, 5);
+    for (int i = 0; i < n; i++) group_nn[i] = gn[i];
+    ngroup_nn = ngn;
+    delete[] gn;
     // the tree index of ID 0
     int t0 = 0;
     while (parts[t0].GetID() != 0) t0++;
@@ -91,6 +103,8 @@ int main(int argc, char** argv) {
   fwrite(ballid.data(), 4, nb, o);
   fwrite(rho_after.data(), 8, n, o);
   fwrite(smvel.data(), 8, 3 * (size_t)n, o);
+  fwrite(&ngroup_nn, 4, 1, o);
+  fwrite(group_nn.data(), 4, n, o);
   fclose(o);
   printf("dropin ok: n=%d nodes=%d groups=%d\n", n, numnodes, ngroup);
   return 0;

@@ -74,6 +74,8 @@ def test_dropin_runs_like_the_reference(gpu, port_built, tmp_path, periodic):
     ball = take(np.int32, nb)
     rho_after = take(np.float64, n)
     smvel = take(np.float64, 3 * n).reshape(n, 3)
+    ngroup_nn = take(np.int32, 1)[0]
+    group_nn = take(np.int32, n)
     per = [box] * 3 if periodic else None
     o = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, per, backend="port")
     assert nodes == o.num_nodes and leaves == o.num_leaves
@@ -91,3 +93,9 @@ def test_dropin_runs_like_the_reference(gpu, port_built, tmp_path, periodic):
     want = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, per,
                              backend="port").smooth_vel_moments(0, 32, ro)
     assert np.max(np.abs(smvel - want)) <= 1e-12 * np.max(np.abs(want))
+    # FOFNNCriterion over the FindNearest lists (the same lists in tree indices)
+    pn, _ = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, per, backend="port").tree_knn(16)
+    gp, ngp = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, per,
+                                backend="port").fof_nn(0, [0, 0, 0, 0, 0, 0, 0.35, 0], pn, 5)
+    assert ngroup_nn == ngp
+    assert_same_partition(group_nn, gp, "drop-in FOFNNCriterion")

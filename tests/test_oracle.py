@@ -223,3 +223,21 @@ def test_port_matches_golden_smoothing(port_built):
                           backend="port")
     assert np.array_equal(Q.veldensity_phys(int(g["phys_nsmooth"]), int(g["phys_nsearch"])),
                           g["veldensity_phys"])
+
+
+@pytest.mark.parametrize("cmp", [0, 1, 2])
+def test_port_fof_nn_matches_reference(ref_built, cmp):
+    """FOFNNCriterion and FOFNNDistCriterion over FindNearest lists: the restatement gives
+    the reference's groups and numbering exactly."""
+    pos, mass, vel = syn.clustered_box(4000, 60.0, seed=41 + cmp, velocities=True)
+    R = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, None, backend="ref")
+    P = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, None, backend="port")
+    rn, rd = R.tree_knn(12)
+    pn, pd = P.tree_knn(12)
+    params = [0, 0.25, 1.0, 0, 0, 0, 0.25, 0.3]
+    gr, ngr = R.fof_nn(cmp, params, rn, 5)
+    gp, ngp = P.fof_nn(cmp, params, pn, 5)
+    assert ngr == ngp and np.array_equal(gr, gp)
+    gr, ngr = R.fof_nn(cmp, params, rn, 5, pidx=[6], dist2=rd * 0.4)
+    gp, ngp = P.fof_nn(cmp, params, pn, 5, values=(pd * 0.4).max(1), pidx=[6])
+    assert ngr == ngp and np.array_equal(gr, gp)
