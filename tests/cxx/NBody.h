@@ -6,6 +6,7 @@
 #pragma once
 #include <cmath>
 #include <cstddef>
+#include <vector>
 
 typedef double Double_t;
 typedef int Int_t;
@@ -68,14 +69,20 @@ class Particle {
 
 class System {
  public:
-  System(Particle* p, Int_t n, Coordinate period) : p_(p), n_(n), period_(period) {}
-  Particle* Parts() const { return p_; }
-  Int_t GetNumParts() const { return n_; }
+  // as the reference's System(num, p, t, period) (src/NBody/System.h:60): the system keeps
+  // its own copy of the particles
+  System(Int_t num, Particle* p, Double_t t = 0.0, Double_t* period = NULL)
+      : parts_(p, p + num), period_(period ? period[0] : 0, period ? period[1] : 0,
+                                    period ? period[2] : 0) {
+    (void)t;
+  }
+  Particle* Parts() { return parts_.data(); }
+  Int_t GetNumParts() const { return (Int_t)parts_.size(); }
   Coordinate GetPeriod() const { return period_; }
+  Particle& operator[](Int_t i) { return parts_[i]; }
 
  private:
-  Particle* p_;
-  Int_t n_;
+  std::vector<Particle> parts_;
   Coordinate period_;
 };
 

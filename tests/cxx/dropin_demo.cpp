@@ -10,7 +10,8 @@
 //            n x 16 int32 FindNearest IDs (row by ID), n x 16 double d2,
 //            int32 ball count, ball IDs, double rho after the destructor (input order),
 //            n x 3 double CalcSmoothVel(32) with the stored densities (by ID),
-//            int32 ngroup_nn, n x int32 FOFNNCriterion(FOF3d, 16 lists) groups (by ID)
+//            int32 ngroup_nn, n x int32 FOFNNCriterion(FOF3d, 16 lists) groups (by ID),
+//            n x double density after DensitySmooth(S, 16, 32) (input order)
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -89,6 +90,16 @@ int main(int argc, char** argv) {
   }
   // the destructor restored input order
   for (int i = 0; i < n; i++) rho_after[i] = parts[i].GetDensity();
+  // DensitySmooth(System&, b, k) of src/Analysis/Density.cxx:157-163, the reference's
+  // in-repo caller: a System-constructed tree (default kernel) and CalcDensity
+  std::vector<double> rho_smooth(n);
+  {
+    System S(n, parts.data());
+    KDTree* tree = new KDTree(S, 16);
+    tree->CalcDensity(32);
+    delete tree;
+    for (int i = 0; i < n; i++) rho_smooth[i] = S[i].GetDensity();
+  }
   FILE* o = fopen(argv[2], "wb");
   fwrite(&n, 4, 1, o);
   fwrite(&numnodes, 4, 1, o);
@@ -105,6 +116,7 @@ int main(int argc, char** argv) {
   fwrite(smvel.data(), 8, 3 * (size_t)n, o);
   fwrite(&ngroup_nn, 4, 1, o);
   fwrite(group_nn.data(), 4, n, o);
+  fwrite(rho_smooth.data(), 8, n, o);
   fclose(o);
   printf("dropin ok: n=%d nodes=%d groups=%d\n", n, numnodes, ngroup);
   return 0;

@@ -36,6 +36,23 @@ def test_compiles_against_the_reference_headers(lib_built, tmp_path):
     compile_demo(str(tmp_path / "demo_ref.o"), inc, link=False)
 
 
+def test_reference_density_smooth_compiles_unmodified(lib_built, tmp_path):
+    """The reference's own in-repo caller, src/Analysis/Density.cxx (DensitySmooth:
+    KDTree(S, b) + CalcDensity), compiles unmodified against the drop-in through
+    include/compat/KDTree.h placed ahead of the reference's KDTree headers."""
+    ref = os.environ.get("NBKDT_REF_SRC", oracle.DEFAULT_REF_SRC)
+    src = os.path.join(ref, "src", "Analysis", "Density.cxx")
+    if not os.path.exists(src):
+        pytest.skip("reference checkout not present on this machine")
+    inc = [os.path.join(ROOT, "include", "compat"), os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "oracle", "gslshim"), os.path.join(ref, "src", "NBody"),
+           os.path.join(ref, "src", "Math"), os.path.join(ref, "src", "Analysis")]
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", *sum((["-I", d] for d in inc), []),
+           "-c", src, "-o", str(tmp_path / "density.o")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+
+
 def test_compiles_against_the_standin(lib_built, tmp_path):
     compile_demo(str(tmp_path / "demo"), [os.path.join(HERE, "cxx")])
 
@@ -76,6 +93,7 @@ def test_dropin_runs_like_the_reference(gpu, port_built, tmp_path, periodic):
     smvel = take(np.float64, 3 * n).reshape(n, 3)
     ngroup_nn = take(np.int32, 1)[0]
     group_nn = take(np.int32, n)
+    rho_smooth = take(np.float64, n)
     per = [box] * 3 if periodic else None
     o = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, per, backend="port")
     assert nodes == o.num_nodes and leaves == o.num_leaves
@@ -99,3 +117,6 @@ def test_dropin_runs_like_the_reference(gpu, port_built, tmp_path, periodic):
                                 backend="port").fof_nn(0, [0, 0, 0, 0, 0, 0, 0.35, 0], pn, 5)
     assert ngroup_nn == ngp
     assert_same_partition(group_nn, gp, "drop-in FOFNNCriterion")
+    # DensitySmooth(S, 16, 32): System constructor (default Epanechnikov kernel, no period)
+    rs = oracle.OracleTree(pos, vel, mass, 16, 0, 2, 1000, None, backend="port").density(32)
+    assert_density_close(rho_smooth, rs, "drop-in DensitySmooth")
