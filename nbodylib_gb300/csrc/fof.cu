@@ -188,6 +188,10 @@ __global__ void __launch_bounds__(32 * kWpb, 4) k_link(FofArgs a) {
       while (todo) {
         int j = __ffs(todo) - 1;
         todo &= todo - 1;
+        int rootj = __shfl_sync(FULL, root, j);
+        // a compact node already in every active lane's component adds nothing: skipped
+        // before its box is broadcast
+        if (rootj >= 0 && __all_sync(FULL, rootj == myroot || !active)) continue;
         NodeRec rj;
 #pragma unroll
         for (int d = 0; d < 3; d++) {
@@ -196,7 +200,6 @@ __global__ void __launch_bounds__(32 * kWpb, 4) k_link(FofArgs a) {
         }
         rj.start = __shfl_sync(FULL, r.start, j);
         rj.count = __shfl_sync(FULL, r.count, j);
-        int rootj = __shfl_sync(FULL, root, j);
         bool need = active && box_d2_lo(qx, qy, qz, eps, rj) < thr;
         if (need && rootj >= 0) {
           // a compact node was prelinked: all its particles share one root. If that root
