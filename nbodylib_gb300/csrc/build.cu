@@ -50,12 +50,11 @@ struct GNode {
   unsigned long long kmin[3], kmax[3];  // node box as order keys (filled by the level above)
 };
 
-// Radix digits of the median selection, most significant first: 11+11+11+11+11+9 bits.
+// Radix passes of the median selection (11-bit digits from each node's highest differing
+// key bit: at most six cover a 64-bit key).
 constexpr int kPasses = 6;
 constexpr int kBins = 2048;
 constexpr int kCollect = kThreads;  // a class this small is gathered and ranked by one block
-__device__ __constant__ static const int kDigitShift[kPasses] = {53, 42, 31, 20, 9, 0};
-__device__ __constant__ static const int kDigitWidth[kPasses] = {11, 11, 11, 11, 11, 9};
 
 struct Chunk {
   int g;      // gnode index within the level
@@ -227,9 +226,14 @@ __global__ void __launch_bounds__(kThreads) k_radix(const Chunk* __restrict__ ch
     dim = s.dim;
     first_diff = s.first_diff;
   }
-  const int shift = kDigitShift[pass], width = kDigitWidth[pass];
-  const unsigned long long dmask = ((1ull << width) - 1ull) << shift;
-  const bool skip = first_diff < shift;  // every key of the node shares this digit
+  // digits start at the node's highest differing key bit: pass p resolves the 11 bits
+  // below first_diff - 11p (fewer for the last one); the bits above first_diff are common
+  // to every key of the node and enter the prefix in pass 0
+  const int hi_bit = first_diff - 11 * pass;
+  const bool skip = hi_bit < 0;  // no bit left: every key of the node is equal
+  const int width = skip ? 1 : min(11, hi_bit + 1), shift = skip ? 0 : hi_bit - width + 1;
+  const unsigned long long dmask = skip ? 0ull : ((1ull << width) - 1ull) << shift;
+  const unsigned long long common = hi_bit >= 63 ? 0ull : (~0ull << (hi_bit + 1));
   const bool collect = !skip && s.ncand <= kCollect;
   if (collect) {
     // gather the class's keys into this node's slice of the candidate buffer
@@ -301,13 +305,17 @@ __global__ void __launch_bounds__(kThreads) k_radix(const Chunk* __restrict__ ch
       write_node(node, nodex, s.node, lo, hi, p0 + s.start, s.size, dim, 0.0);
     }
   }
-  if (skip) {
+  const unsigned long long kmin_dim = sel3(kmin_d[0], kmin_d[1], kmin_d[2], dim);
+  if (skip) {  // all keys equal (first_diff = -1): the median key is the minimum key
     if (threadIdx.x == 0) {
-      g[c.g].prefix = s.prefix | (sel3(kmin_d[0], kmin_d[1], kmin_d[2], dim) & dmask);
-      g[c.g].mask = s.mask | dmask;
+      g[c.g].prefix = kmin_dim;
+      g[c.g].mask = ~0ull;
     }
     return;
   }
+  // pass 0 adds the bits every key shares
+  const unsigned long long base_prefix = pass == 0 ? (kmin_dim & common) : s.prefix;
+  const unsigned long long base_mask = pass == 0 ? common : s.mask;
   if (collect) {
     // the k-th smallest of the gathered keys is the median key: thread t holds key t and
     // counts the keys below it and equal to it
@@ -357,8 +365,8 @@ __global__ void __launch_bounds__(kThreads) k_radix(const Chunk* __restrict__ ch
 #pragma unroll
     for (int e = 0; e < kPer; e++)
       if (threadIdx.x * kPer + e == digit) g[c.g].ncand = (int)cnt[e];
-    g[c.g].prefix = s.prefix | ((unsigned long long)digit << shift);
-    g[c.g].mask = s.mask | dmask;
+    g[c.g].prefix = base_prefix | ((unsigned long long)digit << shift);
+    g[c.g].mask = base_mask | dmask;
   }
 #pragma unroll
   for (int e = 0; e < kPer; e++) hh[threadIdx.x * kPer + e] = 0u;
