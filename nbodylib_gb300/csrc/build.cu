@@ -909,6 +909,30 @@ size_t local_build_smem() {
          sizeof(LNode) * 2 * kLevelCap;
 }
 
+// One growing page-locked buffer per host thread for the build plans.
+struct PinnedStage {
+  unsigned char* p = nullptr;
+  size_t cap = 0, used = 0;
+  unsigned char* data() { return p; }
+  size_t size() const { return used; }
+  ~PinnedStage() {
+    if (p) cudaFreeHost(p);
+  }
+};
+PinnedStage& pinned_stage(size_t bytes) {
+  static thread_local PinnedStage st;
+  if (bytes > st.cap) {
+    if (st.p) cudaFreeHost(st.p);
+    st.p = nullptr;
+    st.cap = 0;
+    size_t cap = std::max<size_t>(bytes, 1 << 20);
+    if (cudaMallocHost((void**)&st.p, cap) == cudaSuccess) st.cap = cap;
+    else st.p = nullptr;
+  }
+  st.used = bytes;
+  return st;
+}
+
 int64_t heap_slots(int64_t n, int b) {
   int d = depth_of(n, b);
   return (int64_t(1) << (d + 1)) - 1;
@@ -1017,13 +1041,24 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
   // one upload: [GNode...][Chunk...][LRoot...]
   size_t bg = sizeof(GNode) * gn.size(), bc = sizeof(Chunk) * ch.size(),
          br = sizeof(LRoot) * lroots.size();
-  std::vector<unsigned char> plan(bg + bc + br + 16);
+  // staged in page-locked memory so the upload is a plain asynchronous copy (the build's
+  // final synchronisation orders it before the buffer is reused by this thread)
+  PinnedStage& plan = pinned_stage(bg + bc + br + 16);
+  if (!plan.data()) {
+    set_error("tree build: page-locked staging allocation failed");
+    return NBK_ERR_NOMEM;
+  }
   memcpy(plan.data(), gn.data(), bg);
   memcpy(plan.data() + bg, ch.data(), bc);
   memcpy(plan.data() + bg + bc, lroots.data(), br);
   unsigned char* d_plan;
   NBK_TRY(alloc.get((void**)&d_plan, plan.size()));
   NBK_CUDA_TRY(cudaMemcpyAsync(d_plan, plan.data(), plan.size(), cudaMemcpyHostToDevice, st));
+  // every way out of here waits for the stream, so the staging buffer is free again
+  struct WaitOnExit {
+    cudaStream_t st;
+    ~WaitOnExit() { cudaStreamSynchronize(st); }
+  } wait_on_exit{st};
   GNode* d_gall = (GNode*)d_plan;
   Chunk* d_call = (Chunk*)(d_plan + bg);
   LRoot* d_r = (LRoot*)(d_plan + bg + bc);

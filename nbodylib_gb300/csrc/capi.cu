@@ -8,6 +8,7 @@
 #include <memory>
 #include <mutex>
 #include <stdexcept>
+#include <tuple>
 
 #include "nbk_build.h"
 
@@ -71,6 +72,35 @@ void kernel_table(int kerntype, int kernres, int nd, std::vector<double>& T, dou
   double delta = 2.0 / (double)(kernres - 1);
   T.resize(kernres);
   for (int i = 0; i < kernres; i++) T[i] = kn * f(i * delta, 1.0);
+}
+
+// Device kernel tables are shared by every tree of one (device, kernel, resolution): built
+// and uploaded once per process, never freed (a few tens of KB each).
+struct KernelEntry {
+  std::vector<double> table;
+  double norm = 0;
+  double* d_img = nullptr;
+};
+static int cached_kernel(int kerntype, int kernres, const KernelEntry** out) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int>, KernelEntry> cache;
+  int dev = 0;
+  NBK_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  auto key = std::make_tuple(dev, kerntype, kernres);
+  auto it = cache.find(key);
+  if (it == cache.end()) {
+    KernelEntry e;
+    kernel_table(kerntype, kernres, 3, e.table, e.norm);
+    std::vector<double> img;
+    kernel_device_image(e.table, img);
+    NBK_CUDA_TRY(cudaMalloc((void**)&e.d_img, sizeof(double) * img.size()));
+    NBK_CUDA_TRY(cudaMemcpy(e.d_img, img.data(), sizeof(double) * img.size(),
+                            cudaMemcpyHostToDevice));
+    it = cache.emplace(key, std::move(e)).first;
+  }
+  *out = &it->second;
+  return NBK_OK;
 }
 
 // Device image of a kernel table: [T | A | B] with W(q) = A[i] + B[i] q on cell i, the
@@ -212,7 +242,6 @@ struct nbk_tree {
   BuiltArrays arr;
   int64_t nslots = 0, numnodes = 0, numleaves = 0;
   std::vector<double> h_kernel;
-  std::vector<double> h_kernel_img;  // device image [T | A | B] of the kernel table
   double kernnorm = 0;
   double* d_kernel = nullptr;
   float eps = 0;
@@ -471,11 +500,13 @@ int nbk_create(const double* pos, const double* vel, const double* mass, int64_t
   }
   t->has_vel = vel != nullptr;
   cudaStream_t st = t->st;
-  kernel_table(t->kerntype, t->kernres, 3, t->h_kernel, t->kernnorm);
-  kernel_device_image(t->h_kernel, t->h_kernel_img);
-  NBK_TRY(dev_malloc((void**)&t->d_kernel, sizeof(double) * t->h_kernel_img.size(), st));
-  NBK_CUDA_TRY(cudaMemcpyAsync(t->d_kernel, t->h_kernel_img.data(),
-                               sizeof(double) * t->h_kernel_img.size(), cudaMemcpyHostToDevice, st));
+  {
+    const KernelEntry* ke;
+    NBK_TRY(cached_kernel(t->kerntype, t->kernres, &ke));
+    t->h_kernel = ke->table;
+    t->kernnorm = ke->norm;
+    t->d_kernel = ke->d_img;  // shared, not owned by the tree
+  }
   NBK_TRY(dev_malloc((void**)&t->d_err, sizeof(int), st));
   NBK_CUDA_TRY(cudaMemsetAsync(t->d_err, 0, sizeof(int), st));
   t->nslots = heap_slots(n, bucket_size);
@@ -539,7 +570,7 @@ int nbk_destroy(nbk_tree* t) {
   dev_free(t->arr.perm, st);
   dev_free(t->arr.node, st);
   dev_free(t->arr.nodex, st);
-  dev_free(t->d_kernel, st);
+  // t->d_kernel belongs to the process-wide kernel cache
   dev_free(t->d_err, st);
   cudaStreamSynchronize(st);
   delete t;
