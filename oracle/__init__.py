@@ -83,6 +83,9 @@ def _lib(backend: str) -> ctypes.CDLL:
                                       _c_dbl_p, _c_dbl_p, _c_dbl_p, ctypes.c_double, _c_dbl_p]),
     }
     if backend == "port":
+        sig["set_aniso"] = (None, [vp, ctypes.c_int])
+        sig["knn_coord"] = (ctypes.c_int, [vp, _c_dbl_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           _c_int_p, _c_dbl_p])
         sig["knn_pos"] = (ctypes.c_int, [vp, _c_dbl_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          _c_int_p, _c_dbl_p])
         sig["density"] = (ctypes.c_int, [vp, ctypes.c_int, _c_dbl_p, _c_int_p])
@@ -95,6 +98,9 @@ def _lib(backend: str) -> ctypes.CDLL:
         sig["adj_fd"] = (ctypes.c_double, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_double])
         sig["adj_destroy"] = (None, [vp])
     else:
+        sig["create_ex"] = (vp, sig["create"][1] + [ctypes.c_int])
+        sig["knn_coord"] = (ctypes.c_int, [vp, _c_dbl_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           _c_int_p, _c_dbl_p])
         sig["knn_pos"] = (ctypes.c_int, [vp, _c_dbl_p, ctypes.c_int, ctypes.c_int, _c_int_p,
                                          _c_dbl_p])
         sig["density"] = (ctypes.c_int, [vp, ctypes.c_int, _c_dbl_p])
@@ -118,7 +124,7 @@ class OracleTree:
     """A CPU kd-tree built by the reference (``ref``) or by the restatement (``port``)."""
 
     def __init__(self, pos, vel=None, mass=None, bucket_size=16, treetype=0, kerntype=0,
-                 kernres=1000, period=None, backend="port", nthreads=0):
+                 kernres=1000, period=None, backend="port", nthreads=0, aniso=0):
         self.backend = backend
         self._lib = _lib(backend)
         self._f = lambda name: getattr(self._lib, ("pt_" if backend == "port" else "ref_") + name)
@@ -130,8 +136,15 @@ class OracleTree:
         per = None if period is None else np.ascontiguousarray(
             np.broadcast_to(np.asarray(period, dtype=np.float64), (3,)))
         self._per = per
-        self._h = self._f("create")(_dp(self.pos), _dp(self.vel), _dp(self.mass), self.n,
-                                    bucket_size, treetype, kerntype, kernres, _dp(per), nthreads)
+        args = (_dp(self.pos), _dp(self.vel), _dp(self.mass), self.n, bucket_size, treetype,
+                kerntype, kernres, _dp(per), nthreads)
+        if backend == "port":
+            self._h = self._f("create")(*args)
+            self._f("set_aniso")(self._h, aniso)
+        else:
+            self._h = self._f("create_ex")(*args, aniso)
+        self.treetype = treetype
+        self.nd = 6 if treetype == 3 else 3
         self.nthreads = nthreads
 
     def close(self):
@@ -180,7 +193,23 @@ class OracleTree:
         """method 0: FindNearest(tt); 1: FindNearestPos(tt). Rows by ID, neighbours as IDs."""
         nn = np.empty((self.n, k), np.int32)
         d2 = np.empty((self.n, k), np.float64)
-        self._f("knn")(self._h, method, k, self.nthreads, _ip(nn), _dp(d2))
+        st = self._f("knn")(self._h, method, k, self.nthreads, _ip(nn), _dp(d2))
+        if st:
+            raise RuntimeError(f"FindNearest: status {st}")
+        return nn, d2
+
+    def knn_coord(self, x, k):
+        """FindNearest(Double_t* x): x rows in the tree's space (3, or 6 for phase space)."""
+        x = np.ascontiguousarray(x, np.float64).reshape(-1, self.nd)
+        nn = np.empty((x.shape[0], k), np.int32)
+        d2 = np.empty((x.shape[0], k), np.float64)
+        if self.backend == "port":
+            st = self._f("knn_coord")(self._h, _dp(x), x.shape[0], k, self.nthreads, _ip(nn),
+                                      _dp(d2))
+        else:
+            st = self._f("knn_coord")(self._h, _dp(x), x.shape[0], self.nd, k, _ip(nn), _dp(d2))
+        if st:
+            raise RuntimeError(f"FindNearest(x): status {st}")
         return nn, d2
 
     def knn_pos(self, x, k):
@@ -199,7 +228,7 @@ class OracleTree:
             nn = np.empty((self.n, k), np.int32) if return_nn else None
             st = self._f("density")(self._h, k, _dp(rho), _ip(nn))
             if st:
-                raise RuntimeError("CalcDensity: fewer than k neighbours")
+                raise RuntimeError(f"CalcDensity: status {st}")
             return (rho, nn) if return_nn else rho
         self._f("density")(self._h, k, _dp(rho))
         return rho

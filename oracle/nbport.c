@@ -43,6 +43,7 @@ typedef struct {
 
 struct PTree {
     int n, b, treetype, nd, kerntype, kernres;
+    int aniso; /* the reference's `anisotropic` flag: -1 plain phase metric, 0 local metric */
     PPart* p;
     PNode* nodes;
     int numnodes, numleaves;
@@ -339,6 +340,7 @@ void pt_destroy(PTree* t) {
     free(t->tree_of_id);
     free(t);
 }
+void pt_set_aniso(PTree* t, int aniso) { t->aniso = aniso; }
 int pt_num_nodes(const PTree* t) { return t->numnodes; }
 int pt_num_leaves(const PTree* t) { return t->numleaves; }
 double pt_kernnorm(const PTree* t) { return t->kernnorm; }
@@ -487,6 +489,120 @@ static void knn_periodic(const PTree* t, PQ* pq, const double* x) {
     }
 }
 
+/* MetricDistSqd (DistFunc.h:58-65): over the six phase coordinates, total += metric[i]*d*d
+   from 0 in dimension order. */
+static inline double metric_dist2(const double* a, const double* b, const double* metric) {
+    double total = 0;
+    for (int i = 0; i < 6; i++) total += metric[i] * (a[i] - b[i]) * (a[i] - b[i]);
+    return total;
+}
+
+/* SplitNode::FindNearestMetric (KDSplitNode.cxx:96-121 target form, 303-331 coordinate
+   form) and LeafNode::FindNearestMetric (KDLeafNode.cxx:58-71, 168-179). The leaves test
+   the metric distance while the pruning test compares the unscaled incremental offset rd
+   with the heap top, so the search is not exact and its result depends on the traversal
+   order, which this restatement keeps. target < 0: the coordinate form. Both forms skip
+   distance 0; the target form also skips the target. */
+static void knn_metric(const PTree* t, int node, double rd, PQ* pq, double* off, int target,
+                       const double* x, const double* metric) {
+    const PNode* nd = &t->nodes[node];
+    if (nd->left < 0) {
+        double xi[6];
+        for (int i = nd->start; i < nd->end; i++) {
+            if (i == target) continue;
+            tvec(t, &t->p[i], xi);
+            double d2 = metric_dist2(x, xi, metric);
+            if (d2 < pq_top(pq) && d2 > 0) {
+                pq_pop(pq);
+                pq_push(pq, i, d2);
+            }
+        }
+        return;
+    }
+    int cd = nd->cut_dim;
+    double old_off = off[cd];
+    double new_off = x[cd] - nd->cut_val;
+    if (new_off < 0) {
+        knn_metric(t, nd->left, rd, pq, off, target, x, metric);
+        rd += -old_off * old_off + new_off * new_off;
+        if (rd < pq_top(pq)) {
+            off[cd] = new_off;
+            knn_metric(t, nd->right, rd, pq, off, target, x, metric);
+            off[cd] = old_off;
+        }
+    } else {
+        knn_metric(t, nd->right, rd, pq, off, target, x, metric);
+        rd += -old_off * old_off + new_off * new_off;
+        if (rd < pq_top(pq)) {
+            off[cd] = new_off;
+            knn_metric(t, nd->left, rd, pq, off, target, x, metric);
+            off[cd] = old_off;
+        }
+    }
+}
+
+static void phase_periodic(const PTree* t, PQ* pq, const double* x, const double* metric);
+
+/* KDTree::CalculateMetricSpacing: the 8 nearest in plain phase space around x (coordinate
+   search: a particle at x itself is included), popped into ID[7..0]; the six direct
+   offsets to ID[1] (or to the next one if their product is 0) give metric[j] =
+   1/sr0[j]^2. The reference defines this inline function twice: the copy in
+   KDCalcSmoothQuantities.cxx:17-56, which the density functions use, always searches
+   without images; the copy in KDFindNearest.cxx:34-105, which FindNearest uses, searches
+   the periodic images of a periodic tree (FindNearestPhasePeriodic). `periodic` selects
+   the latter. Returns 6 when fewer than 8 particles exist (the reference exits). */
+static int metric_spacing(const PTree* t, const double* x, double* metric, int periodic) {
+    PQ pq;
+    pq_init(&pq, 8);
+    for (int i = 0; i < 8; i++) pq_push(&pq, -1, MAXVALUE);
+    double off[6] = {0, 0, 0, 0, 0, 0};
+    if (periodic) phase_periodic(t, &pq, x, NULL);
+    else knn_coord(t, 0, 0.0, &pq, off, x);
+    int id[8];
+    for (int i = 7; i >= 0; i--) {
+        id[i] = pq_topq(&pq);
+        if (id[i] == -1) {
+            pq_free(&pq);
+            return 6;
+        }
+        pq_pop(&pq);
+    }
+    pq_free(&pq);
+    double kvol = 0.0, sr0[6] = {0, 0, 0, 0, 0, 0};
+    int ivol = 1;
+    while (kvol == 0.0 && ivol < 8) {
+        kvol = 1.0;
+        for (int j = 0; j < 6; j++) {
+            const PPart* a = &t->p[id[ivol]];
+            sr0[j] = fabs((j < 3 ? a->pos[j] : a->vel[j - 3]) - x[j]);
+            kvol *= sr0[j];
+        }
+        ivol++;
+    }
+    for (int j = 0; j < 6; j++) metric[j] = 1.0 / (sr0[j] * sr0[j]);
+    return 0;
+}
+
+/* SplitNode::FindNearestPhasePeriodic / FindNearestMetricPeriodic (KDSplitNode.cxx:
+   1153-1186, 1193-1218): the coordinate search around x (position and velocity), then the
+   seven position images x, y, z, xy, xz, yz, xyz with no gate, the offsets reset before
+   each. metric == NULL: plain phase distance. A root that is a leaf searches x alone
+   (KDLeafNode.cxx:666-679, 708-711, 725-728). */
+static void phase_periodic(const PTree* t, PQ* pq, const double* x, const double* metric) {
+    double off[6] = {0, 0, 0, 0, 0, 0};
+    if (metric) knn_metric(t, 0, 0.0, pq, off, -1, x, metric);
+    else knn_coord(t, 0, 0.0, pq, off, x);
+    if (t->nodes[0].left < 0) return;
+    for (int m = 0; m < 7; m++) {
+        double xp[6];
+        for (int j = 0; j < 6; j++) off[j] = 0.0;
+        reflect(x, xp, t->period, kImageMask[m]);
+        for (int j = 3; j < 6; j++) xp[j] = x[j];
+        if (metric) knn_metric(t, 0, 0.0, pq, off, -1, xp, metric);
+        else knn_coord(t, 0, 0.0, pq, off, xp);
+    }
+}
+
 /* LoadNN (KDFindNearest.cxx:11-24): pop the ns largest into nn[ns-1..0]. */
 static void load_nn(const PTree* t, int ns, PQ* pq, int* nn, double* d) {
     for (int i = ns - 1; i >= 0; i--) {
@@ -497,31 +613,57 @@ static void load_nn(const PTree* t, int ns, PQ* pq, int* nn, double* d) {
     }
 }
 
-/* KDTree::FindNearest(tt) / FindNearestPos(tt) for a physical tree
-   (KDFindNearest.cxx:247-334). method 0: FindNearest, 1: FindNearestPos. A root that is
-   a leaf dispatches the periodic call to the non-periodic target search
-   (KDLeafNode.cxx:658-661). */
-static void find_nearest_one(const PTree* t, int method, int tt, int k, PQ* pq, int* nn, double* d) {
+/* The search KDTree::FindNearest(tt) runs for the tree's type (KDFindNearest.cxx:
+   255-310): physical trees the target search or the gated periodic one; velocity trees
+   the target search even when periodic; phase-space trees the plain phase search
+   (anisotropic -1) or the local-metric search (0), each with its ungated periodic form.
+   xt: the target's tree coordinates. Returns 6 when the metric spacing fails. */
+static int search_target(const PTree* t, PQ* pq, int tt, const double* xt) {
+    double off[6] = {0, 0, 0, 0, 0, 0};
+    int per = t->periodic;
+    if (t->treetype == TPHS) {
+        if (t->aniso == -1) {
+            if (!per) knn_target(t, 0, 0.0, pq, off, tt, xt);
+            else phase_periodic(t, pq, xt, NULL);
+        } else {
+            double m[6];
+            if (metric_spacing(t, xt, m, per)) return 6;
+            if (!per) knn_metric(t, 0, 0.0, pq, off, tt, xt, m);
+            else phase_periodic(t, pq, xt, m);
+        }
+        return 0;
+    }
+    int root_leaf = t->nodes[0].left < 0;
+    if (!per || root_leaf || t->treetype == TVEL) knn_target(t, 0, 0.0, pq, off, tt, xt);
+    else knn_periodic(t, pq, xt);
+    return 0;
+}
+
+/* KDTree::FindNearest(tt) / FindNearestPos(tt) (KDFindNearest.cxx:247-334). method 0:
+   FindNearest, 1: FindNearestPos (physical trees only). A periodic tree searches for k+1
+   (any tree type, :250) and then loads k: FindNearest drops the nearest entry,
+   FindNearestPos pops the farthest first (:331). */
+static int find_nearest_one(const PTree* t, int method, int tt, int k, PQ* pq, int* nn, double* d) {
     int ns = k;
-    int per = t->periodic && t->treetype != TVEL;
+    int per = t->periodic;
     if (per) ns += 1;
     pq->n = 0;
     for (int i = 0; i < ns; i++) pq_push(pq, -1, MAXVALUE);
-    double off[6] = {0, 0, 0, 0, 0, 0};
     double xt[6] = {0, 0, 0, 0, 0, 0};
     tvec(t, &t->p[tt], xt);
-    int root_leaf = t->nodes[0].left < 0;
-    if (!per || root_leaf) knn_target(t, 0, 0.0, pq, off, tt, xt);
-    else knn_periodic(t, pq, xt);
+    int st = search_target(t, pq, tt, xt);
     if (per) {
         if (method == 1) pq_pop(pq);
         ns -= 1;
     }
     load_nn(t, ns, pq, nn, d);
+    return st;
 }
 
 int pt_knn(PTree* t, int method, int k, int nthreads, int* nn_ids, double* d2) {
     int n = t->n;
+    if (method == 1 && t->treetype != TPHYS) return 7;
+    int status = 0;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #pragma omp parallel
@@ -534,11 +676,13 @@ int pt_knn(PTree* t, int method, int k, int nthreads, int* nn_ids, double* d2) {
 #endif
         for (int id = 0; id < n; id++) {
             int tt = t->tree_of_id[id];
-            find_nearest_one(t, method, tt, k, &pq, nn_ids + (size_t)id * k, d2 + (size_t)id * k);
+            if (find_nearest_one(t, method, tt, k, &pq, nn_ids + (size_t)id * k,
+                                 d2 + (size_t)id * k))
+                status = 6;
         }
         pq_free(&pq);
     }
-    return 0;
+    return status;
 }
 
 /* KDTree::FindNearestPos(Double_t *x) (KDFindNearest.cxx:509-520). */
@@ -567,10 +711,84 @@ int pt_knn_pos(PTree* t, const double* x, int nq, int k, int nthreads, int* nn_i
     return 0;
 }
 
+/* KDTree::FindNearest(Double_t *x) (KDFindNearest.cxx:460-507): x holds the tree's
+   coordinates (3 positions, 3 velocities, or 6 phase coordinates per row); nothing is
+   excluded except, in the local-metric search, distance 0. Periodic velocity trees are
+   not restated (returns 7). */
+int pt_knn_coord(PTree* t, const double* x, int nq, int k, int nthreads, int* nn_ids, double* d2) {
+    if (t->periodic && t->treetype == TVEL) return 7;
+    int nd = t->nd, status = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel
+#endif
+    {
+        PQ pq;
+        pq_init(&pq, k);
+#ifdef _OPENMP
+#pragma omp for schedule(guided)
+#endif
+        for (int q = 0; q < nq; q++) {
+            pq.n = 0;
+            for (int i = 0; i < k; i++) pq_push(&pq, -1, MAXVALUE);
+            double off[6] = {0, 0, 0, 0, 0, 0};
+            const double* xq = x + (size_t)nd * q;
+            if (t->treetype == TPHS) {
+                double m[6];
+                if (t->aniso == -1) {
+                    if (!t->periodic) knn_coord(t, 0, 0.0, &pq, off, xq);
+                    else phase_periodic(t, &pq, xq, NULL);
+                } else if (metric_spacing(t, xq, m, t->periodic)) {
+                    status = 6;
+                } else if (!t->periodic) {
+                    knn_metric(t, 0, 0.0, &pq, off, -1, xq, m);
+                } else {
+                    phase_periodic(t, &pq, xq, m);
+                }
+            } else if (!t->periodic || t->nodes[0].left < 0) {
+                knn_coord(t, 0, 0.0, &pq, off, xq);
+            } else {
+                knn_periodic(t, &pq, xq);
+            }
+            load_nn(t, k, &pq, nn_ids + (size_t)q * k, d2 + (size_t)q * k);
+        }
+        pq_free(&pq);
+    }
+    return status;
+}
+
+/* The neighbour search of CalcDensity / CalcDensityParticle for the tree's type
+   (KDCalcSmoothQuantities.cxx:227-263, 782-816): always non-periodic. For a phase-space
+   tree with the local metric, *scale receives the product of sqrt(metric[j]) that
+   multiplies the normalisation (:265-270); otherwise 1. Returns 7 for a phase-space tree
+   without the local metric (the reference multiplies uninitialised metric arrays there),
+   6 when the metric spacing fails. */
+static int density_search(const PTree* t, PQ* pq, int i, double* scale) {
+    double off[6] = {0, 0, 0, 0, 0, 0};
+    double xt[6] = {0, 0, 0, 0, 0, 0};
+    tvec(t, &t->p[i], xt);
+    *scale = 1.0;
+    if (t->treetype != TPHS) {
+        knn_target(t, 0, 0.0, pq, off, i, xt);
+        return 0;
+    }
+    if (t->aniso != 0) return 7;
+    double m[6];
+    if (metric_spacing(t, xt, m, 0)) return 6;
+    knn_metric(t, 0, 0.0, pq, off, i, xt, m);
+    double temp = 1.0;
+    for (int j = 0; j < 6; j++) m[j] = sqrt(m[j]);
+    for (int j = 0; j < 6; j++) temp *= m[j];
+    *scale = temp;
+    return 0;
+}
+
 /* ---------------------------------------------------------------- SPH density */
-/* KDTree::CalcDensity (KDCalcSmoothQuantities.cxx:203-305), physical tree: non-periodic
-   target search for every particle in tree order; h = 0.5 sqrt(top); symmetric scatter.
-   Returns 6 when a neighbour slot stays empty (the reference calls exit(1), :273-276). */
+/* KDTree::CalcDensity (KDCalcSmoothQuantities.cxx:203-305): non-periodic target search
+   (density_search) for every particle in tree order; h = 0.5 sqrt(top), norm = h^-ND
+   (times the metric factor of a phase-space tree); symmetric scatter. Returns 6 when a
+   neighbour slot stays empty (the reference calls exit(1), :273-276), 7 for a phase-space
+   tree without the local metric. */
 int pt_density(PTree* t, int k, double* rho, int* nn_ids) {
     int n = t->n;
     for (int i = 0; i < n; i++) t->p[i].rho = 0;
@@ -582,12 +800,12 @@ int pt_density(PTree* t, int k, double* rho, int* nn_ids) {
     for (int i = 0; i < n && !status; i++) {
         pq.n = 0;
         for (int j = 0; j < k; j++) pq_push(&pq, -1, MAXVALUE);
-        double off[6] = {0, 0, 0, 0, 0, 0};
-        double xt[6] = {0, 0, 0, 0, 0, 0};
-        tvec(t, &t->p[i], xt);
-        knn_target(t, 0, 0.0, &pq, off, i, xt);
+        double scale;
+        status = density_search(t, &pq, i, &scale);
+        if (status) break;
         double hi = 0.5 * sqrt(pq_top(&pq));
         double norm = 1.0 / pow(hi, (double)(nd * 1.));
+        if (t->treetype == TPHS) norm *= scale;
         for (int j = 0; j < k; j++) {
             if (pq_topq(&pq) == -1) {
                 status = 6;
@@ -676,13 +894,15 @@ double pt_density_particle(PTree* t, int id, int k) {
     PQ pq;
     pq_init(&pq, k);
     for (int j = 0; j < k; j++) pq_push(&pq, -1, MAXVALUE);
-    double off[6] = {0, 0, 0, 0, 0, 0};
-    double xt[6] = {0, 0, 0, 0, 0, 0};
-    tvec(t, &t->p[i], xt);
-    knn_target(t, 0, 0.0, &pq, off, i, xt);
+    double scale;
+    if (density_search(t, &pq, i, &scale)) {
+        pq_free(&pq);
+        return NAN;
+    }
     double delta = 2.0 / (double)(t->kernres - 1);
     double hi = 0.5 * sqrt(pq_top(&pq));
     double norm = 1.0 / pow(hi, (double)(t->nd * 1.));
+    if (t->treetype == TPHS) norm *= scale;
     double den = 0.;
     for (int j = 0; j < k; j++) {
         if (pq_topq(&pq) == -1) {

@@ -21,6 +21,10 @@ typedef struct PTree PTree;
 PTree* pt_create(const double* pos, const double* vel, const double* mass, int n, int b,
                  int treetype, int kerntype, int kernres, const double* period, int nthreads);
 void pt_destroy(PTree* t);
+/* The reference's Aniso constructor argument for phase-space trees: -1 plain phase-space
+   distance (FindNearestPhase), 0 local metric (CalculateMetricSpacing + FindNearestMetric,
+   the reference's default). */
+void pt_set_aniso(PTree* t, int aniso);
 int pt_num_nodes(const PTree* t);
 int pt_num_leaves(const PTree* t);
 double pt_kernnorm(const PTree* t);
@@ -29,10 +33,13 @@ void pt_ids(const PTree* t, int* ids);
 void pt_leaf_start(const PTree* t, int* leaf_start);
 double pt_build_seconds(const PTree* t);
 
-/* method 0: FindNearest(tt), 1: FindNearestPos(tt). Row i belongs to the particle with ID i. */
+/* method 0: FindNearest(tt), 1: FindNearestPos(tt) (physical trees). Row i belongs to the
+   particle with ID i. Returns 6 when a phase-space metric spacing fails, 7 if unsupported. */
 int pt_knn(PTree* t, int method, int k, int nthreads, int* nn_ids, double* d2);
 /* FindNearestPos(x) for nq coordinates. */
 int pt_knn_pos(PTree* t, const double* x, int nq, int k, int nthreads, int* nn_ids, double* d2);
+/* FindNearest(x) for nq coordinates of the tree's space (3 or 6 per row). */
+int pt_knn_coord(PTree* t, const double* x, int nq, int k, int nthreads, int* nn_ids, double* d2);
 /* CalcDensity(k) (KDCalcSmoothQuantities.cxx:203-305). rho in ID order. If nn_ids is not
    NULL it receives the k neighbours of each particle (ID rows, descending d2 as the heap
    pops them) so that tests can freeze them for the adjoint. */

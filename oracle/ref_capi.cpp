@@ -43,8 +43,20 @@ void refresh_index(RefTree* r) {
 
 extern "C" {
 
+/* The constructor with its Aniso argument (KDTree.h:229-245): -1 plain phase-space
+   distance, 0 local metric (the default) for phase-space trees. */
+void* ref_create_ex(const double* pos, const double* vel, const double* mass, int n, int b,
+                    int treetype, int kerntype, int kernres, const double* period, int nthreads,
+                    int aniso);
+
 void* ref_create(const double* pos, const double* vel, const double* mass, int n, int b,
                  int treetype, int kerntype, int kernres, const double* period, int nthreads) {
+    return ref_create_ex(pos, vel, mass, n, b, treetype, kerntype, kernres, period, nthreads, 0);
+}
+
+void* ref_create_ex(const double* pos, const double* vel, const double* mass, int n, int b,
+                    int treetype, int kerntype, int kernres, const double* period, int nthreads,
+                    int aniso) {
 #ifdef USEOPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
@@ -69,7 +81,7 @@ void* ref_create(const double* pos, const double* vel, const double* mass, int n
         for (int k = 0; k < 3; k++) r->period[k] = period[k];
     }
     auto t0 = std::chrono::steady_clock::now();
-    r->tree = new KDTree(r->parts.data(), n, b, treetype, kerntype, kernres, 0, 0, 0, pp);
+    r->tree = new KDTree(r->parts.data(), n, b, treetype, kerntype, kernres, 0, aniso, 0, pp);
     auto t1 = std::chrono::steady_clock::now();
     r->build_seconds = std::chrono::duration<double>(t1 - t0).count();
     refresh_index(r);
@@ -142,6 +154,24 @@ int ref_knn_pos(void* h, const double* x, int nq, int k, int* nn_ids, double* d2
     for (int q = 0; q < nq; q++) {
         double xx[3] = {x[3 * q], x[3 * q + 1], x[3 * q + 2]};
         r->tree->FindNearestPos(xx, nn.data(), dd.data(), k);
+        for (int j = 0; j < k; j++) {
+            nn_ids[(size_t)q * k + j] = nn[j] >= 0 ? r->parts[nn[j]].GetID() : -1;
+            d2[(size_t)q * k + j] = dd[j];
+        }
+    }
+    return 0;
+}
+
+/* FindNearest(Double_t* x) (KDFindNearest.cxx:460-507) for nq coordinates of the tree's
+   space: nd = 3 (positions, or velocities for a velocity tree) or 6 (phase space). */
+int ref_knn_coord(void* h, const double* x, int nq, int nd, int k, int* nn_ids, double* d2) {
+    RefTree* r = (RefTree*)h;
+    std::vector<int> nn(k);
+    std::vector<double> dd(k);
+    for (int q = 0; q < nq; q++) {
+        double xx[6];
+        for (int j = 0; j < nd; j++) xx[j] = x[(size_t)nd * q + j];
+        r->tree->FindNearest(xx, nn.data(), dd.data(), k);
         for (int j = 0; j < k; j++) {
             nn_ids[(size_t)q * k + j] = nn[j] >= 0 ? r->parts[nn[j]].GetID() : -1;
             d2[(size_t)q * k + j] = dd[j];

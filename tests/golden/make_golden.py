@@ -167,9 +167,63 @@ def smoothing():
                 phys_nsearch=32, veldensity_phys=vphys, veldensity_phys_id=vphys_id, **one)
 
 
+def phase_space():
+    """Phase-space (TPHS) and velocity (TVEL) trees on clustered particles with velocities:
+    the tree, FindNearest(tt) and FindNearest(x) with the plain phase distance
+    (Aniso = -1) and with the local metric (Aniso = 0, the reference's default), periodic
+    and not; CalcDensity / CalcDensityParticle with the local metric (the reference
+    reads uninitialised arrays for Aniso = -1); FOFCriterion with the three comparators on
+    the phase-space tree."""
+    n, box = 1000, 20.0
+    pos, mass, vel = syn.clustered_box(n, box, seed=31, velocities=True)
+    rng = np.random.default_rng(32)
+    ids = np.array([0, 17, 404, 777, n - 1], np.int32)
+    pts6 = np.concatenate([pos[ids], vel[ids]], 1) + rng.normal(scale=0.02, size=(len(ids), 6))
+    pts3 = vel[ids] + rng.normal(scale=0.02, size=(len(ids), 3))
+    out = dict(pos=pos, vel=vel, mass=mass, b=16, box=box, ids=ids, points6=pts6, points3=pts3)
+
+    def mk(tt, aniso, per):
+        return oracle.OracleTree(pos, vel, mass, 16, tt, 0, 1000, per, backend="ref",
+                                 nthreads=4, aniso=aniso)
+    for tag, aniso in (("plain", -1), ("metric", 0)):
+        for ptag, per in (("", None), ("_per", [box] * 3)):
+            t = mk(3, aniso, per)
+            if aniso == -1 and per is None:
+                out["phs_num_nodes"] = t.num_nodes
+                out["phs_leaf_ids"] = _leaf_sets(t)
+            nn, d2 = t.knn(10)
+            out[f"phs_{tag}{ptag}_nn"], out[f"phs_{tag}{ptag}_d2"] = nn, d2
+            nn, d2 = t.knn_coord(pts6, 10)
+            out[f"phs_{tag}{ptag}_pt_nn"], out[f"phs_{tag}{ptag}_pt_d2"] = nn, d2
+            if aniso == 0:
+                out[f"phs_{tag}{ptag}_rho"] = mk(3, aniso, per).density(16)
+                out[f"phs_{tag}{ptag}_rho_id"] = np.array(
+                    [t.density_particle(int(i), 16) for i in ids])
+    t = mk(2, 0, None)
+    out["vel_num_nodes"] = t.num_nodes
+    out["vel_leaf_ids"] = _leaf_sets(t)
+    out["vel_nn"], out["vel_d2"] = t.knn(10)
+    out["vel_pt_nn"], out["vel_pt_d2"] = t.knn_coord(pts3, 10)
+    out["vel_rho"] = mk(2, 0, None).density(16)
+    # The search region (params[1], params[2] per dimension kind) contains each
+    # comparator's linking region, so every link is found from both of its ends; the
+    # reference's breadth-first grouping relies on that (otherwise a later group can take
+    # a particle of an earlier one, which corrupts its member lists).
+    for cmp, (s1, s2, l6, l7) in ((0, (0.09, 1e30, 0.09, 0)), (1, (1e30, 0.0025, 0.0025, 0)),
+                                  (2, (0.25, 0.04, 0.25, 0.04))):
+        params = np.zeros(20)
+        params[:3] = [3, s1, s2]
+        params[6:8] = [l6, l7]
+        out[f"fof_params_{cmp}"] = params
+        for ptag, per in (("", None), ("_per", [box] * 3)):
+            g, ng = mk(3, 0, per).fof_criterion(cmp, params, 8, 0)
+            out[f"fof{ptag}_{cmp}"], out[f"fof{ptag}_{cmp}_ng"] = g, ng
+    return out
+
+
 FIXTURES = [("uniform_periodic", uniform_periodic), ("clustered", clustered),
             ("nonperiodic", nonperiodic), ("tiny_periodic", tiny_periodic),
-            ("smoothing", smoothing)]
+            ("smoothing", smoothing), ("phase_space", phase_space)]
 
 
 def main(names=None):

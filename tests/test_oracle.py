@@ -241,3 +241,74 @@ def test_port_fof_nn_matches_reference(ref_built, cmp):
     gr, ngr = R.fof_nn(cmp, params, rn, 5, pidx=[6], dist2=rd * 0.4)
     gp, ngp = P.fof_nn(cmp, params, pn, 5, values=(pd * 0.4).max(1), pidx=[6])
     assert ngr == ngp and np.array_equal(gr, gp)
+
+
+def _phase_tree(g, treetype, aniso, periodic, backend="port"):
+    per = [float(g["box"])] * 3 if periodic else None
+    return oracle.OracleTree(g["pos"], g["vel"], g["mass"], int(g["b"]), treetype, 0, 1000, per,
+                             backend=backend, nthreads=4, aniso=aniso)
+
+
+@pytest.mark.parametrize("aniso", [-1, 0])
+@pytest.mark.parametrize("periodic", [False, True])
+def test_port_phase_space_matches_golden(port_built, aniso, periodic):
+    """Phase-space trees: FindNearest(tt), FindNearest(x) and, with the local metric,
+    CalcDensity / CalcDensityParticle, bit-identical to the reference's outputs."""
+    g = golden("phase_space")
+    tag = ("plain" if aniso == -1 else "metric") + ("_per" if periodic else "")
+    t = _phase_tree(g, 3, aniso, periodic)
+    assert t.num_nodes == int(g["phs_num_nodes"])
+    k = g[f"phs_{tag}_nn"].shape[1]
+    nn, d2 = t.knn(k)
+    np.testing.assert_array_equal(nn, g[f"phs_{tag}_nn"])
+    np.testing.assert_array_equal(d2, g[f"phs_{tag}_d2"])
+    nn, d2 = t.knn_coord(g["points6"], k)
+    np.testing.assert_array_equal(nn, g[f"phs_{tag}_pt_nn"])
+    np.testing.assert_array_equal(d2, g[f"phs_{tag}_pt_d2"])
+    if aniso == 0:
+        np.testing.assert_array_equal(_phase_tree(g, 3, aniso, periodic).density(16),
+                                      g[f"phs_{tag}_rho"])
+        np.testing.assert_array_equal([t.density_particle(int(i), 16) for i in g["ids"]],
+                                      g[f"phs_{tag}_rho_id"])
+
+
+def test_port_velocity_tree_matches_golden(port_built):
+    g = golden("phase_space")
+    t = _phase_tree(g, 2, 0, False)
+    assert t.num_nodes == int(g["vel_num_nodes"])
+    k = g["vel_nn"].shape[1]
+    nn, d2 = t.knn(k)
+    np.testing.assert_array_equal(nn, g["vel_nn"])
+    np.testing.assert_array_equal(d2, g["vel_d2"])
+    nn, d2 = t.knn_coord(g["points3"], k)
+    np.testing.assert_array_equal(nn, g["vel_pt_nn"])
+    np.testing.assert_array_equal(d2, g["vel_pt_d2"])
+    np.testing.assert_array_equal(_phase_tree(g, 2, 0, False).density(16), g["vel_rho"])
+
+
+@pytest.mark.parametrize("cmp", [0, 1, 2])
+@pytest.mark.parametrize("periodic", [False, True])
+def test_port_phase_space_fof_criterion_matches_golden(port_built, cmp, periodic):
+    g = golden("phase_space")
+    tag = "_per" if periodic else ""
+    grp, ng = _phase_tree(g, 3, 0, periodic).fof_criterion(cmp, g[f"fof_params_{cmp}"], 8, 0)
+    assert ng == int(g[f"fof{tag}_{cmp}_ng"])
+    np.testing.assert_array_equal(grp, g[f"fof{tag}_{cmp}"])
+
+
+@pytest.mark.parametrize("aniso", [-1, 0])
+@pytest.mark.parametrize("periodic", [False, True])
+def test_port_phase_space_matches_reference(ref_built, aniso, periodic):
+    """A larger clustered set straight against the compiled reference."""
+    pos, mass, vel = syn.clustered_box(4000, 30.0, seed=41, velocities=True)
+    per = [30.0] * 3 if periodic else None
+    mk = lambda be: oracle.OracleTree(pos, vel, mass, 16, 3, 0, 1000, per, backend=be,
+                                      nthreads=4, aniso=aniso)
+    R, P = mk("ref"), mk("port")
+    np.testing.assert_array_equal(R.ids(), P.ids())
+    a, da = R.knn(16)
+    b, db = P.knn(16)
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(da, db)
+    if aniso == 0:
+        np.testing.assert_array_equal(mk("ref").density(32), mk("port").density(32))
