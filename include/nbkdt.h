@@ -110,11 +110,19 @@ int64_t nbk_trace_json(char* buf, int64_t cap);
  *  vel  : n x 3 velocities or NULL (needed by nbk_veldensity, nbk_fof_criterion)
  *  mass : n masses or NULL (unit masses)
  *  period: 3 box lengths or NULL (non-periodic)
- * Supported: treetype NBK_TPHYS; kernel types all four; splitting 0, aniso 0,
- * scale_space 0. Anything else returns NBK_ERR_UNSUPPORTED. The tree is built on the
- * GPU with the reference's rules (split dimension of largest spread, median split with
+ * Supported: treetype NBK_TPHYS, NBK_TVEL (velocities required, non-periodic) and
+ * NBK_TPHS (velocities required); kernel types all four; splitting 0, scale_space 0;
+ * aniso 0 or -1 (for a phase-space tree: 0 the local metric of CalculateMetricSpacing +
+ * FindNearestMetric, the reference's default; -1 the plain phase-space distance of
+ * FindNearestPhase; other trees ignore it). Anything else returns NBK_ERR_UNSUPPORTED.
+ * The tree is built on the GPU with the reference's rules (split dimension of largest
+ * spread over the tree's coordinates: x, y, z; vx, vy, vz; or all six; median split with
  * the left child taking ceil(size/2), leaf when size <= bucket_size), so its leaves hold
  * the same particle sets as the reference's.
+ * Velocity and phase-space trees run nbk_knn / nbk_knn_targets (FindNearest),
+ * nbk_knn_coords, nbk_density / nbk_density_particles (phase space: aniso 0 only) and,
+ * for phase-space trees, nbk_fof_criterion; every other call returns NBK_ERR_UNSUPPORTED
+ * for them (the reference refuses them or compares positions with velocity cut values).
  */
 int nbk_create(const double* pos, const double* vel, const double* mass, int64_t n,
                int bucket_size, int treetype, int kerntype, int kernres,
@@ -164,6 +172,14 @@ int nbk_knn_targets(nbk_tree* tree, const int32_t* targets, int64_t ntargets, in
    (KDFindNearest.cxx:509-520); nothing is excluded. */
 int nbk_knn_points(nbk_tree* tree, const double* x, int64_t nq, int k, int periodic_mode,
                    int32_t* nn, double* d2);
+
+/* k nearest neighbours of nq coordinates in the tree's own space. Replaces
+   KDTree::FindNearest(Double_t* x, Int_t* nn, Double_t* dist2, Int_t Nsearch)
+   (KDFindNearest.cxx:460-507): x holds 3 positions per row (physical tree, as
+   nbk_knn_points with NBK_PERIODIC_REF), 3 velocities (velocity tree) or
+   x, y, z, vx, vy, vz (phase-space tree: the plain or local-metric search with the
+   ungated position images of a periodic tree, KDSplitNode.cxx:1153-1218). */
+int nbk_knn_coords(nbk_tree* tree, const double* x, int64_t nq, int k, int32_t* nn, double* d2);
 
 /*
  * SPH density of every particle. Replaces KDTree::CalcDensity(Int_t Nsmooth)

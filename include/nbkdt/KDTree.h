@@ -149,8 +149,11 @@ class KDTree {
   void FindNearestPos(Int_t** nn, Double_t** dist2, Int_t Nsearch = 64) {
     knn_all(nn, dist2, Nsearch, NBK_FINDNEARESTPOS);
   }
+  // x in the tree's space: x, y, z (physical), vx, vy, vz (velocity) or all six (phase)
   void FindNearest(Double_t* x, Int_t* nn, Double_t* dist2, Int_t Nsearch = 64) {
-    FindNearestPos(x, nn, dist2, Nsearch);
+    std::vector<int32_t> n32(Nsearch);
+    nbkdt::check(nbk_knn_coords(tree_, x, 1, Nsearch, n32.data(), dist2));
+    for (Int_t j = 0; j < Nsearch; j++) nn[j] = n32[j];
   }
   void FindNearestPos(Double_t* x, Int_t* nn, Double_t* dist2, Int_t Nsearch = 64) {
     std::vector<int32_t> n32(Nsearch);

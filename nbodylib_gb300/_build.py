@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libnbkdt.so")
-SOURCES = ["capi.cu", "build.cu", "knn.cu", "smooth.cu", "fof.cu", "ball.cu", "adjoint.cu",
+SOURCES = ["capi.cu", "build.cu", "knn.cu", "smooth.cu", "phase.cu", "fof.cu", "ball.cu", "adjoint.cu",
            "batch.cu", "noalloc.cu", "probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Host code is compiled without floating-point contraction: the kernel table is built on

@@ -7,9 +7,13 @@
 // the coordinate), building level by level with the same rules yields nodes holding the
 // same particle sets as the reference's, hence the same node counts and bounding boxes.
 //
+// The same code builds phase-space trees (TreeType TPHS: six coordinates x, y, z, vx, vy,
+// vz, SpreadestPhs / MedianPhs, KDTree.cxx:71-100, 414-456); every kernel takes the
+// number of coordinates ND as a template parameter.
+//
 // Phase 1 (levels whose nodes hold more than kLocalMax particles): for all nodes of a
 // level at once, over chunks of kChunk particles:
-//   bbox      segmented min/max of x, y, z (order-preserving uint64 keys, atomics); for
+//   bbox      segmented min/max of each coordinate (order-preserving uint64 keys); for
 //             the first level only, later levels get it from the partition above them
 //   select    6 radix passes (11, 11, 11, 11, 11, 9 bits) find the key of the median
 //             particle exactly; pass 0 also picks the split dimension from the box
@@ -32,7 +36,11 @@ constexpr int kThreads = 256;
 constexpr int kRounds = kChunk / kThreads;
 constexpr int kLevelCap = kLocalMax;  // level lists hold up to 2*size/(b+1) nodes
 
-struct GNode {
+// The coordinates of the particles being partitioned live in one buffer per ping-pong
+// side: coordinate d of particle i at C[d * cs + i] (cs = the buffer's particle count).
+// ND = 3 for physical trees (x, y, z), 6 for phase-space trees (x, y, z, vx, vy, vz).
+template <int ND>
+struct GNodeT {
   int start, size;  // absolute tree-index range
   int node;         // absolute node index
   int dim;
@@ -47,7 +55,7 @@ struct GNode {
   int ncand;        // keys in the current prefix class
   unsigned nfill;   // keys of the class gathered so far (collect mode)
   unsigned long long prefix, mask;
-  unsigned long long kmin[3], kmax[3];  // node box as order keys (filled by the level above)
+  unsigned long long kmin[ND], kmax[ND];  // node box as order keys (filled by the level above)
 };
 
 // Radix passes of the median selection (11-bit digits from each node's highest differing
@@ -71,16 +79,81 @@ struct LRoot {
   int pad;
 };
 
-__global__ void k_init_soa(const double* __restrict__ pos_in, double* X, double* Y, double* Z,
-                           int* ID, int64_t n, int* err) {
+// Node records written by the build: NodeRec + NodeX for ND = 3, NodeS + NodeB6 for 6.
+template <int ND>
+struct NodeOut;
+template <>
+struct NodeOut<3> {
+  NodeRec* node;
+  NodeX* nodex;
+  __device__ __forceinline__ void write(int idx, const double* lo, const double* hi, int start,
+                                        int count, int dim, double split_val) const {
+    NodeRec r;
+    NodeX x;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      r.lo[d] = __double2float_rd(lo[d]);
+      r.hi[d] = __double2float_ru(hi[d]);
+      x.lo[d] = lo[d];
+      x.hi[d] = hi[d];
+    }
+    r.start = start;
+    r.count = count;
+    x.split_dim = dim;
+    x.split_val = split_val;
+    x.pad = 0;
+    node[idx] = r;
+    nodex[idx] = x;
+  }
+  __device__ __forceinline__ void set_split(int idx, double v) const { nodex[idx].split_val = v; }
+};
+template <>
+struct NodeOut<6> {
+  NodeS* nodes;
+  NodeB6* nodeb;
+  __device__ __forceinline__ void write(int idx, const double* lo, const double* hi, int start,
+                                        int count, int dim, double split_val) const {
+    NodeS r;
+    NodeB6 x;
+#pragma unroll
+    for (int d = 0; d < 6; d++) {
+      x.lo[d] = lo[d];
+      x.hi[d] = hi[d];
+    }
+    r.split_val = split_val;
+    r.split_dim = dim;
+    r.start = start;
+    r.count = count;
+    r.pad = 0;
+    nodes[idx] = r;
+    nodeb[idx] = x;
+  }
+  __device__ __forceinline__ void set_split(int idx, double v) const { nodes[idx].split_val = v; }
+};
+
+// a[dim] of a small array indexed at run time, kept in registers
+template <int ND, typename T>
+__device__ __forceinline__ T sel(const T* a, int dim) {
+  T r = a[0];
+#pragma unroll
+  for (int d = 1; d < ND; d++)
+    if (dim == d) r = a[d];
+  return r;
+}
+
+template <int ND>
+__global__ void k_init_soa(const double* __restrict__ pos_in, const double* __restrict__ vel_in,
+                           double* C, int64_t cs, int* ID, int64_t n, int* err) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double x = pos_in[3 * i], y = pos_in[3 * i + 1], z = pos_in[3 * i + 2];
-  if (!(x == x) || !(y == y) || !(z == z) || isinf(x) || isinf(y) || isinf(z))
-    atomicExch(err, 1);
-  X[i] = x;
-  Y[i] = y;
-  Z[i] = z;
+  bool bad = false;
+#pragma unroll
+  for (int d = 0; d < ND; d++) {
+    double v = d < 3 ? pos_in[3 * i + d] : vel_in[3 * i + d - 3];
+    bad = bad || !(v == v) || isinf(v);
+    C[d * cs + i] = v;
+  }
+  if (bad) atomicExch(err, 1);
   ID[i] = (int)i;
 }
 
@@ -99,85 +172,70 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
   return v;
 }
 
-__global__ void __launch_bounds__(kThreads) k_bbox(const Chunk* __restrict__ chunks, GNode* g,
-                                                   const double* X, const double* Y,
-                                                   const double* Z) {
+template <int ND>
+__global__ void __launch_bounds__(kThreads) k_bbox(const Chunk* __restrict__ chunks,
+                                                   GNodeT<ND>* g, const double* C, int64_t cs) {
   Chunk c = chunks[blockIdx.x];
-  unsigned long long mn[3] = {~0ull, ~0ull, ~0ull}, mx[3] = {0ull, 0ull, 0ull};
-  double vx[kRounds], vy[kRounds], vz[kRounds];
+  unsigned long long mn[ND], mx[ND];
 #pragma unroll
-  for (int r = 0; r < kRounds; r++) {
-    int i = r * kThreads + threadIdx.x;
-    if (i < c.len) {
-      vx[r] = X[c.start + i];
-      vy[r] = Y[c.start + i];
-      vz[r] = Z[c.start + i];
-    }
+  for (int d = 0; d < ND; d++) {
+    mn[d] = ~0ull;
+    mx[d] = 0ull;
   }
 #pragma unroll
-  for (int r = 0; r < kRounds; r++) {
-    int i = r * kThreads + threadIdx.x;
-    if (i < c.len) {
-      unsigned long long k0 = okey(vx[r]), k1 = okey(vy[r]), k2 = okey(vz[r]);
-      mn[0] = min(mn[0], k0);
-      mx[0] = max(mx[0], k0);
-      mn[1] = min(mn[1], k1);
-      mx[1] = max(mx[1], k1);
-      mn[2] = min(mn[2], k2);
-      mx[2] = max(mx[2], k2);
+  for (int d = 0; d < ND; d++) {
+    double v[kRounds];
+#pragma unroll
+    for (int r = 0; r < kRounds; r++) {
+      int i = r * kThreads + threadIdx.x;
+      if (i < c.len) v[r] = C[d * cs + c.start + i];
+    }
+#pragma unroll
+    for (int r = 0; r < kRounds; r++) {
+      int i = r * kThreads + threadIdx.x;
+      if (i < c.len) {
+        unsigned long long k = okey(v[r]);
+        mn[d] = min(mn[d], k);
+        mx[d] = max(mx[d], k);
+      }
     }
   }
-  __shared__ unsigned long long s[6][kThreads / 32];
+  __shared__ unsigned long long s[2 * ND][kThreads / 32];
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int d = 0; d < 3; d++) {
+#pragma unroll
+  for (int d = 0; d < ND; d++) {
     unsigned long long a = warp_min_u64(mn[d]), b = warp_max_u64(mx[d]);
     if (lane == 0) {
       s[d][w] = a;
-      s[3 + d][w] = b;
+      s[ND + d][w] = b;
     }
   }
   __syncthreads();
-  if (threadIdx.x < 3) {
+  if (threadIdx.x < ND) {
     int d = threadIdx.x;
     unsigned long long a = ~0ull, b = 0ull;
     for (int i = 0; i < kThreads / 32; i++) {
       a = min(a, s[d][i]);
-      b = max(b, s[3 + d][i]);
+      b = max(b, s[ND + d][i]);
     }
     atomicMin(&g[c.g].kmin[d], a);
     atomicMax(&g[c.g].kmax[d], b);
   }
 }
 
-__device__ __forceinline__ void write_node(NodeRec* node, NodeX* nodex, int idx, const double lo[3],
-                           const double hi[3], int start, int count, int dim, double split_val) {
-  NodeRec r;
-  NodeX x;
-  for (int d = 0; d < 3; d++) {
-    r.lo[d] = __double2float_rd(lo[d]);
-    r.hi[d] = __double2float_ru(hi[d]);
-    x.lo[d] = lo[d];
-    x.hi[d] = hi[d];
-  }
-  r.start = start;
-  r.count = count;
-  x.split_dim = dim;
-  x.split_val = split_val;
-  x.pad = 0;
-  node[idx] = r;
-  nodex[idx] = x;
-}
-
 // DetermineSplitDim (KDTree.cxx:459-504): spread = max - min per dimension in FP64, the
 // first strictly larger spread wins.
-__device__ __forceinline__ int split_dim_of(const GNode& s, double lo[3], double hi[3]) {
-  for (int d = 0; d < 3; d++) {
+template <int ND>
+__device__ __forceinline__ int split_dim_of(const GNodeT<ND>& s, double* lo, double* hi) {
+#pragma unroll
+  for (int d = 0; d < ND; d++) {
     lo[d] = okey_inv(s.kmin[d]);
     hi[d] = okey_inv(s.kmax[d]);
   }
   int dim = 0;
   double cur = dsub(hi[0], lo[0]);
-  for (int d = 1; d < 3; d++) {
+#pragma unroll
+  for (int d = 1; d < ND; d++) {
     double sp = dsub(hi[d], lo[d]);
     if (sp > cur) {
       dim = d;
@@ -189,43 +247,35 @@ __device__ __forceinline__ int split_dim_of(const GNode& s, double lo[3], double
 
 __device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned* tot, unsigned* wsum);
 
-__device__ __forceinline__ unsigned long long sel3(unsigned long long a, unsigned long long b,
-                                                   unsigned long long c, int d) {
-  return d == 0 ? a : (d == 1 ? b : c);
-}
-
 // One radix pass of the median selection for every node of a level. Each block
 // histograms one chunk's digits; the last block of a node to finish (arrival counter,
 // no waiting) reads the node's histogram, narrows the rank to one digit and clears the
 // histogram for the next pass. Pass 0 also fixes the split dimension from the node box
 // (each block derives the same one) and writes the node's records.
-__global__ void __launch_bounds__(kThreads) k_radix(const Chunk* __restrict__ chunks, GNode* g,
-                                                    const double* X, const double* Y,
-                                                    const double* Z, unsigned* hist,
-                                                    unsigned long long* cand, int pass,
-                                                    NodeRec* node, NodeX* nodex, int p0,
-                                                    int* err) {
+template <int ND>
+__global__ void __launch_bounds__(kThreads) k_radix(const Chunk* __restrict__ chunks,
+                                                    GNodeT<ND>* g, const double* Cb, int64_t cs,
+                                                    unsigned* hist, unsigned long long* cand,
+                                                    int pass, NodeOut<ND> out, int p0, int* err) {
   static_assert(kCollect <= kBins / 2, "the gathered keys share the bins' shared memory");
   __shared__ unsigned long long sk[kBins / 2];  // the bins, or the gathered keys
   unsigned* h = reinterpret_cast<unsigned*>(sk);
   __shared__ unsigned wsum[32], tot;
   __shared__ int s_last;
   Chunk c = chunks[blockIdx.x];
-  const GNode s = g[c.g];
+  const GNodeT<ND> s = g[c.g];
   if (s.mask == ~0ull) return;  // the median key of this node is already known
   int dim, first_diff;
-  double lo[3], hi[3];
-  // (the node record stays in registers: no element of it is indexed at run time)
-  const unsigned long long kmin_d[3] = {s.kmin[0], s.kmin[1], s.kmin[2]};
+  double lo[ND], hi[ND];
   if (pass == 0) {
-    dim = split_dim_of(s, lo, hi);
-    unsigned long long x = sel3(s.kmin[0], s.kmin[1], s.kmin[2], dim) ^
-                           sel3(s.kmax[0], s.kmax[1], s.kmax[2], dim);
+    dim = split_dim_of<ND>(s, lo, hi);
+    unsigned long long x = sel<ND>(s.kmin, dim) ^ sel<ND>(s.kmax, dim);
     first_diff = x ? 63 - __clzll((long long)x) : -1;
   } else {
     dim = s.dim;
     first_diff = s.first_diff;
   }
+  const double* C = Cb + (int64_t)dim * cs;
   // digits start at the node's highest differing key bit: pass p resolves the 11 bits
   // below first_diff - 11p (fewer for the last one); the bits above first_diff are common
   // to every key of the node and enter the prefix in pass 0
@@ -237,7 +287,6 @@ __global__ void __launch_bounds__(kThreads) k_radix(const Chunk* __restrict__ ch
   const bool collect = !skip && s.ncand <= kCollect;
   if (collect) {
     // gather the class's keys into this node's slice of the candidate buffer
-    const double* C = dim == 0 ? X : (dim == 1 ? Y : Z);
     double v[kRounds];
 #pragma unroll
     for (int r = 0; r < kRounds; r++) {
@@ -266,7 +315,6 @@ __global__ void __launch_bounds__(kThreads) k_radix(const Chunk* __restrict__ ch
   } else if (!skip) {
     for (int i = threadIdx.x; i < kBins; i += kThreads) h[i] = 0;
     __syncthreads();
-    const double* C = dim == 0 ? X : (dim == 1 ? Y : Z);
     double v[kRounds];
 #pragma unroll
     for (int r = 0; r < kRounds; r++) {
@@ -302,10 +350,10 @@ __global__ void __launch_bounds__(kThreads) k_radix(const Chunk* __restrict__ ch
       g[c.g].dim = dim;
       g[c.g].first_diff = first_diff;
       // the split value is written once the median key is known (k_chunk_scan)
-      write_node(node, nodex, s.node, lo, hi, p0 + s.start, s.size, dim, 0.0);
+      out.write(s.node, lo, hi, p0 + s.start, s.size, dim, 0.0);
     }
   }
-  const unsigned long long kmin_dim = sel3(kmin_d[0], kmin_d[1], kmin_d[2], dim);
+  const unsigned long long kmin_dim = sel<ND>(s.kmin, dim);
   if (skip) {  // all keys equal (first_diff = -1): the median key is the minimum key
     if (threadIdx.x == 0) {
       g[c.g].prefix = kmin_dim;
@@ -402,15 +450,16 @@ __device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned* tot, u
 }
 
 // Per chunk: how many keys are below / equal to the median key.
+template <int ND>
 __global__ void __launch_bounds__(kThreads) k_count(const Chunk* __restrict__ chunks,
-                                                    const GNode* __restrict__ g, const double* X,
-                                                    const double* Y, const double* Z,
+                                                    const GNodeT<ND>* __restrict__ g,
+                                                    const double* Cb, int64_t cs,
                                                     unsigned* cnt_less, unsigned* cnt_eq) {
   Chunk c = chunks[blockIdx.x];
-  const GNode& s = g[c.g];
+  const GNodeT<ND>& s = g[c.g];
   unsigned long long piv = s.prefix;
   unsigned a = 0, e = 0;
-  const double* C = s.dim == 0 ? X : (s.dim == 1 ? Y : Z);
+  const double* C = Cb + (int64_t)s.dim * cs;
   double v[kRounds];
 #pragma unroll
   for (int r = 0; r < kRounds; r++) {
@@ -448,25 +497,27 @@ __global__ void __launch_bounds__(kThreads) k_count(const Chunk* __restrict__ ch
 
 // One block per node: exclusive scan of the chunk counts (chunk order), the split value,
 // and the number of equal keys that go left.
-__global__ void __launch_bounds__(kThreads) k_chunk_scan(GNode* g, const unsigned* cnt_less,
+template <int ND>
+__global__ void __launch_bounds__(kThreads) k_chunk_scan(GNodeT<ND>* g, const unsigned* cnt_less,
                                                          const unsigned* cnt_eq,
                                                          unsigned* base_less, unsigned* base_eq,
-                                                         NodeX* nodex) {
+                                                         NodeOut<ND> out) {
   __shared__ unsigned wsum[32];
   __shared__ unsigned tot;
-  GNode s = g[blockIdx.x];
+  const GNodeT<ND>& sg = g[blockIdx.x];
+  const int nchunks = sg.nchunks, first_chunk = sg.first_chunk;
   unsigned run_l = 0, run_e = 0;
-  for (int c0 = 0; c0 < s.nchunks; c0 += kThreads) {
+  for (int c0 = 0; c0 < nchunks; c0 += kThreads) {
     int c = c0 + threadIdx.x;
-    unsigned vl = c < s.nchunks ? cnt_less[s.first_chunk + c] : 0;
-    unsigned ve = c < s.nchunks ? cnt_eq[s.first_chunk + c] : 0;
+    unsigned vl = c < nchunks ? cnt_less[first_chunk + c] : 0;
+    unsigned ve = c < nchunks ? cnt_eq[first_chunk + c] : 0;
     unsigned el = block_excl_scan(vl, &tot, wsum);
     unsigned tl = tot;
     unsigned ee = block_excl_scan(ve, &tot, wsum);
     unsigned te = tot;
-    if (c < s.nchunks) {
-      base_less[s.first_chunk + c] = run_l + el;
-      base_eq[s.first_chunk + c] = run_e + ee;
+    if (c < nchunks) {
+      base_less[first_chunk + c] = run_l + el;
+      base_eq[first_chunk + c] = run_e + ee;
     }
     run_l += tl;
     run_e += te;
@@ -474,11 +525,11 @@ __global__ void __launch_bounds__(kThreads) k_chunk_scan(GNode* g, const unsigne
   if (threadIdx.x == 0) {
     // after selection n_less counts every key below the median key; rank k + 1 particles
     // go left: all of those plus (k_total + 1 - n_less) equal keys.
-    int ktot = (s.size - 1) / 2;
+    int ktot = (sg.size - 1) / 2;
     g[blockIdx.x].need_eq = ktot + 1 - (int)run_l;
     g[blockIdx.x].total_eq = (int)run_e;
     g[blockIdx.x].n_less = (int)run_l;
-    nodex[s.node].split_val = okey_inv(s.prefix);
+    out.set_split(sg.node, okey_inv(sg.prefix));
   }
 }
 
@@ -486,30 +537,29 @@ __global__ void __launch_bounds__(kThreads) k_chunk_scan(GNode* g, const unsigne
 // buffer. Each warp owns 256 consecutive particles of the chunk, taken 32 at a time, so
 // ballots give every particle its rank inside its class and the writes of one class are
 // contiguous across the warp; one block scan of the warps' (less, equal, valid) counts
-// orders the warps. The children's bounding boxes (order keys of x, y, z) are gathered on
-// the way and merged into the next level's nodes.
+// orders the warps. The children's bounding boxes (order keys of every coordinate) are
+// gathered on the way and merged into the next level's nodes.
+template <int ND>
 __global__ void __launch_bounds__(kThreads) k_scatter(const Chunk* __restrict__ chunks,
-                                                      const GNode* __restrict__ g,
-                                                      const double* __restrict__ X,
-                                                      const double* __restrict__ Y,
-                                                      const double* __restrict__ Z,
+                                                      const GNodeT<ND>* __restrict__ g,
+                                                      const double* __restrict__ Cb,
                                                       const int* __restrict__ ID,
-                                                      double* __restrict__ X2,
-                                                      double* __restrict__ Y2,
-                                                      double* __restrict__ Z2,
-                                                      int* __restrict__ ID2,
+                                                      double* __restrict__ C2,
+                                                      int* __restrict__ ID2, int64_t cs,
                                                       const unsigned* base_less,
                                                       const unsigned* base_eq, int* err,
-                                                      GNode* gnext) {
+                                                      GNodeT<ND>* gnext) {
   constexpr int kWarps = kThreads / 32, kPerWarp = kChunk / kWarps;
   __shared__ unsigned wl[kWarps], we[kWarps], wv[kWarps];
-  __shared__ unsigned long long bb[kWarps][12];
+  __shared__ unsigned long long bb[kWarps][4 * ND];
   Chunk c = chunks[blockIdx.x];
-  const GNode s = g[c.g];
+  const GNodeT<ND>& s = g[c.g];
   const unsigned long long piv = s.prefix;
+  const int sdim = s.dim, sstart = s.start, ssize = s.size, sneed = s.need_eq,
+            sless = s.n_less, stot = s.total_eq, child0 = s.child[0], child1 = s.child[1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
-  const double* C = s.dim == 0 ? X : (s.dim == 1 ? Y : Z);
+  const double* C = Cb + (int64_t)sdim * cs;
   const int w0 = warp * kPerWarp;
   unsigned cls = 0, nl = 0, ne = 0, nv = 0;
 #pragma unroll
@@ -538,14 +588,14 @@ __global__ void __launch_bounds__(kThreads) k_scatter(const Chunk* __restrict__ 
     pv += wv[q];
   }
   const unsigned bl = base_less[blockIdx.x], be = base_eq[blockIdx.x];
-  const int kleft = (s.size - 1) / 2 + 1;
-  const int right0 = s.start + kleft;
-  const int excess = s.total_eq - s.need_eq;
+  const int kleft = (ssize - 1) / 2 + 1;
+  const int right0 = sstart + kleft;
+  const int excess = stot - sneed;
   unsigned rl = bl + pl, re = be + pe;
   unsigned rg = ((unsigned)c.off - bl - be) + (pv - pl - pe);  // greater keys before this warp
-  unsigned long long mnl[3], mxl[3], mnr[3], mxr[3];  // left / right child boxes
+  unsigned long long mnl[ND], mxl[ND], mnr[ND], mxr[ND];  // left / right child boxes
 #pragma unroll
-  for (int d = 0; d < 3; d++) {
+  for (int d = 0; d < ND; d++) {
     mnl[d] = mnr[d] = ~0ull;
     mxl[d] = mxr[d] = 0ull;
   }
@@ -558,76 +608,72 @@ __global__ void __launch_bounds__(kThreads) k_scatter(const Chunk* __restrict__ 
       int p = c.start + w0 + r * 32 + lane;
       int dst;
       if (k == 0) {
-        dst = s.start + (int)(rl + __popc(bL & lt));
+        dst = sstart + (int)(rl + __popc(bL & lt));
       } else if (k == 1) {
         int e = (int)(re + __popc(bE & lt));
-        dst = e < s.need_eq ? s.start + s.n_less + e : right0 + (e - s.need_eq);
+        dst = e < sneed ? sstart + sless + e : right0 + (e - sneed);
       } else {
         dst = right0 + excess + (int)(rg + __popc(bG & lt));
       }
-      if (dst < s.start || dst >= s.start + s.size) {  // selection inconsistent: report
+      if (dst < sstart || dst >= sstart + ssize) {  // selection inconsistent: report
         atomicExch(err, 2);
         dst = p;
       }
-      double x = X[p], y = Y[p], z = Z[p];
-      X2[dst] = x;
-      Y2[dst] = y;
-      Z2[dst] = z;
-      ID2[dst] = ID[p];
-      unsigned long long kk[3] = {okey(x), okey(y), okey(z)};
-      if (dst < right0) {
+      const bool to_left = dst < right0;
 #pragma unroll
-        for (int d = 0; d < 3; d++) {
-          mnl[d] = min(mnl[d], kk[d]);
-          mxl[d] = max(mxl[d], kk[d]);
-        }
-      } else {
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-          mnr[d] = min(mnr[d], kk[d]);
-          mxr[d] = max(mxr[d], kk[d]);
+      for (int d = 0; d < ND; d++) {
+        double x = Cb[d * cs + p];
+        C2[d * cs + dst] = x;
+        unsigned long long kk = okey(x);
+        if (to_left) {
+          mnl[d] = min(mnl[d], kk);
+          mxl[d] = max(mxl[d], kk);
+        } else {
+          mnr[d] = min(mnr[d], kk);
+          mxr[d] = max(mxr[d], kk);
         }
       }
+      ID2[dst] = ID[p];
     }
     rl += __popc(bL);
     re += __popc(bE);
     rg += __popc(bG);
   }
-  if (gnext == nullptr || (s.child[0] < 0 && s.child[1] < 0)) return;
+  if (gnext == nullptr || (child0 < 0 && child1 < 0)) return;
 #pragma unroll
-  for (int d = 0; d < 3; d++) {
+  for (int d = 0; d < ND; d++) {
     unsigned long long a = warp_min_u64(mnl[d]), b = warp_max_u64(mxl[d]);
     unsigned long long a2 = warp_min_u64(mnr[d]), b2 = warp_max_u64(mxr[d]);
     if (lane == 0) {
       bb[warp][d] = a;
-      bb[warp][3 + d] = b;
-      bb[warp][6 + d] = a2;
-      bb[warp][9 + d] = b2;
+      bb[warp][ND + d] = b;
+      bb[warp][2 * ND + d] = a2;
+      bb[warp][3 * ND + d] = b2;
     }
   }
   __syncthreads();
-  if (threadIdx.x < 12) {
-    int t = threadIdx.x / 6, e = threadIdx.x % 6;
-    int child = t == 0 ? s.child[0] : s.child[1];
+  if (threadIdx.x < 4 * ND) {
+    int t = threadIdx.x / (2 * ND), e = threadIdx.x % (2 * ND);
+    int child = t == 0 ? child0 : child1;
     if (child >= 0) {
-      bool is_min = e < 3;
+      bool is_min = e < ND;
       unsigned long long v = is_min ? ~0ull : 0ull;
       for (int q = 0; q < kWarps; q++) {
         unsigned long long u = bb[q][threadIdx.x];
         v = is_min ? min(v, u) : max(v, u);
       }
       if (is_min) atomicMin(&gnext[child].kmin[e], v);
-      else atomicMax(&gnext[child].kmax[e - 3], v);
+      else atomicMax(&gnext[child].kmax[e - ND], v);
     }
   }
 }
 
 // ---- phase 2: one CTA per subtree of at most kLocalMax particles.
-// The subtree is sorted once along x, y and z (key, then local index). No level sorts
-// again: a node's bounding box is the first and last entry of its segment in each sorted
-// list, its median along the split dimension is the middle entry of that list, and the
-// four index lists (the three sorted lists and the particle order) are split stably into
-// the children's segments with one block scan per level.
+// The subtree is sorted once along every coordinate (key, then local index). No level
+// sorts again: a node's bounding box is the first and last entry of its segment in each
+// sorted list, its median along the split dimension is the middle entry of that list,
+// and the ND + 1 index lists (the sorted lists and the particle order) are split stably
+// into the children's segments with one block scan per level (two lists per scan word).
 struct LNode {
   short start, size;  // local range
   int h;              // heap index within the tree
@@ -636,52 +682,78 @@ struct LNode {
   int dim;            // -1 leaf
 };
 
-constexpr int kSortN = 3 * kLocalMax;
-constexpr int kLocalThreads = 512;  // two CTAs of 16 warps per SM (shared memory bound)
+constexpr int kLocalThreads = 512;  // two CTAs of 16 warps per SM for ND = 3 (shared memory)
 
+// Shared-memory layout of k_local_build<ND>.
+template <int ND>
+struct LocalLayout {
+  static constexpr int K = kLocalMax;
+  static constexpr int kSortN = ND * K;
+  static constexpr int kLists = ND + 1;
+  static constexpr int kWords = (kLists + 1) / 2;  // packed scan words per position
+  static constexpr size_t coords = 0;                                         // double[ND][K]
+  static constexpr size_t skey = coords + sizeof(double) * ND * K;            // u64[kSortN]
+  static constexpr size_t id = skey + sizeof(unsigned long long) * kSortN;    // int[K]
+  static constexpr size_t sidx = id + sizeof(int) * K;                        // u16[kSortN]
+  static constexpr size_t lst = sidx + sizeof(unsigned short) * kSortN;       // u16[2][kLists][K]
+  static constexpr size_t lv = lst + sizeof(unsigned short) * 2 * kLists * K;  // LNode[2][cap]
+  static constexpr size_t total = lv + sizeof(LNode) * 2 * kLevelCap;
+  // reused after the sort, inside skey: scan words, node slots, left flags
+  static constexpr size_t sc = skey;                                  // unsigned[kWords][K]
+  static constexpr size_t node_at = sc + sizeof(unsigned) * kWords * K;  // short[K]
+  static constexpr size_t left = node_at + sizeof(short) * K;           // u8[K]
+  static_assert(left + K <= id, "the reused region fits inside the sort keys");
+  static_assert(lv % 16 == 0, "LNode alignment");
+};
+
+template <int ND>
+struct PartOut {
+  P4* pos;
+  float4* posf;
+  V4* vel;
+  int* perm;
+};
+
+template <int ND>
 __global__ void __launch_bounds__(kLocalThreads) k_local_build(
-    const LRoot* __restrict__ roots, const double* Xa, const double* Ya, const double* Za,
-    const int* IDa, const double* Xb, const double* Yb, const double* Zb, const int* IDb,
-    const double* __restrict__ mass_in, const double* __restrict__ vel_in, int b,
-    NodeRec* node, NodeX* nodex, P4* pos, float4* posf, V4* vel, int* perm, int* err, int p0) {
+    const LRoot* __restrict__ roots, const double* Ca, const int* IDa, const double* Cb,
+    const int* IDb, int64_t cs, const double* __restrict__ mass_in,
+    const double* __restrict__ vel_in, int b, NodeOut<ND> out, PartOut<ND> po, int* err,
+    int p0) {
+  using L = LocalLayout<ND>;
   extern __shared__ __align__(16) unsigned char smem[];
-  double* cx = (double*)smem;                                         // [kLocalMax]
-  double* cy = cx + kLocalMax;
-  double* cz = cy + kLocalMax;
-  unsigned long long* skey = (unsigned long long*)(cz + kLocalMax);  // [kSortN], sort only
-  unsigned* sc01 = (unsigned*)skey;             // after the sort: packed scans of lists 0,1
-  unsigned* sc23 = sc01 + kLocalMax;            //                 and of lists 2,3
-  short* node_at = (short*)(sc23 + kLocalMax);  // level slot of each position, -1 finished
-  unsigned char* left = (unsigned char*)(node_at + kLocalMax);  // per particle
-  int* id = (int*)(skey + kSortN);                              // [kLocalMax]
-  unsigned short* sidx = (unsigned short*)(id + kLocalMax);     // [kSortN]
-  unsigned short* lst = sidx + kSortN;                          // [2][4][kLocalMax]
-  LNode* lv = (LNode*)(lst + 8 * kLocalMax);                    // [kLevelCap]
+  double* cc = (double*)(smem + L::coords);                        // cc[d * K + r]
+  unsigned long long* skey = (unsigned long long*)(smem + L::skey);  // sort only
+  unsigned* sc = (unsigned*)(smem + L::sc);            // after the sort: packed scans
+  short* node_at = (short*)(smem + L::node_at);        // level slot of each position, -1 done
+  unsigned char* left = smem + L::left;                // per particle
+  int* id = (int*)(smem + L::id);
+  unsigned short* sidx = (unsigned short*)(smem + L::sidx);
+  unsigned short* lst = (unsigned short*)(smem + L::lst);
+  LNode* lv = (LNode*)(smem + L::lv);
   LNode* lv2 = lv + kLevelCap;
   __shared__ int n_cur, n_next;
   __shared__ unsigned wsum[32], tot;
-  const int K = kLocalMax;
+  constexpr int K = L::K;
+  constexpr int NL = L::kLists;
 
   const LRoot R = roots[blockIdx.x];
   const int S = R.size;
-  const double* X = R.buf ? Xb : Xa;
-  const double* Y = R.buf ? Yb : Ya;
-  const double* Z = R.buf ? Zb : Za;
+  const double* C = R.buf ? Cb : Ca;
   const int* I = R.buf ? IDb : IDa;
   for (int e = threadIdx.x; e < S; e += kLocalThreads) {
-    cx[e] = X[R.start + e];
-    cy[e] = Y[R.start + e];
-    cz[e] = Z[R.start + e];
+#pragma unroll
+    for (int d = 0; d < ND; d++) cc[d * K + e] = C[d * cs + R.start + e];
     id[e] = I[R.start + e];
   }
   __syncthreads();
   int P = 1;
   while (P < S) P <<= 1;
-  const int total = 3 * P;
+  const int total = ND * P;
   for (int t = threadIdx.x; t < total; t += kLocalThreads) {
     int d = t / P, r = t - d * P;
     if (r < S) {
-      skey[t] = okey(d == 0 ? cx[r] : (d == 1 ? cy[r] : cz[r]));
+      skey[t] = okey(cc[d * K + r]);
       sidx[t] = (unsigned short)r;
     } else {
       skey[t] = ~0ull;
@@ -689,7 +761,7 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_build(
     }
   }
   __syncthreads();
-  // three segments of P sorted at once; every segment ascending by (key, local index)
+  // ND segments of P sorted at once; every segment ascending by (key, local index)
   for (int kk = 2; kk <= P; kk <<= 1) {
     for (int jj = kk >> 1; jj > 0; jj >>= 1) {
       for (int t = threadIdx.x; t < total; t += kLocalThreads) {
@@ -711,8 +783,8 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_build(
     }
   }
   unsigned short* cur = lst;
-  unsigned short* nxt = lst + 4 * K;
-  for (int t = threadIdx.x; t < 3 * S; t += kLocalThreads) {
+  unsigned short* nxt = lst + NL * K;
+  for (int t = threadIdx.x; t < ND * S; t += kLocalThreads) {
     int d = t / S, i = t - d * S;
     unsigned short q = sidx[d * P + i];
     if (q >= S) {  // a padding slot inside the sorted range: report, keep in bounds
@@ -721,8 +793,9 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_build(
     }
     cur[d * K + i] = q;
   }
+  __syncthreads();  // the sort keys' region is reused from here on
   for (int i = threadIdx.x; i < S; i += kLocalThreads) {
-    cur[3 * K + i] = (unsigned short)i;
+    cur[ND * K + i] = (unsigned short)i;
     node_at[i] = 0;
   }
   if (threadIdx.x == 0) {
@@ -744,15 +817,20 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_build(
     for (int j = threadIdx.x; j < n_cur; j += kLocalThreads) {
       LNode nd = lv[j];
       int a0 = nd.start, a1 = nd.start + nd.size - 1;
-      double lo[3] = {cx[cur[a0]], cy[cur[K + a0]], cz[cur[2 * K + a0]]};
-      double hi[3] = {cx[cur[a1]], cy[cur[K + a1]], cz[cur[2 * K + a1]]};
+      double lo[ND], hi[ND];
+#pragma unroll
+      for (int d = 0; d < ND; d++) {
+        lo[d] = cc[d * K + cur[d * K + a0]];
+        hi[d] = cc[d * K + cur[d * K + a1]];
+      }
       int dim = -1;
       double split = 0.0;
       if (nd.size > b) {
         // DetermineSplitDim: the first strictly larger FP64 spread wins
         dim = 0;
         double spread = dsub(hi[0], lo[0]);
-        for (int d = 1; d < 3; d++) {
+#pragma unroll
+        for (int d = 1; d < ND; d++) {
           double sp = dsub(hi[d], lo[d]);
           if (sp > spread) {
             dim = d;
@@ -761,7 +839,7 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_build(
         }
         int kl = (nd.size - 1) / 2 + 1;
         int q = cur[dim * K + nd.start + kl - 1];
-        split = dim == 0 ? cx[q] : (dim == 1 ? cy[q] : cz[q]);
+        split = cc[dim * K + q];
         int slot = atomicAdd(&n_next, 2);
         if (slot + 2 <= kLevelCap) {
           LNode l, r;
@@ -784,13 +862,12 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_build(
       }
       nd.dim = dim;
       lv[j] = nd;
-      write_node(node, nodex, R.nbase + nd.h, lo, hi, p0 + R.start + nd.start, nd.size, dim,
-                 split);
+      out.write(R.nbase + nd.h, lo, hi, p0 + R.start + nd.start, nd.size, dim, split);
     }
     __syncthreads();
     if (n_next == 0 || n_next > kLevelCap) break;
     // B: which particles go left, read off the list of their node's split dimension
-    for (int t = threadIdx.x; t < 3 * S; t += kLocalThreads) {
+    for (int t = threadIdx.x; t < ND * S; t += kLocalThreads) {
       int d = t / S, i = t - d * S;
       int j = node_at[i];
       if (j >= 0) {
@@ -799,35 +876,40 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_build(
       }
     }
     __syncthreads();
-    // C: exclusive scans of the left flags of the four lists (two packed per word); each
+    // C: exclusive scans of the left flags of the NL lists (two packed per word); each
     // thread covers kPerT consecutive positions
     {
       constexpr int kPerT = kLocalMax / kLocalThreads;
-      unsigned f01[kPerT], f23[kPerT], s01 = 0, s23 = 0;
+      constexpr int NW = L::kWords;
+      unsigned f[NW][kPerT], sw[NW];
+#pragma unroll
+      for (int w = 0; w < NW; w++) sw[w] = 0;
 #pragma unroll
       for (int u = 0; u < kPerT; u++) {
         int i = kPerT * threadIdx.x + u;
-        unsigned a = 0, c = 0;
+        bool split_here = false;
         if (i < S) {
           int j = node_at[i];
-          if (j >= 0 && lv[j].dim >= 0) {
-            a = left[cur[i]] | ((unsigned)left[cur[K + i]] << 16);
-            c = left[cur[2 * K + i]] | ((unsigned)left[cur[3 * K + i]] << 16);
-          }
+          split_here = j >= 0 && lv[j].dim >= 0;
         }
-        f01[u] = s01;
-        f23[u] = s23;
-        s01 += a;
-        s23 += c;
-      }
-      unsigned b01 = block_excl_scan_t<kLocalThreads>(s01, &tot, wsum);
-      unsigned b23 = block_excl_scan_t<kLocalThreads>(s23, &tot, wsum);
 #pragma unroll
-      for (int u = 0; u < kPerT; u++) {
-        int i = kPerT * threadIdx.x + u;
-        if (i < S) {
-          sc01[i] = b01 + f01[u];
-          sc23[i] = b23 + f23[u];
+        for (int w = 0; w < NW; w++) {
+          unsigned a = 0;
+          if (split_here) {
+            a = left[cur[(2 * w) * K + i]];
+            if (2 * w + 1 < NL) a |= (unsigned)left[cur[(2 * w + 1) * K + i]] << 16;
+          }
+          f[w][u] = sw[w];
+          sw[w] += a;
+        }
+      }
+#pragma unroll
+      for (int w = 0; w < NW; w++) {
+        unsigned bw = block_excl_scan_t<kLocalThreads>(sw[w], &tot, wsum);
+#pragma unroll
+        for (int u = 0; u < kPerT; u++) {
+          int i = kPerT * threadIdx.x + u;
+          if (i < S) sc[w * K + i] = bw + f[w][u];
         }
       }
     }
@@ -837,21 +919,23 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_build(
       int j = node_at[i];
       if (j < 0) {
 #pragma unroll
-        for (int l = 0; l < 4; l++) nxt[l * K + i] = cur[l * K + i];
+        for (int l = 0; l < NL; l++) nxt[l * K + i] = cur[l * K + i];
         continue;
       }
       LNode nd = lv[j];
       if (nd.dim < 0) {
 #pragma unroll
-        for (int l = 0; l < 4; l++) nxt[l * K + i] = cur[l * K + i];
+        for (int l = 0; l < NL; l++) nxt[l * K + i] = cur[l * K + i];
         node_at[i] = -1;
         continue;
       }
       int rel = i - nd.start;
-      unsigned v01 = sc01[i] - sc01[nd.start], v23 = sc23[i] - sc23[nd.start];
+      unsigned vw[L::kWords];
 #pragma unroll
-      for (int l = 0; l < 4; l++) {
-        unsigned v = l < 2 ? v01 : v23;
+      for (int w = 0; w < L::kWords; w++) vw[w] = sc[w * K + i] - sc[w * K + nd.start];
+#pragma unroll
+      for (int l = 0; l < NL; l++) {
+        unsigned v = vw[l >> 1];
         int before = (int)((l & 1) ? (v >> 16) : (v & 0xffffu));  // left entries before i
         unsigned short q = cur[l * K + i];
         int dst = left[q] ? nd.start + before : nd.start + nd.kl + (rel - before);
@@ -875,20 +959,24 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_build(
   }
   // final tree-order arrays: the particle-order list holds every leaf contiguously
   for (int e = threadIdx.x; e < S; e += kLocalThreads) {
-    int q = cur[3 * K + e];
+    int q = cur[ND * K + e];
     int t = p0 + R.start + e;  // absolute tree index
     int ii = p0 + id[q];       // absolute input index
     double m = mass_in ? mass_in[ii] : 1.0;
     P4 p;
-    p.x = cx[q];
-    p.y = cy[q];
-    p.z = cz[q];
+    p.x = cc[q];
+    p.y = cc[K + q];
+    p.z = cc[2 * K + q];
     p.m = m;
-    pos[t] = p;
-    posf[t] = make_float4(__double2float_rn(p.x), __double2float_rn(p.y),
-                          __double2float_rn(p.z), 0.f);
-    perm[t] = ii;
-    if (vel && vel_in) vel[t] = make_v4(vel_in[3 * ii], vel_in[3 * ii + 1], vel_in[3 * ii + 2], 0.0);
+    po.pos[t] = p;
+    po.posf[t] = make_float4(__double2float_rn(p.x), __double2float_rn(p.y),
+                             __double2float_rn(p.z), 0.f);
+    po.perm[t] = ii;
+    if (ND == 6) {
+      po.vel[t] = make_v4(cc[3 * K + q], cc[4 * K + q], cc[5 * K + q], 0.0);
+    } else if (po.vel && vel_in) {
+      po.vel[t] = make_v4(vel_in[3 * ii], vel_in[3 * ii + 1], vel_in[3 * ii + 2], 0.0);
+    }
   }
 }
 
@@ -903,10 +991,8 @@ int depth_of(int64_t n, int b) {
 
 }  // namespace
 
-size_t local_build_smem() {
-  return sizeof(double) * 3 * kLocalMax + sizeof(unsigned long long) * kSortN +
-         sizeof(int) * kLocalMax + sizeof(unsigned short) * (kSortN + 8 * kLocalMax) +
-         sizeof(LNode) * 2 * kLevelCap;
+size_t local_build_smem(int nd) {
+  return nd == 6 ? LocalLayout<6>::total : LocalLayout<3>::total;
 }
 
 // One growing page-locked buffer per host thread for the build plans.
@@ -945,9 +1031,12 @@ int64_t count_nodes(int64_t n, int b) {
 }
 
 // Build every tree of the forest. All arrays live on `st`. Returns NBK status.
-int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_in,
-                 const double* d_mass_in, const double* d_vel_in, BuiltArrays& out,
-                 DevAlloc& alloc, cudaStream_t st, NodeX* root_out) {
+template <int ND>
+static int build_forest_t(const std::vector<TreeSpec>& trees, int b, const double* d_pos_in,
+                          const double* d_mass_in, const double* d_vel_in, NodeOut<ND> nout,
+                          PartOut<ND> pout, DevAlloc& alloc, cudaStream_t st, void* root_out,
+                          size_t root_bytes, const void* root_src) {
+  using GNode = GNodeT<ND>;
   Phase ph("build", st);
   // internal buffers cover only [p0, p0 + ntot), the particles of these trees
   int64_t p0 = trees.empty() ? 0 : trees[0].pstart, pend = 0;
@@ -957,18 +1046,15 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
   }
   int64_t ntot = pend - p0;
   if (ntot == 0) return NBK_OK;
-  double *Xa, *Ya, *Za, *Xb, *Yb, *Zb;
+  double *Ca, *Cb;
   int *IDa, *IDb, *d_err;
-  NBK_TRY(alloc.get((void**)&Xa, sizeof(double) * ntot));
-  NBK_TRY(alloc.get((void**)&Ya, sizeof(double) * ntot));
-  NBK_TRY(alloc.get((void**)&Za, sizeof(double) * ntot));
-  NBK_TRY(alloc.get((void**)&Xb, sizeof(double) * ntot));
-  NBK_TRY(alloc.get((void**)&Yb, sizeof(double) * ntot));
-  NBK_TRY(alloc.get((void**)&Zb, sizeof(double) * ntot));
+  NBK_TRY(alloc.get((void**)&Ca, sizeof(double) * ND * ntot));
+  NBK_TRY(alloc.get((void**)&Cb, sizeof(double) * ND * ntot));
   NBK_TRY(alloc.get((void**)&IDa, sizeof(int) * ntot));
   NBK_TRY(alloc.get((void**)&IDb, sizeof(int) * ntot));
   NBK_TRY(alloc.get((void**)&d_err, sizeof(int)));
   NBK_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+  const int64_t cs = ntot;  // coordinate stride of the ping-pong buffers
 
   // The whole plan (every global level's nodes and chunks, every subtree handed to the
   // per-CTA phase) depends only on the tree sizes, so it is computed on the host first
@@ -1001,7 +1087,7 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
       g.k = (int)((cur[i].size - 1) / 2);  // rank of the median inside the node
       g.ncand = (int)cur[i].size;
       g.child[0] = g.child[1] = -1;
-      for (int d = 0; d < 3; d++) {
+      for (int d = 0; d < ND; d++) {
         g.kmin[d] = ~0ull;  // boxes are merged in with atomics
         g.kmax[d] = 0ull;
       }
@@ -1074,8 +1160,9 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
     NBK_TRY(alloc.get((void**)&d_bl, sizeof(unsigned) * ncall));
     NBK_TRY(alloc.get((void**)&d_be, sizeof(unsigned) * ncall));
   }
-  k_init_soa<<<(unsigned)((ntot + 255) / 256), 256, 0, st>>>(d_pos_in + 3 * p0, Xa, Ya, Za, IDa, ntot,
-                                                            d_err); note_launch();
+  k_init_soa<ND><<<(unsigned)((ntot + 255) / 256), 256, 0, st>>>(
+      d_pos_in + 3 * p0, d_vel_in ? d_vel_in + 3 * p0 : nullptr, Ca, cs, IDa, ntot, d_err);
+  note_launch();
   NBK_CUDA_TRY(cudaGetLastError());
   for (size_t li = 0; li < levels.size(); li++) {
     const Level& L = levels[li];
@@ -1084,50 +1171,45 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
     Chunk* d_c = d_call + L.c0;
     unsigned *cl = d_cl + L.c0, *ce = d_ce + L.c0, *bl = d_bl + L.c0, *be = d_be + L.c0;
     int ng = L.ng, nc = L.nc;
-    const double* X = L.buf ? Xb : Xa;
-    const double* Y = L.buf ? Yb : Ya;
-    const double* Z = L.buf ? Zb : Za;
+    const double* C = L.buf ? Cb : Ca;
     const int* I = L.buf ? IDb : IDa;
-    double* X2 = L.buf ? Xa : Xb;
-    double* Y2 = L.buf ? Ya : Yb;
-    double* Z2 = L.buf ? Za : Zb;
+    double* C2 = L.buf ? Ca : Cb;
     int* I2 = L.buf ? IDa : IDb;
     // boxes of the first level's nodes; every later level gets them from the scatter above
     if (li == 0) {
-      k_bbox<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z); note_launch();
+      k_bbox<ND><<<nc, kThreads, 0, st>>>(d_c, d_g, C, cs); note_launch();
     }
     for (int pass = 0; pass < kPasses; pass++) {
-      k_radix<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, d_hist, d_cand, pass, out.node,
-                                       out.nodex, (int)p0, d_err); note_launch();
+      k_radix<ND><<<nc, kThreads, 0, st>>>(d_c, d_g, C, cs, d_hist, d_cand, pass, nout, (int)p0,
+                                           d_err); note_launch();
     }
-    k_count<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, cl, ce); note_launch();
-    k_chunk_scan<<<ng, kThreads, 0, st>>>(d_g, cl, ce, bl, be, out.nodex); note_launch();
-    k_scatter<<<nc, kThreads, 0, st>>>(d_c, d_g, X, Y, Z, I, X2, Y2, Z2, I2, bl, be, d_err,
-                                       d_gnext); note_launch();
+    k_count<ND><<<nc, kThreads, 0, st>>>(d_c, d_g, C, cs, cl, ce); note_launch();
+    k_chunk_scan<ND><<<ng, kThreads, 0, st>>>(d_g, cl, ce, bl, be, nout); note_launch();
+    k_scatter<ND><<<nc, kThreads, 0, st>>>(d_c, d_g, C, I, C2, I2, cs, bl, be, d_err, d_gnext);
+    note_launch();
     NBK_CUDA_TRY(cudaGetLastError());
   }
   if (!lroots.empty()) {
-    size_t sm = local_build_smem();
+    size_t sm = LocalLayout<ND>::total;
     static bool attr_set = false;
     if (!attr_set) {
-      NBK_CUDA_TRY(cudaFuncSetAttribute(k_local_build, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)sm));
+      NBK_CUDA_TRY(cudaFuncSetAttribute(k_local_build<ND>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
       attr_set = true;
     }
-    k_local_build<<<(unsigned)lroots.size(), kLocalThreads, sm, st>>>(
-        d_r, Xa, Ya, Za, IDa, Xb, Yb, Zb, IDb, d_mass_in, d_vel_in, b, out.node, out.nodex,
-        out.pos, out.posf, out.vel, out.perm, d_err, (int)p0); note_launch();
+    k_local_build<ND><<<(unsigned)lroots.size(), kLocalThreads, sm, st>>>(
+        d_r, Ca, IDa, Cb, IDb, cs, d_mass_in, d_vel_in, b, nout, pout, d_err, (int)p0);
+    note_launch();
     NBK_CUDA_TRY(cudaGetLastError());
   }
-  if (root_out && !trees.empty())
-    NBK_CUDA_TRY(cudaMemcpyAsync(root_out, out.nodex + trees[0].nbase, sizeof(NodeX),
-                                 cudaMemcpyDeviceToHost, st));
+  if (root_out && root_src)
+    NBK_CUDA_TRY(cudaMemcpyAsync(root_out, root_src, root_bytes, cudaMemcpyDeviceToHost, st));
   int h_err = 0;
   NBK_CUDA_TRY(cudaMemcpyAsync(&h_err, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
   NBK_CUDA_TRY(cudaStreamSynchronize(st));
   alloc.release_all_scratch(st);
   if (h_err == 1) {
-    set_error("input positions contain NaN or infinity");
+    set_error("input positions or velocities contain NaN or infinity");
     return NBK_ERR_INVALID;
   }
   if (h_err) {
@@ -1135,6 +1217,30 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
     return NBK_ERR_DEVICE;
   }
   return NBK_OK;
+}
+
+int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_in,
+                 const double* d_mass_in, const double* d_vel_in, BuiltArrays& out,
+                 DevAlloc& alloc, cudaStream_t st, NodeX* root_out) {
+  NodeOut<3> no{out.node, out.nodex};
+  PartOut<3> po{out.pos, out.posf, out.vel, out.perm};
+  const void* src = trees.empty() ? nullptr : (const void*)(out.nodex + trees[0].nbase);
+  return build_forest_t<3>(trees, b, d_pos_in, d_mass_in, d_vel_in, no, po, alloc, st, root_out,
+                           sizeof(NodeX), src);
+}
+
+int build_forest_phase(const std::vector<TreeSpec>& trees, int b, const double* d_pos_in,
+                       const double* d_mass_in, const double* d_vel_in, BuiltArrays& out,
+                       DevAlloc& alloc, cudaStream_t st, NodeB6* root_out) {
+  if (!d_vel_in) {
+    set_error("phase-space tree: velocities are required");
+    return NBK_ERR_INVALID;
+  }
+  NodeOut<6> no{out.nodes6, out.nodeb6};
+  PartOut<6> po{out.pos, out.posf, out.vel, out.perm};
+  const void* src = trees.empty() ? nullptr : (const void*)(out.nodeb6 + trees[0].nbase);
+  return build_forest_t<6>(trees, b, d_pos_in, d_mass_in, d_vel_in, no, po, alloc, st, root_out,
+                           sizeof(NodeB6), src);
 }
 
 }  // namespace nbk

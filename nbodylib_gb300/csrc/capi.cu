@@ -74,24 +74,25 @@ void kernel_table(int kerntype, int kernres, int nd, std::vector<double>& T, dou
   for (int i = 0; i < kernres; i++) T[i] = kn * f(i * delta, 1.0);
 }
 
-// Device kernel tables are shared by every tree of one (device, kernel, resolution): built
+// Device kernel tables are shared by every tree of one (device, kernel, resolution,
+// dimension count): built
 // and uploaded once per process, never freed (a few tens of KB each).
 struct KernelEntry {
   std::vector<double> table;
   double norm = 0;
   double* d_img = nullptr;
 };
-static int cached_kernel(int kerntype, int kernres, const KernelEntry** out) {
+static int cached_kernel(int kerntype, int kernres, int nd, const KernelEntry** out) {
   static std::mutex mu;
-  static std::map<std::tuple<int, int, int>, KernelEntry> cache;
+  static std::map<std::tuple<int, int, int, int>, KernelEntry> cache;
   int dev = 0;
   NBK_CUDA_TRY(cudaGetDevice(&dev));
   std::lock_guard<std::mutex> lock(mu);
-  auto key = std::make_tuple(dev, kerntype, kernres);
+  auto key = std::make_tuple(dev, kerntype, kernres, nd);
   auto it = cache.find(key);
   if (it == cache.end()) {
     KernelEntry e;
-    kernel_table(kerntype, kernres, 3, e.table, e.norm);
+    kernel_table(kerntype, kernres, nd, e.table, e.norm);
     std::vector<double> img;
     kernel_device_image(e.table, img);
     NBK_CUDA_TRY(cudaMalloc((void**)&e.d_img, sizeof(double) * img.size()));
@@ -234,6 +235,7 @@ using namespace nbk;
 struct nbk_tree {
   int64_t n = 0;
   int b = 16, treetype = 0, kerntype = 0, kernres = 1000;
+  int aniso = 0;  // phase-space trees: -1 plain phase distance, 0 local metric
   bool periodic = false;
   double period[3] = {0, 0, 0};
   unsigned flags = 0;
@@ -255,6 +257,7 @@ struct nbk_tree {
     v.perm = arr.perm;
     v.node = arr.node;
     v.nodex = arr.nodex;
+    v.nodes6 = arr.nodes6;
     v.n = (int)n;
     v.pstart = 0;
     v.nbase = 0;
@@ -360,6 +363,19 @@ int check_tree(const nbk_tree* t) {
   return NBK_OK;
 }
 
+// The entry points that only a physical tree supports: on velocity and phase-space trees
+// the reference either refuses them (CalcVelDensity, the smoothing family) or compares
+// positions with velocity or phase-space cut values (ball searches, FOF), which
+// KDTree::GetPosition(j) answers past the end of its three-element array for j > 2.
+int check_phys(const nbk_tree* t, const char* what) {
+  NBK_TRY(check_tree(t));
+  if (t->treetype != NBK_TPHYS) {
+    set_error(std::string(what) + ": runs on physical trees only (TreeType TPHYS)");
+    return NBK_ERR_UNSUPPORTED;
+  }
+  return NBK_OK;
+}
+
 }  // namespace
 
 namespace nbk {
@@ -370,6 +386,10 @@ int density_into_scratch(nbk_tree* t, int k, double* scratch, double* rho_dev) {
   if (!t || !scratch || !rho_dev || k < 1) {
     set_error("nbk_density_noalloc: invalid argument");
     return NBK_ERR_INVALID;
+  }
+  if (t->treetype == NBK_TPHS) {
+    set_error("nbk_density_noalloc: physical and velocity trees only");
+    return NBK_ERR_UNSUPPORTED;
   }
   if (k > t->n - 1) {
     set_error("nbk_density_noalloc: k = " + std::to_string(k) + " exceeds the " +
@@ -467,18 +487,27 @@ int nbk_create(const double* pos, const double* vel, const double* mass, int64_t
     set_error("nbk_create: bucket sizes >= 1024 are not supported on the GPU");
     return NBK_ERR_UNSUPPORTED;
   }
-  if (treetype != NBK_TPHYS) {
-    set_error("nbk_create: only the physical tree (TPHYS) runs on the GPU");
+  if (treetype != NBK_TPHYS && treetype != NBK_TVEL && treetype != NBK_TPHS) {
+    set_error("nbk_create: tree types TPHYS, TVEL and TPHS run on the GPU (TPROJ and TMETRIC do not)");
     return NBK_ERR_UNSUPPORTED;
   }
-  if (splitting_criterion != 0 || aniso != 0 || scale_space != 0) {
-    set_error("nbk_create: splitting criterion, anisotropic metric and space scaling other than 0 are not supported");
+  if ((treetype == NBK_TVEL || treetype == NBK_TPHS) && !vel) {
+    set_error("nbk_create: velocity and phase-space trees need velocities");
+    return NBK_ERR_INVALID;
+  }
+  if (treetype == NBK_TVEL && period) {
+    set_error("nbk_create: periodic velocity trees are not supported");
+    return NBK_ERR_UNSUPPORTED;
+  }
+  if (splitting_criterion != 0 || scale_space != 0 || (aniso != 0 && aniso != -1)) {
+    set_error("nbk_create: splitting criterion and space scaling other than 0, and the anisotropic metric tensor (Aniso 1), are not supported");
     return NBK_ERR_UNSUPPORTED;
   }
   std::unique_ptr<nbk_tree> t(new nbk_tree);
   t->n = n;
   t->b = bucket_size;
   t->treetype = treetype;
+  t->aniso = aniso;
   t->kerntype = (kerntype >= NBK_KSPH && kerntype <= NBK_KTH) ? kerntype : NBK_KSPH;
   t->kernres = kernres < 100 ? 100 : kernres;  // KDTree.cxx:1145-1148
   t->flags = flags;
@@ -502,7 +531,7 @@ int nbk_create(const double* pos, const double* vel, const double* mass, int64_t
   cudaStream_t st = t->st;
   {
     const KernelEntry* ke;
-    NBK_TRY(cached_kernel(t->kerntype, t->kernres, &ke));
+    NBK_TRY(cached_kernel(t->kerntype, t->kernres, treetype == NBK_TPHS ? 6 : 3, &ke));
     t->h_kernel = ke->table;
     t->kernnorm = ke->norm;
     t->d_kernel = ke->d_img;  // shared, not owned by the tree
@@ -522,10 +551,17 @@ int nbk_create(const double* pos, const double* vel, const double* mass, int64_t
   NBK_TRY(dev_malloc((void**)&A.posf, sizeof(float4) * n, st));
   NBK_TRY(dev_malloc((void**)&A.perm, sizeof(int) * n, st));
   if (vel) NBK_TRY(dev_malloc((void**)&A.vel, sizeof(V4) * n, st));
-  NBK_TRY(dev_malloc((void**)&A.node, sizeof(NodeRec) * t->nslots, st));
-  NBK_TRY(dev_malloc((void**)&A.nodex, sizeof(NodeX) * t->nslots, st));
-  NBK_CUDA_TRY(cudaMemsetAsync(A.node, 0, sizeof(NodeRec) * t->nslots, st));
-  NBK_CUDA_TRY(cudaMemsetAsync(A.nodex, 0, sizeof(NodeX) * t->nslots, st));
+  if (treetype == NBK_TPHS) {
+    NBK_TRY(dev_malloc((void**)&A.nodes6, sizeof(NodeS) * t->nslots, st));
+    NBK_TRY(dev_malloc((void**)&A.nodeb6, sizeof(NodeB6) * t->nslots, st));
+    NBK_CUDA_TRY(cudaMemsetAsync(A.nodes6, 0, sizeof(NodeS) * t->nslots, st));
+    NBK_CUDA_TRY(cudaMemsetAsync(A.nodeb6, 0, sizeof(NodeB6) * t->nslots, st));
+  } else {
+    NBK_TRY(dev_malloc((void**)&A.node, sizeof(NodeRec) * t->nslots, st));
+    NBK_TRY(dev_malloc((void**)&A.nodex, sizeof(NodeX) * t->nslots, st));
+    NBK_CUDA_TRY(cudaMemsetAsync(A.node, 0, sizeof(NodeRec) * t->nslots, st));
+    NBK_CUDA_TRY(cudaMemsetAsync(A.nodex, 0, sizeof(NodeX) * t->nslots, st));
+  }
   DevAlloc alloc;
   alloc.st = st;
   const double *d_pos = pos, *d_vel = vel, *d_mass = mass;
@@ -547,12 +583,29 @@ int nbk_create(const double* pos, const double* vel, const double* mass, int64_t
   }
   std::vector<TreeSpec> trees{{0, n, 0}};
   // the root's exact box comes back with the build's own final synchronisation
-  NodeX root;
-  NBK_TRY(build_forest(trees, bucket_size, d_pos, d_mass, d_vel, A, alloc, st, &root));
+  double rlo[3], rhi[3];
+  if (treetype == NBK_TPHS) {
+    NodeB6 root;
+    NBK_TRY(build_forest_phase(trees, bucket_size, d_pos, d_mass, d_vel, A, alloc, st, &root));
+    for (int d = 0; d < 3; d++) {
+      rlo[d] = root.lo[d];
+      rhi[d] = root.hi[d];
+    }
+  } else {
+    // a velocity tree is the same tree over the velocities (FindNearestVel,
+    // BoundaryandMeanVel, MedianVel): positions and velocities trade places on the device
+    if (treetype == NBK_TVEL) std::swap(d_pos, d_vel);
+    NodeX root;
+    NBK_TRY(build_forest(trees, bucket_size, d_pos, d_mass, d_vel, A, alloc, st, &root));
+    for (int d = 0; d < 3; d++) {
+      rlo[d] = root.lo[d];
+      rhi[d] = root.hi[d];
+    }
+  }
   // FP32 rounding bound for coordinates and image coordinates
   double maxabs = 0;
   for (int d = 0; d < 3; d++)
-    maxabs = std::max(maxabs, std::max(std::fabs(root.lo[d]), std::fabs(root.hi[d])));
+    maxabs = std::max(maxabs, std::max(std::fabs(rlo[d]), std::fabs(rhi[d])));
   double maxper = std::max(t->period[0], std::max(t->period[1], t->period[2]));
   t->eps = (float)std::ldexp(maxabs + maxper, -23) * 1.0001f + 1e-38f;
   alloc.release_all_scratch(st);
@@ -570,6 +623,8 @@ int nbk_destroy(nbk_tree* t) {
   dev_free(t->arr.perm, st);
   dev_free(t->arr.node, st);
   dev_free(t->arr.nodex, st);
+  dev_free(t->arr.nodes6, st);
+  dev_free(t->arr.nodeb6, st);
   // t->d_kernel belongs to the process-wide kernel cache
   dev_free(t->d_err, st);
   cudaStreamSynchronize(st);
@@ -618,6 +673,41 @@ int nbk_get_kernel(const nbk_tree* t, double* table, double* kernnorm) {
   return NBK_OK;
 }
 
+// Phase-space trees: FindNearest(tt) for qmode 0 (every particle) / 2 (targets) and
+// FindNearest(x) for qmode 1 (six values per point), through the reference's own walk
+// (phase.cu). A periodic target search grows the heap by one and drops its nearest entry
+// (KDFindNearest.cxx:250, 310).
+static int phase_nn(nbk_tree* t, int qmode, const int* dq, const double* dx, int64_t nq, int k,
+                    int* dnn, double* dd2) {
+  PhaseArgs pa{};
+  pa.k = base_args(t);
+  pa.k.periodic = t->periodic ? 1 : 0;
+  pa.k.kheap = (t->periodic && qmode != 1) ? k + 1 : k;
+  pa.k.kout = k;
+  pa.k.qmode = qmode;
+  pa.k.qidx = dq;
+  pa.k.qx = dx;
+  pa.k.nq = (int)nq;
+  pa.k.nn = dnn;
+  pa.k.d2 = dd2;
+  pa.metric = t->aniso == 0;
+  pa.spacing_periodic = t->periodic ? 1 : 0;
+  pa.epi = kPhNN;
+  return launch_phase(pa, t->st);
+}
+
+static int knn_variant_ok(const nbk_tree* t, int variant, const char* what) {
+  if (t->treetype != NBK_TPHYS && variant != NBK_FINDNEAREST) {
+    set_error(std::string(what) + ": FindNearestPos runs on physical trees only");
+    return NBK_ERR_UNSUPPORTED;
+  }
+  if (t->treetype == NBK_TPHS && t->n < 8 && t->aniso == 0) {
+    set_error(std::string(what) + ": the local metric needs at least 8 particles (the reference exits)");
+    return NBK_ERR_TOO_FEW;
+  }
+  return NBK_OK;
+}
+
 int nbk_knn(nbk_tree* t, int k, int variant, int periodic_mode, int32_t* nn, double* d2) {
   API_BEGIN
   NBK_TRY(check_tree(t));
@@ -629,12 +719,19 @@ int nbk_knn(nbk_tree* t, int k, int variant, int periodic_mode, int32_t* nn, dou
     set_error("nbk_knn: unknown variant");
     return NBK_ERR_INVALID;
   }
+  NBK_TRY(knn_variant_ok(t, variant, "nbk_knn"));
   Stage S(t);
   int *dnn;
   double* dd2;
   NBK_TRY(S.out(nn, (size_t)t->n * k, &dnn));
   NBK_TRY(S.out(d2, (size_t)t->n * k, &dd2));
   NBK_TRY(clear_err(t));
+  if (t->treetype == NBK_TPHS) {
+    NBK_TRY(phase_nn(t, 0, nullptr, nullptr, t->n, k, dnn, dd2));
+    NBK_TRY(S.finish());
+    if (!t->dev()) NBK_TRY(check_err(t, "nbk_knn"));
+    return NBK_OK;
+  }
   KnnArgs a = base_args(t);
   bool per = t->periodic;  // the heap grows by one whenever a period is set
   a.kheap = per ? k + 1 : k;
@@ -667,6 +764,7 @@ int nbk_knn_targets(nbk_tree* t, const int32_t* targets, int64_t nt, int k, int 
     set_error("nbk_knn_targets: unknown variant");
     return NBK_ERR_INVALID;
   }
+  NBK_TRY(knn_variant_ok(t, variant, "nbk_knn_targets"));
   if (nt == 0) return NBK_OK;
   if (!t->dev())
     for (int64_t i = 0; i < nt; i++)
@@ -682,6 +780,12 @@ int nbk_knn_targets(nbk_tree* t, const int32_t* targets, int64_t nt, int k, int 
   NBK_TRY(S.out(nn, (size_t)nt * k, &dnn));
   NBK_TRY(S.out(d2, (size_t)nt * k, &dd2));
   NBK_TRY(clear_err(t));
+  if (t->treetype == NBK_TPHS) {
+    NBK_TRY(phase_nn(t, 2, dt, nullptr, nt, k, dnn, dd2));
+    NBK_TRY(S.finish());
+    if (!t->dev()) NBK_TRY(check_err(t, "nbk_knn_targets"));
+    return NBK_OK;
+  }
   KnnArgs a = base_args(t);
   bool per = t->periodic;
   a.kheap = per ? k + 1 : k;
@@ -705,7 +809,7 @@ int nbk_knn_targets(nbk_tree* t, const int32_t* targets, int64_t nt, int k, int 
 int nbk_knn_points(nbk_tree* t, const double* x, int64_t nq, int k, int periodic_mode,
                    int32_t* nn, double* d2) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_knn_points"));
   if (k < 1 || !x || !nn || !d2 || nq < 0) {
     set_error("nbk_knn_points: invalid argument");
     return NBK_ERR_INVALID;
@@ -738,6 +842,73 @@ int nbk_knn_points(nbk_tree* t, const double* x, int64_t nq, int k, int periodic
 }
 
 
+int nbk_knn_coords(nbk_tree* t, const double* x, int64_t nq, int k, int32_t* nn, double* d2) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  if (k < 1 || !x || !nn || !d2 || nq < 0) {
+    set_error("nbk_knn_coords: invalid argument");
+    return NBK_ERR_INVALID;
+  }
+  if (t->treetype == NBK_TPHYS) return nbk_knn_points(t, x, nq, k, NBK_PERIODIC_REF, nn, d2);
+  NBK_TRY(knn_variant_ok(t, NBK_FINDNEAREST, "nbk_knn_coords"));
+  if (nq == 0) return NBK_OK;
+  const int nd = t->treetype == NBK_TPHS ? 6 : 3;
+  Stage S(t);
+  const double* dx;
+  int* dnn;
+  double* dd2;
+  NBK_TRY(S.in(x, (size_t)nq * nd, &dx));
+  NBK_TRY(S.out(nn, (size_t)nq * k, &dnn));
+  NBK_TRY(S.out(d2, (size_t)nq * k, &dd2));
+  NBK_TRY(clear_err(t));
+  if (t->treetype == NBK_TPHS) {
+    NBK_TRY(phase_nn(t, 1, nullptr, dx, nq, k, dnn, dd2));
+  } else {  // velocity tree (never periodic): FindNearestVel(x) over the swapped arrays
+    KnnArgs a = base_args(t);
+    a.kheap = k;
+    a.kout = k;
+    a.periodic = 0;
+    a.exclude_self = 0;
+    a.qmode = 1;
+    a.qx = dx;
+    a.nq = (int)nq;
+    a.nn = dnn;
+    a.d2 = dd2;
+    NBK_TRY(launch_knn(a, kEpiNN, t->st));
+  }
+  NBK_TRY(S.finish());
+  if (!t->dev()) NBK_TRY(check_err(t, "nbk_knn_coords"));
+  return NBK_OK;
+  API_END
+}
+
+// CalcDensity / CalcDensityParticle on a phase-space tree with the local metric: qmode 0
+// scatters into `trho` (tree order), qmode 2 gathers into `out` (query order).
+static int phase_density(nbk_tree* t, int qmode, const int* dq, int64_t nq, int k, double* rho) {
+  if (t->aniso != 0) {
+    set_error("phase-space density needs the local metric (Aniso 0); with Aniso -1 the "
+              "reference multiplies uninitialised metric arrays");
+    return NBK_ERR_UNSUPPORTED;
+  }
+  if (t->n < 8) {
+    set_error("phase-space density: the local metric needs at least 8 particles");
+    return NBK_ERR_TOO_FEW;
+  }
+  PhaseArgs pa{};
+  pa.k = base_args(t);
+  pa.k.periodic = 0;  // CalcDensity ignores the period, and its metric spacing too
+  pa.k.kheap = k;
+  pa.k.kout = k;
+  pa.k.qmode = qmode;
+  pa.k.qidx = dq;
+  pa.k.nq = (int)nq;
+  pa.k.rho = rho;
+  pa.metric = 1;
+  pa.spacing_periodic = 0;
+  pa.epi = qmode == 0 ? kPhDensity : kPhDensPart;
+  return launch_phase(pa, t->st);
+}
+
 static int density_common(nbk_tree* t, int k, int nsmooth, double* rho, double* vden, int epi) {
   if (k < 1) {
     set_error("density: k must be >= 1");
@@ -752,6 +923,10 @@ static int density_common(nbk_tree* t, int k, int nsmooth, double* rho, double* 
     set_error("velocity density needs velocities at nbk_create");
     return NBK_ERR_INVALID;
   }
+  if (epi != kEpiDensity && t->treetype != NBK_TPHYS) {
+    set_error("velocity density runs on physical trees only");
+    return NBK_ERR_UNSUPPORTED;
+  }
   Stage S(t);
   double *drho = nullptr, *dv = nullptr, *trho = nullptr, *tv = nullptr;
   if (rho) NBK_TRY(S.out(rho, t->n, &drho));
@@ -762,6 +937,13 @@ static int density_common(nbk_tree* t, int k, int nsmooth, double* rho, double* 
   }
   if (vden) NBK_TRY(S.alloc.get((void**)&tv, sizeof(double) * t->n));
   NBK_TRY(clear_err(t));
+  if (t->treetype == NBK_TPHS) {
+    NBK_TRY(phase_density(t, 0, nullptr, t->n, k, trho));
+    NBK_TRY(scatter_to_input_order(trho, t->arr.perm, drho, t->n, 1, t->st));
+    NBK_TRY(S.finish());
+    if (!t->dev()) NBK_TRY(check_err(t, "density"));
+    return NBK_OK;
+  }
   KnnArgs a = base_args(t);
   a.tv.periodic = 0;  // CalcDensity ignores the period (KDCalcSmoothQuantities.cxx:227)
   a.kheap = k;
@@ -829,6 +1011,10 @@ static int particles_common(nbk_tree* t, const int32_t* targets, int64_t nt, int
     set_error("velocity density needs velocities at nbk_create");
     return NBK_ERR_INVALID;
   }
+  if (epi != kEpiDensPart && t->treetype != NBK_TPHYS) {
+    set_error("velocity density runs on physical trees only");
+    return NBK_ERR_UNSUPPORTED;
+  }
   if (nt == 0) return NBK_OK;
   if (!t->dev()) {
     for (int64_t i = 0; i < nt; i++)
@@ -843,6 +1029,12 @@ static int particles_common(nbk_tree* t, const int32_t* targets, int64_t nt, int
   NBK_TRY(S.in(targets, nt, &dt));
   NBK_TRY(S.out(out, nt, &dout));
   NBK_TRY(clear_err(t));
+  if (t->treetype == NBK_TPHS) {
+    NBK_TRY(phase_density(t, 2, dt, nt, k, dout));
+    NBK_TRY(S.finish());
+    if (!t->dev()) NBK_TRY(check_err(t, "particle density"));
+    return NBK_OK;
+  }
   KnnArgs a = base_args(t);
   a.tv.periodic = 0;
   a.kheap = k;
@@ -952,7 +1144,7 @@ static int smooth_common(nbk_tree* t, int which, int qmode, const int32_t* targe
 
 int nbk_smooth_vel(nbk_tree* t, int nsmooth, const double* rho, double* smvel) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_smooth_vel"));
   return smooth_common(t, kSmVel, 0, nullptr, nullptr, 0, nsmooth, 0, rho, nullptr, nullptr,
                        nullptr, nullptr, smvel);
   API_END
@@ -961,7 +1153,7 @@ int nbk_smooth_vel(nbk_tree* t, int nsmooth, const double* rho, double* smvel) {
 int nbk_smooth_vel_disp(nbk_tree* t, int nsmooth, const double* rho, const double* smvel,
                         double* disp) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_smooth_vel_disp"));
   return smooth_common(t, kSmVelDisp, 0, nullptr, nullptr, 0, nsmooth, 0, rho, smvel, nullptr,
                        nullptr, nullptr, disp);
   API_END
@@ -970,7 +1162,7 @@ int nbk_smooth_vel_disp(nbk_tree* t, int nsmooth, const double* rho, const doubl
 int nbk_smooth_vel_skew(nbk_tree* t, int nsmooth, const double* rho, const double* smvel,
                         const double* disp, double* skew) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_smooth_vel_skew"));
   return smooth_common(t, kSmVelSkew, 0, nullptr, nullptr, 0, nsmooth, 0, rho, smvel, disp,
                        nullptr, nullptr, skew);
   API_END
@@ -979,7 +1171,7 @@ int nbk_smooth_vel_skew(nbk_tree* t, int nsmooth, const double* rho, const doubl
 int nbk_smooth_vel_kurtosis(nbk_tree* t, int nsmooth, const double* rho, const double* smvel,
                             const double* disp, double* kurt) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_smooth_vel_kurtosis"));
   return smooth_common(t, kSmVelKurt, 0, nullptr, nullptr, 0, nsmooth, 0, rho, smvel, disp,
                        nullptr, nullptr, kurt);
   API_END
@@ -988,7 +1180,7 @@ int nbk_smooth_vel_kurtosis(nbk_tree* t, int nsmooth, const double* rho, const d
 int nbk_veldensity_physdensity(nbk_tree* t, int nsmooth, int nsearch, const double* rho,
                                double* vden) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_veldensity_physdensity"));
   return smooth_common(t, kSmVelPhys, 0, nullptr, nullptr, 0, nsmooth, nsearch, rho, nullptr,
                        nullptr, nullptr, nullptr, vden);
   API_END
@@ -998,7 +1190,7 @@ int nbk_veldensity_physdensity_particles(nbk_tree* t, const int32_t* targets, in
                                          int nsmooth, int nsearch, const double* rho,
                                          double* vden) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_veldensity_physdensity_particles"));
   return smooth_common(t, kSmVelPhys, 2, targets, nullptr, nt, nsmooth, nsearch, rho, nullptr,
                        nullptr, nullptr, nullptr, vden);
   API_END
@@ -1007,7 +1199,7 @@ int nbk_veldensity_physdensity_particles(nbk_tree* t, const int32_t* targets, in
 int nbk_smooth_vel_particles(nbk_tree* t, const int32_t* targets, int64_t nt, int nsmooth,
                              const double* rho, double* smvel) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_smooth_vel_particles"));
   return smooth_common(t, kSmVelOne, 2, targets, nullptr, nt, nsmooth, 0, rho, nullptr, nullptr,
                        nullptr, nullptr, smvel);
   API_END
@@ -1016,7 +1208,7 @@ int nbk_smooth_vel_particles(nbk_tree* t, const int32_t* targets, int64_t nt, in
 int nbk_smooth_vel_points(nbk_tree* t, const double* x, int64_t nq, int nsmooth,
                           const double* rho, double* smvel) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_smooth_vel_points"));
   return smooth_common(t, kSmVelOne, 1, nullptr, x, nq, nsmooth, 0, rho, nullptr, nullptr,
                        nullptr, nullptr, smvel);
   API_END
@@ -1025,7 +1217,7 @@ int nbk_smooth_vel_points(nbk_tree* t, const double* x, int64_t nq, int nsmooth,
 int nbk_smooth_vel_disp_particles(nbk_tree* t, const int32_t* targets, int64_t nt, int nsmooth,
                                   const double* rho, const double* smvel, double* disp) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_smooth_vel_disp_particles"));
   return smooth_common(t, kSmVelDispOne, 2, targets, nullptr, nt, nsmooth, 0, rho, smvel,
                        nullptr, nullptr, nullptr, disp);
   API_END
@@ -1034,7 +1226,7 @@ int nbk_smooth_vel_disp_particles(nbk_tree* t, const int32_t* targets, int64_t n
 int nbk_smooth_vel_disp_points(nbk_tree* t, const double* x, int64_t nq, int nsmooth,
                                const double* rho, const double* smvel, double* disp) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_smooth_vel_disp_points"));
   return smooth_common(t, kSmVelDispOne, 1, nullptr, x, nq, nsmooth, 0, rho, smvel, nullptr,
                        nullptr, nullptr, disp);
   API_END
@@ -1044,7 +1236,7 @@ int nbk_smooth_local_mean_particles(nbk_tree* t, const int32_t* targets, int64_t
                                     int nsmooth, const double* rho, const double* weight,
                                     double* mean) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_smooth_local_mean_particles"));
   return smooth_common(t, kSmMeanOne, 2, targets, nullptr, nt, nsmooth, 0, rho, nullptr,
                        nullptr, weight, nullptr, mean);
   API_END
@@ -1053,7 +1245,7 @@ int nbk_smooth_local_mean_particles(nbk_tree* t, const int32_t* targets, int64_t
 int nbk_smooth_local_mean_points(nbk_tree* t, const double* x, int64_t nq, int nsmooth,
                                  const double* rho, const double* weight, double* mean) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_smooth_local_mean_points"));
   return smooth_common(t, kSmMeanOne, 1, nullptr, x, nq, nsmooth, 0, rho, nullptr, nullptr,
                        weight, nullptr, mean);
   API_END
@@ -1063,7 +1255,7 @@ int nbk_smooth_local_disp_particles(nbk_tree* t, const int32_t* targets, int64_t
                                     int nsmooth, const double* rho, const double* weight,
                                     const double* mean, double* disp) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_smooth_local_disp_particles"));
   return smooth_common(t, kSmDispOne, 2, targets, nullptr, nt, nsmooth, 0, rho, nullptr,
                        nullptr, weight, mean, disp);
   API_END
@@ -1073,7 +1265,7 @@ int nbk_smooth_local_disp_points(nbk_tree* t, const double* x, int64_t nq, int n
                                  const double* rho, const double* weight, const double* mean,
                                  double* disp) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_smooth_local_disp_points"));
   return smooth_common(t, kSmDispOne, 1, nullptr, x, nq, nsmooth, 0, rho, nullptr, nullptr,
                        weight, mean, disp);
   API_END
@@ -1140,7 +1332,7 @@ static int ball_common(nbk_tree* t, int qmode, const int32_t* targets, const dou
 int nbk_ball_tagged(nbk_tree* t, const int32_t* targets, int64_t ntargets, double fdist2,
                     int64_t* offsets, int32_t* out, int64_t out_capacity, int64_t* total) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_ball_tagged"));
   return ball_common(t, 0, targets, nullptr, ntargets, fdist2, offsets, out, out_capacity, total);
   API_END
 }
@@ -1149,7 +1341,7 @@ int nbk_ball_tagged_points(nbk_tree* t, const double* x, int64_t nq, double fdis
                            int64_t* offsets, int32_t* out, int64_t out_capacity,
                            int64_t* total) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_ball_tagged_points"));
   return ball_common(t, 1, nullptr, x, nq, fdist2, offsets, out, out_capacity, total);
   API_END
 }
@@ -1157,7 +1349,7 @@ int nbk_ball_tagged_points(nbk_tree* t, const double* x, int64_t nq, double fdis
 int nbk_ball_mark(nbk_tree* t, int32_t target, double fdist2, int32_t imark, int32_t* nn,
                   double* dist2) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_ball_mark"));
   if (!nn || !dist2 || target < 0 || target >= t->n) {
     set_error("nbk_ball_mark: invalid argument");
     return NBK_ERR_INVALID;
@@ -1178,7 +1370,7 @@ int nbk_ball_mark(nbk_tree* t, int32_t target, double fdist2, int32_t imark, int
 int nbk_fof(nbk_tree* t, double fdist, int32_t minnum, int order, int32_t* group,
             int32_t* ngroup) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_fof"));
   if (!group || !ngroup || !(fdist >= 0)) {
     set_error("nbk_fof: invalid argument");
     return NBK_ERR_INVALID;
@@ -1223,6 +1415,11 @@ int nbk_fof_criterion(nbk_tree* t, int comparator, const double* params, int32_t
   if (comparator != NBK_FOF3D && !t->has_vel) {
     set_error("nbk_fof_criterion: FOFVel and FOF6d need velocities at nbk_create");
     return NBK_ERR_INVALID;
+  }
+  if (t->treetype == NBK_TVEL) {
+    // FOFSearchCriterion compares GetPhase(cut_dim), a position, with a velocity cut value
+    set_error("nbk_fof_criterion: runs on physical and phase-space trees");
+    return NBK_ERR_UNSUPPORTED;
   }
   double p[8];
   if (t->dev()) NBK_CUDA_TRY(cudaMemcpy(p, params, sizeof(p), cudaMemcpyDeviceToHost));
@@ -1323,7 +1520,7 @@ static int fof_nn_common(nbk_tree* t, int comparator, const double* params, int 
 int nbk_fof_nn_criterion(nbk_tree* t, int comparator, const double* params, int numnn,
                          const int32_t* nn, int32_t minnum, int32_t* group, int32_t* ngroup) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_fof_nn_criterion"));
   return fof_nn_common(t, comparator, params, numnn, nn, nullptr, 0, nullptr, minnum, group,
                        ngroup);
   API_END
@@ -1334,7 +1531,7 @@ int nbk_fof_nn_dist_criterion(nbk_tree* t, int comparator, const double* params,
                               const int32_t* pidx, int32_t minnum, int32_t* group,
                               int32_t* ngroup) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_fof_nn_dist_criterion"));
   return fof_nn_common(t, comparator, params, numnn, nn, values, npc, pidx, minnum, group,
                        ngroup);
   API_END
@@ -1343,7 +1540,7 @@ int nbk_fof_nn_dist_criterion(nbk_tree* t, int comparator, const double* params,
 int nbk_density_adjoint(nbk_tree* t, int k, const double* w, double* rho, double* grad_pos,
                         double* grad_mass) {
   API_BEGIN
-  NBK_TRY(check_tree(t));
+  NBK_TRY(check_phys(t, "nbk_density_adjoint"));
   if (!w || !rho || !grad_pos || !grad_mass || k < 1) {
     set_error("nbk_density_adjoint: invalid argument");
     return NBK_ERR_INVALID;

@@ -419,6 +419,88 @@ __global__ void __launch_bounds__(128) k_crit_link(FofArgs a) {
   }
 }
 
+// FOFCriterion on a phase-space tree (KDFOF.cxx:157-265 with FOFSearchCriterion[Periodic],
+// KDSplitNode.cxx:991-1030, 1649-1682, KDLeafNode.cxx:591-619): every particle walks the
+// tree with the reference's reachability rule (the farther child when the offset sum,
+// scaled per cut dimension by 1/params[1] or 1/params[2], stays below 1) and unites with
+// each particle the comparator accepts. The reference's breadth-first grouping equals
+// these connected components when each comparator's linking region lies inside the search
+// region, so that every link is found from both of its ends.
+__global__ void __launch_bounds__(128) k_crit_link6(FofArgs a) {
+  const TreeView& tv = a.tv;
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= tv.n) return;
+  const int self = tv.pstart + q;
+  const P4 me = tv.pos[self];
+  const V4 mv = tv.vel[self];
+  const double x0[6] = {me.x, me.y, me.z, mv.x, mv.y, mv.z};
+  const NodeS* N = tv.nodes6 + tv.nbase;
+  int npass = (tv.periodic && N[0].split_dim >= 0) ? 8 : 1;
+  for (int pass = 0; pass < npass; pass++) {
+    double x[6];
+    reflect(x0, x, tv.period, kImageMask[pass]);  // ungated (KDSplitNode.cxx:1649-1681)
+    x[3] = x0[3];
+    x[4] = x0[4];
+    x[5] = x0[5];
+    double off[6] = {0, 0, 0, 0, 0, 0};
+    double rd_at[kPhDepth], old_at[kPhDepth];
+    int h = 0, depth = 0, prev = -1;
+    bool down = true;
+    rd_at[0] = 0.0;
+    while (true) {
+      const NodeS nd = N[h];
+      if (down && nd.split_dim < 0) {
+        for (int i = nd.start; i < nd.start + nd.count; i++) {
+          if (i == self) continue;
+          if (crit_cmp(a.cmp, a.params, x, mv, tv.pos[i], tv.vel[i])) unite(a.parent, self, i, a.err);
+        }
+        if (h == 0) break;
+        prev = h;
+        h = (h - 1) >> 1;
+        depth--;
+        down = false;
+        continue;
+      }
+      const int cd = nd.split_dim;
+      const double new_off = dsub(get6(x, cd), nd.split_val);
+      const int nearh = new_off < 0 ? 2 * h + 1 : 2 * h + 2;
+      const int farh = new_off < 0 ? 2 * h + 2 : 2 * h + 1;
+      if (down) {
+        if (depth + 1 >= kPhDepth) {
+          atomicExch(a.err, kErrCapacity);
+          return;
+        }
+        rd_at[depth + 1] = rd_at[depth];
+        prev = h;
+        h = nearh;
+        depth++;
+        continue;
+      }
+      if (prev == nearh) {
+        const double old = get6(off, cd);
+        const double rdf = dadd(rd_at[depth], dmul(dadd(dmul(-old, old), dmul(new_off, new_off)),
+                                                   crit_invscaling(a.params, cd)));
+        if (rdf < 1.0) {
+          old_at[depth] = old;
+          set6(off, cd, new_off);
+          rd_at[depth + 1] = rdf;
+          prev = h;
+          h = farh;
+          depth++;
+          down = true;
+          continue;
+        }
+      } else {
+        set6(off, cd, old_at[depth]);
+      }
+      if (h == 0) break;
+      prev = h;
+      h = (h - 1) >> 1;
+      depth--;
+    }
+  }
+}
+
 // Point every particle straight at its root (between phases: no unions in flight).
 __global__ void k_compress(int* parent, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -576,6 +658,9 @@ int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tr
   if (a.crit == 2) {
     Phase ph("fof_nn_link", st);
     k_nn_link<<<(n + 255) / 256, 256, 0, st>>>(a); note_launch();
+  } else if (a.crit && a.tv.nodes6) {
+    Phase ph("fof_criterion_link", st);
+    k_crit_link6<<<(n + 127) / 128, 128, 0, st>>>(a); note_launch();
   } else if (a.crit) {
     Phase ph("fof_criterion_link", st);
     k_crit_link<<<(n + 127) / 128, 128, 0, st>>>(a); note_launch();

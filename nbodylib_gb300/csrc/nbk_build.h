@@ -30,8 +30,10 @@ struct BuiltArrays {
   float4* posf = nullptr;
   V4* vel = nullptr;
   int* perm = nullptr;
-  NodeRec* node = nullptr;
+  NodeRec* node = nullptr;    // physical / velocity trees
   NodeX* nodex = nullptr;
+  NodeS* nodes6 = nullptr;    // phase-space trees
+  NodeB6* nodeb6 = nullptr;
 };
 
 // Stream-ordered device allocations. Scratch allocations made through get() are freed
@@ -50,12 +52,18 @@ void dev_free(void* p, cudaStream_t st);
 
 int64_t heap_slots(int64_t n, int b);
 int64_t count_nodes(int64_t n, int b);
-size_t local_build_smem();
+size_t local_build_smem(int nd = 3);
 // Builds every tree of the forest; if root_out is given, the first tree's root node
 // (exact bounding box) is copied there before the build's final synchronisation.
 int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_in,
                  const double* d_mass_in, const double* d_vel_in, BuiltArrays& out,
                  DevAlloc& alloc, cudaStream_t st, NodeX* root_out = nullptr);
+// The phase-space tree (KDTree with TreeType TPHS): the same rules over the six
+// coordinates (x, y, z, vx, vy, vz); d_vel_in is required. Fills pos, posf, vel, perm,
+// nodes6 and nodeb6; root_out receives the root's exact box.
+int build_forest_phase(const std::vector<TreeSpec>& trees, int b, const double* d_pos_in,
+                       const double* d_mass_in, const double* d_vel_in, BuiltArrays& out,
+                       DevAlloc& alloc, cudaStream_t st, NodeB6* root_out = nullptr);
 
 // ---- kNN family
 enum Epi : int {
@@ -91,6 +99,21 @@ struct KnnArgs {
   int* err;
 };
 int launch_knn(const KnnArgs& a, int epi, cudaStream_t st);
+
+// ---- phase-space trees (phase.cu)
+enum PhaseEpi : int {
+  kPhNN = 0,        // FindNearest(tt) / FindNearest(x): neighbour lists
+  kPhDensity = 1,   // CalcDensity scatter (tree order)
+  kPhDensPart = 2,  // CalcDensityParticle (query order)
+};
+struct PhaseArgs {
+  KnnArgs k;             // queries (qmode 0 / 1 with 6 values per point / 2), heap, outputs;
+                         // k.periodic: search the position images (ungated)
+  int metric;            // 1: local metric (Aniso 0), 0: plain phase distance (Aniso -1)
+  int spacing_periodic;  // the metric spacing searches the images (FindNearest's copy)
+  int epi;               // PhaseEpi
+};
+int launch_phase(const PhaseArgs& a, cudaStream_t st);
 
 // ---- SPH smoothing over the nearest neighbours (smooth.cu)
 enum Smooth : int {

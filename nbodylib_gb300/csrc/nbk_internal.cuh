@@ -50,6 +50,19 @@ struct NodeX {
   int pad;
 };
 
+// Phase-space (six-dimensional) tree nodes, heap-indexed like the physical ones: the
+// split record the searches walk and the exact bounding box, in separate arrays.
+struct NodeS {
+  double split_val;  // coordinate of the median particle along split_dim (cut_val)
+  int split_dim;     // 0-2 position, 3-5 velocity; -1 for a leaf
+  int start;         // first particle (tree index, absolute)
+  int count;         // particles in the node; 0 marks an unused heap slot
+  int pad;
+};
+struct NodeB6 {
+  double lo[6], hi[6];
+};
+
 // Device view of one tree (or of one tree of a batch).
 struct TreeView {
   const P4* pos;
@@ -58,6 +71,7 @@ struct TreeView {
   const int* perm;
   const NodeRec* node;
   const NodeX* nodex;
+  const NodeS* nodes6;  // phase-space trees only (node/nodex are then unused)
   int n;       // particles in this tree
   int pstart;  // absolute tree index of its first particle
   int nbase;   // index of its root in the node arrays
@@ -249,6 +263,23 @@ __device__ __forceinline__ double wsm_line(double q, int size, double inv_delta,
   if (i < size - 1) return __fma_rn(img[2 * size + i], q, img[size + i]);
   return img[size - 1];
 }
+
+// ---- phase-space trees: depth bound of their per-thread walks, six-vector access
+constexpr int kPhDepth = 64;
+// v[d] of a six-vector indexed at run time (registers, no local memory)
+__device__ __forceinline__ double get6(const double v[6], int d) {
+  double r = v[0];
+#pragma unroll
+  for (int k = 1; k < 6; k++)
+    if (d == k) r = v[k];
+  return r;
+}
+__device__ __forceinline__ void set6(double v[6], int d, double x) {
+#pragma unroll
+  for (int k = 0; k < 6; k++)
+    if (d == k) v[k] = x;
+}
+
 
 // ---- device error word: kernels report bounded-wait and capacity failures here
 enum DeviceErr : int {

@@ -1,0 +1,377 @@
+// Searches over a phase-space tree (KDTree with TreeType TPHS): the six coordinates
+// (x, y, z, vx, vy, vz) of every particle, a tree split over all six.
+//
+// Replaces, for such trees:
+//   FindNearest(tt) / FindNearest(x)        src/KDTree/KDFindNearest.cxx:247-310, 460-507
+//   CalculateMetricSpacing                  KDFindNearest.cxx:34-105 (FindNearest's copy,
+//                                           periodic-aware) and KDCalcSmoothQuantities.cxx:
+//                                           17-56 (the densities' copy, never periodic)
+//   SplitNode/LeafNode::FindNearestPhase    KDSplitNode.cxx:69-95, 260-296; KDLeafNode.cxx:43-56,
+//                                           143-161
+//   SplitNode/LeafNode::FindNearestMetric   KDSplitNode.cxx:96-121, 303-331; KDLeafNode.cxx:58-71,
+//                                           168-179
+//   FindNearestPhasePeriodic / ...MetricPeriodic  KDSplitNode.cxx:1085-1097, 1153-1218
+//   CalcDensity / CalcDensityParticle       KDCalcSmoothQuantities.cxx:203-305, 768-843
+//
+// The local-metric search (the reference's default, Aniso = 0) scales the distance at the
+// leaves by a per-query metric but prunes with the unscaled incremental offset, so its
+// result is not the exact nearest-neighbour set and depends on the order in which the
+// tree is walked. Each query is therefore one thread that walks the tree in exactly the
+// reference's depth-first order (nearer child first; the farther child opened when the
+// FP64 offset sum, rounded as the reference rounds it, is below the heap top at that
+// moment) with the same bounded max-heap, which reproduces the reference's neighbour
+// sets. The walk is stackless over the heap-indexed nodes (the parent of h is (h-1)/2);
+// per depth it keeps the offset sum and the overwritten offset. The plain phase-space
+// search (Aniso = -1) is exact and runs through the same walk.
+#include "nbk_build.h"
+
+namespace nbk {
+namespace {
+
+// Per-thread bounded max-heap in shared memory, one column per thread.
+template <int KMAX, int NT>
+struct PhHeap {
+  double d[KMAX][NT];
+  int i[KMAX][NT];
+};
+
+// Replace the root (the largest entry) with (d, j) and restore the heap of size K.
+template <int KMAX, int NT>
+__device__ __forceinline__ void ph_replace_top(PhHeap<KMAX, NT>& H, int t, int K, double d,
+                                               int j) {
+  int pos = 0;
+  while (true) {
+    int c = 2 * pos + 1;
+    if (c >= K) break;
+    double dc = H.d[c][t];
+    if (c + 1 < K) {
+      double dc2 = H.d[c + 1][t];
+      if (dc2 > dc) {
+        c = c + 1;
+        dc = dc2;
+      }
+    }
+    if (d >= dc) break;
+    H.d[pos][t] = dc;
+    H.i[pos][t] = H.i[c][t];
+    pos = c;
+  }
+  H.d[pos][t] = d;
+  H.i[pos][t] = j;
+}
+
+template <int KMAX, int NT>
+__device__ __forceinline__ void ph_fill(PhHeap<KMAX, NT>& H, int t, int K) {
+  for (int s = 0; s < K; s++) {
+    H.d[s][t] = kMaxValue;
+    H.i[s][t] = -1;
+  }
+}
+
+// PhaseDistSqd (DistFunc.h:41-49): ((((dx^2 + dy^2) + dz^2) + dvx^2) + dvy^2) + dvz^2.
+__device__ __forceinline__ double phase_d2(const double x[6], const P4& p, const V4& v) {
+  double a = dsub(x[0], p.x), b = dsub(x[1], p.y), c = dsub(x[2], p.z);
+  double e = dsub(x[3], v.x), f = dsub(x[4], v.y), g = dsub(x[5], v.z);
+  double s = dadd(dmul(a, a), dmul(b, b));
+  s = dadd(s, dmul(c, c));
+  s = dadd(s, dmul(e, e));
+  s = dadd(s, dmul(f, f));
+  return dadd(s, dmul(g, g));
+}
+// MetricDistSqd (DistFunc.h:58-65): total += (metric[i] * d) * d from 0, dimension order.
+__device__ __forceinline__ double metric_d2(const double x[6], const P4& p, const V4& v,
+                                            const double m[6]) {
+  const double y[6] = {p.x, p.y, p.z, v.x, v.y, v.z};
+  double total = 0.0;
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    double d = dsub(x[k], y[k]);
+    total = dadd(total, dmul(dmul(m[k], d), d));
+  }
+  return total;
+}
+
+// One depth-first walk of the reference's search from x (a phase-space point). metric:
+// the local metric, or nullptr for the plain phase distance. target: a tree index the
+// leaves skip (the target forms), or -1. need_pos: leaves accept only distances > 0.
+// top: the heap's largest entry, kept current.
+template <int KMAX, int NT>
+__device__ void ph_walk(const TreeView& tv, PhHeap<KMAX, NT>& H, int t, int K, const double x[6],
+                        const double* metric, int target, bool need_pos, double& top, int* err) {
+  double m[6] = {1, 1, 1, 1, 1, 1};
+  if (metric)
+#pragma unroll
+    for (int k = 0; k < 6; k++) m[k] = metric[k];
+  double off[6] = {0, 0, 0, 0, 0, 0};
+  double rd_at[kPhDepth], old_at[kPhDepth];
+  const NodeS* N = tv.nodes6 + tv.nbase;
+  int h = 0, depth = 0, prev = -1;
+  bool down = true;
+  rd_at[0] = 0.0;
+  while (true) {
+    const NodeS nd = N[h];
+    if (down && nd.split_dim < 0) {  // a leaf: test its particles in tree order
+      for (int i = nd.start; i < nd.start + nd.count; i++) {
+        if (i == target) continue;
+        P4 p = tv.pos[i];
+        V4 v = tv.vel[i];
+        double d2 = metric ? metric_d2(x, p, v, m) : phase_d2(x, p, v);
+        if (d2 < top && (!need_pos || d2 > 0)) {
+          ph_replace_top<KMAX, NT>(H, t, K, d2, i);
+          top = H.d[0][t];
+        }
+      }
+      if (h == 0) break;
+      prev = h;
+      h = (h - 1) >> 1;
+      depth--;
+      down = false;
+      continue;
+    }
+    const int cd = nd.split_dim;
+    const double new_off = dsub(get6(x, cd), nd.split_val);
+    const int nearh = new_off < 0 ? 2 * h + 1 : 2 * h + 2;
+    const int farh = new_off < 0 ? 2 * h + 2 : 2 * h + 1;
+    if (down) {  // the nearer child first, with the same offset sum
+      if (depth + 1 >= kPhDepth) {
+        atomicExch(err, kErrCapacity);
+        return;
+      }
+      rd_at[depth + 1] = rd_at[depth];
+      prev = h;
+      h = nearh;
+      depth++;
+      continue;
+    }
+    if (prev == nearh) {
+      // back from the nearer child: rd += -old_off*old_off + new_off*new_off, and the
+      // farther child is opened when rd < top
+      const double old = get6(off, cd);
+      const double rdf = dadd(rd_at[depth], dadd(dmul(-old, old), dmul(new_off, new_off)));
+      if (rdf < top) {
+        old_at[depth] = old;
+        set6(off, cd, new_off);
+        rd_at[depth + 1] = rdf;
+        prev = h;
+        h = farh;
+        depth++;
+        down = true;
+        continue;
+      }
+    } else {
+      set6(off, cd, old_at[depth]);  // back from the farther child: restore the offset
+    }
+    if (h == 0) break;
+    prev = h;
+    h = (h - 1) >> 1;
+    depth--;
+  }
+}
+
+// The coordinate search around x with the seven position images of a periodic tree, no
+// gate (FindNearestPhasePeriodic / FindNearestMetricPeriodic, KDSplitNode.cxx:1153-1218);
+// a tree that is one leaf searches x alone (KDLeafNode.cxx:666-679, 708-711, 725-728).
+template <int KMAX, int NT>
+__device__ void ph_walk_images(const TreeView& tv, PhHeap<KMAX, NT>& H, int t, int K,
+                               const double x[6], const double* metric, bool need_pos,
+                               bool periodic, double& top, int* err) {
+  ph_walk<KMAX, NT>(tv, H, t, K, x, metric, -1, need_pos, top, err);
+  if (!periodic || tv.nodes6[tv.nbase].split_dim < 0) return;
+  for (int pass = 1; pass < 8; pass++) {
+    double xp[6];
+    reflect(x, xp, tv.period, kImageMask[pass]);
+    xp[3] = x[3];
+    xp[4] = x[4];
+    xp[5] = x[5];
+    ph_walk<KMAX, NT>(tv, H, t, K, xp, metric, -1, need_pos, top, err);
+  }
+}
+
+// CalculateMetricSpacing: the 8 nearest in plain phase space around x (a particle at x
+// itself included); the six direct offsets to the second nearest (or the next one whose
+// offsets are all non-zero) give metric[j] = 1/sr0[j]^2. Uses the first 8 heap rows.
+template <int KMAX, int NT>
+__device__ bool ph_metric_spacing(const TreeView& tv, PhHeap<KMAX, NT>& H, int t,
+                                  const double x[6], bool periodic, double metric[6], int* err) {
+  ph_fill<KMAX, NT>(H, t, 8);
+  double top = kMaxValue;
+  ph_walk_images<KMAX, NT>(tv, H, t, 8, x, nullptr, false, periodic, top, err);
+  // the reference pops the heap into ID[7..0]: ID ascending by distance
+  double d[8];
+  int id[8];
+  for (int s = 0; s < 8; s++) {
+    d[s] = H.d[s][t];
+    id[s] = H.i[s][t];
+  }
+  for (int a = 1; a < 8; a++)
+    for (int b = a; b > 0 && d[b] < d[b - 1]; b--) {
+      double td = d[b];
+      d[b] = d[b - 1];
+      d[b - 1] = td;
+      int ti = id[b];
+      id[b] = id[b - 1];
+      id[b - 1] = ti;
+    }
+  if (id[0] < 0) return false;  // fewer than 8 particles (the reference exits)
+  double sr0[6] = {0, 0, 0, 0, 0, 0};
+  double kvol = 0.0;
+  for (int ivol = 1; kvol == 0.0 && ivol < 8; ivol++) {
+    P4 p = tv.pos[id[ivol]];
+    V4 v = tv.vel[id[ivol]];
+    const double y[6] = {p.x, p.y, p.z, v.x, v.y, v.z};
+    kvol = 1.0;
+#pragma unroll
+    for (int j = 0; j < 6; j++) {
+      sr0[j] = fabs(dsub(y[j], x[j]));
+      kvol = dmul(kvol, sr0[j]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 6; j++) metric[j] = __ddiv_rn(1.0, dmul(sr0[j], sr0[j]));
+  return true;
+}
+
+template <int KMAX, int NT>
+__global__ void __launch_bounds__(NT) k_phase(PhaseArgs pa) {
+  const KnnArgs& a = pa.k;
+  const TreeView& tv = a.tv;
+  extern __shared__ __align__(16) unsigned char smem[];
+  PhHeap<KMAX, NT>& H = *reinterpret_cast<PhHeap<KMAX, NT>*>(smem);
+  const int t = threadIdx.x;
+  const int q = blockIdx.x * NT + t;
+  if (q >= a.nq) return;
+  // the query: a tree particle (qmode 0: q0 + q; 2: qidx[q]) or a phase-space point
+  int self = -1;
+  double x[6];
+  if (a.qmode == 1) {
+#pragma unroll
+    for (int j = 0; j < 6; j++) x[j] = a.qx[6 * (size_t)q + j];
+  } else {
+    int ti = a.qmode == 0 ? a.q0 + q : a.qidx[q];
+    if (ti < 0 || ti >= tv.n) {
+      atomicExch(a.err, kErrTarget);
+      return;
+    }
+    self = tv.pstart + ti;
+    P4 p = tv.pos[self];
+    V4 v = tv.vel[self];
+    x[0] = p.x;
+    x[1] = p.y;
+    x[2] = p.z;
+    x[3] = v.x;
+    x[4] = v.y;
+    x[5] = v.z;
+  }
+  const int K = a.kheap;
+  const bool periodic = a.periodic != 0;
+  double metric[6];
+  if (pa.metric && !ph_metric_spacing<KMAX, NT>(tv, H, t, x, pa.spacing_periodic != 0, metric,
+                                                a.err)) {
+    atomicExch(a.err, kErrTooFew);
+    return;
+  }
+  const double* mp = pa.metric ? metric : nullptr;
+  ph_fill<KMAX, NT>(H, t, K);
+  double top = kMaxValue;
+  if (self >= 0 && !periodic) {
+    // the target forms: the target itself and distance 0 are skipped
+    ph_walk<KMAX, NT>(tv, H, t, K, x, mp, self, true, top, a.err);
+  } else {
+    // the coordinate forms (also a periodic target search): the local metric skips
+    // distance 0, the plain distance skips nothing
+    ph_walk_images<KMAX, NT>(tv, H, t, K, x, mp, pa.metric != 0, periodic, top, a.err);
+  }
+  if (pa.epi == kPhNN) {
+    // LoadNN: the heap popped into rows [kout-1 .. 0]; a heap of kout + 1 drops its nearest
+    double d[KMAX];
+    int id[KMAX];
+    for (int s = 0; s < K; s++) {
+      d[s] = H.d[s][t];
+      id[s] = H.i[s][t];
+    }
+    for (int s = 1; s < K; s++)
+      for (int b = s; b > 0 && d[b] < d[b - 1]; b--) {
+        double td = d[b];
+        d[b] = d[b - 1];
+        d[b - 1] = td;
+        int ti = id[b];
+        id[b] = id[b - 1];
+        id[b - 1] = ti;
+      }
+    const int skip = K - a.kout;
+    for (int s = 0; s < a.kout; s++) {
+      int j = id[skip + s];
+      a.nn[(size_t)q * a.kout + s] = j >= 0 ? j - tv.pstart : -1;
+      a.d2[(size_t)q * a.kout + s] = d[skip + s];
+    }
+    return;
+  }
+  // CalcDensity / CalcDensityParticle: h = 0.5 sqrt(top), norm = h^-6 times the product
+  // of sqrt(metric[j]) (KDCalcSmoothQuantities.cxx:251-270)
+  for (int s = 0; s < K; s++)
+    if (H.i[s][t] < 0) {
+      atomicExch(a.err, kErrTooFew);
+      return;
+    }
+  const double hh = dmul(0.5, __dsqrt_rn(top));
+  const double ih = __ddiv_rn(1.0, hh);
+  const double ih2 = dmul(ih, ih);
+  double norm = dmul(dmul(ih2, ih2), ih2);
+  if (pa.metric) {
+    double temp = 1.0;
+#pragma unroll
+    for (int j = 0; j < 6; j++) temp = dmul(temp, __dsqrt_rn(metric[j]));
+    norm = dmul(norm, temp);
+  }
+  const int kr = a.kernres;
+  const double inv_delta = 0.5 * (double)(kr - 1);
+  const bool scatter = pa.epi == kPhDensity;
+  const double wnorm = scatter ? dmul(0.5, norm) : norm;
+  const double mi = tv.pos[self].m;
+  double acc = 0.0;
+  for (int s = 0; s < K; s++) {
+    const int j = H.i[s][t];
+    const double rij = __dsqrt_rn(H.d[s][t]);
+    const double w = dmul(wsm_line(__ddiv_rn(rij, hh), kr, inv_delta, a.kernel), wnorm);
+    const double mj = tv.pos[j].m;
+    acc = dadd(acc, dmul(w, mj));
+    if (scatter) atomicAdd(&a.rho[j - tv.pstart], dmul(w, mi));
+  }
+  if (scatter) atomicAdd(&a.rho[self - tv.pstart], acc);
+  else a.rho[q] = acc;
+}
+
+template <int KMAX, int NT>
+int launch_phase_t(const PhaseArgs& pa, cudaStream_t st) {
+  size_t sm = sizeof(PhHeap<KMAX, NT>);
+  static bool attr_set = false;
+  if (!attr_set) {
+    NBK_CUDA_TRY(cudaFuncSetAttribute(k_phase<KMAX, NT>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    attr_set = true;
+  }
+  unsigned blocks = (unsigned)((pa.k.nq + NT - 1) / NT);
+  k_phase<KMAX, NT><<<blocks, NT, sm, st>>>(pa);
+  note_launch();
+  NBK_CUDA_TRY(cudaGetLastError());
+  return NBK_OK;
+}
+
+}  // namespace
+
+int launch_phase(const PhaseArgs& pa, cudaStream_t st) {
+  if (pa.k.nq <= 0) return NBK_OK;
+  Phase ph(pa.epi == kPhNN ? "phase_knn" : "phase_density", st);
+  int K = pa.k.kheap;
+  if (K < 1 || K > 128 || pa.k.kout > K) {
+    set_error("phase-space search: heap size must be in [1, 128]");
+    return NBK_ERR_UNSUPPORTED;
+  }
+  // heaps hold at least the 8 entries of the metric spacing
+  if (K <= 16) return launch_phase_t<16, 256>(pa, st);
+  if (K <= 32) return launch_phase_t<32, 128>(pa, st);
+  if (K <= 64) return launch_phase_t<64, 64>(pa, st);
+  return launch_phase_t<128, 32>(pa, st);
+}
+
+}  // namespace nbk

@@ -56,6 +56,8 @@ class KDTree:
                 np.broadcast_to(np.asarray(period, np.float64), (3,)))
             args = [pos, vel, mass]
         self._keep = (args, per)
+        self.treetype = treetype
+        self.nd = 6 if treetype == TPHS else 3
         self.periodic = period is not None
         self.bucket_size = bucket_size
         self.kernres = max(100, kernres)
@@ -147,6 +149,27 @@ class KDTree:
         d2 = self._empty((nq, k), np.float64)
         _capi.check(self._lib.nbk_knn_points(self._h, _ptr(x), nq, k, periodic_mode, _ptr(nn),
                                              _ptr(d2)))
+        return nn, d2
+
+    def FindNearestTargets(self, targets, k, variant=FINDNEAREST, periodic_mode=PERIODIC_REF):
+        """FindNearest(tt) / FindNearestPos(tt) for the given tree indices: row i belongs
+        to targets[i]."""
+        targets = self._targets(targets)
+        nn = self._empty((len(targets), k), np.int32)
+        d2 = self._empty((len(targets), k), np.float64)
+        _capi.check(self._lib.nbk_knn_targets(self._h, _ptr(targets), len(targets), k, variant,
+                                              periodic_mode, _ptr(nn), _ptr(d2)))
+        return nn, d2
+
+    def FindNearestPoints(self, x, k):
+        """FindNearest(Double_t *x) for every row of x, in the tree's own space: 3 positions
+        (physical tree), 3 velocities (velocity tree) or x, y, z, vx, vy, vz (phase space)."""
+        if not self.device:
+            x = np.ascontiguousarray(x, np.float64).reshape(-1, self.nd)
+        nq = x.shape[0]
+        nn = self._empty((nq, k), np.int32)
+        d2 = self._empty((nq, k), np.float64)
+        _capi.check(self._lib.nbk_knn_coords(self._h, _ptr(x), nq, k, _ptr(nn), _ptr(d2)))
         return nn, d2
 
     # ---- SPH (KDTree.h:407-425)
