@@ -423,6 +423,55 @@ def components(args, lib):
         "phase_ms": {kk: round(v, 4) for kk, v in pha.items()},
         "target": "backward <= 2x forward",
     }
+    del dpos, dmass, w
+
+    # phase-space tree (TreeType TPHS) on the 2^20 clustered particles with velocities:
+    # build + CalcDensity(32) with the local metric (the reference's default), and
+    # FindNearest(32) with the local metric and with the plain phase distance; every query
+    # walks the tree in the reference's order (the local-metric result depends on it)
+    pos, mass, vel = syn.clustered_box(N_FOF, BOX, seed=2, velocities=True)
+    dpos, dmass, dvel = (torch.from_numpy(a).cuda() for a in (pos, mass, vel))
+    from nbodylib_gb300.kdtree import TPHS
+
+    def phase_step():
+        t = KDTree(dpos, dvel, dmass, BUCKET, treetype=TPHS, kerntype=0, device=True)
+        t.CalcDensity(32)
+        t.sync()
+        t.close()
+
+    phase_step()
+    ph_ms = _timed(phase_step, reps, flush)
+    php = _trace(lib, phase_step)
+    res = {"n": N_FOF, "k": 32, "step_build_plus_density_ms": ph_ms,
+           "particles_per_s_step": N_FOF / (ph_ms / 1e3),
+           "phase_ms": {kk: round(v, 4) for kk, v in php.items()}}
+    for aniso, tag in ((0, "local_metric"), (-1, "plain")):
+        t = KDTree(dpos, dvel, dmass, BUCKET, treetype=TPHS, kerntype=0, aniso=aniso,
+                   device=True)
+        t.FindNearest(32)
+        t.sync()
+        knn_ms = _timed(lambda: (t.FindNearest(32), t.sync()), reps, flush)
+        res[f"findnearest_{tag}_ms"] = knn_ms
+        res[f"findnearest_{tag}_queries_per_s"] = N_FOF / (knn_ms / 1e3)
+        t.close()
+    if not args.no_cpu:
+        import oracle
+        oracle.build(ref=False)
+        threads = os.cpu_count() or 1
+        sub = np.arange(0, N_FOF, 64)
+        o = oracle.OracleTree(pos, vel, mass, BUCKET, 3, 0, 1000, None, backend="port",
+                              nthreads=threads)
+        x = np.concatenate([pos[sub], vel[sub]], 1)
+        t0 = time.perf_counter()
+        o.knn_coord(x, 32)
+        dt = time.perf_counter() - t0
+        o.close()
+        res["cpu_findnearest_local_metric"] = {
+            "queries_per_s": len(sub) / dt, "cores": threads, "kind": "port",
+            "sample": f"FindNearest(x) at {len(sub)} particles' own phase-space coordinates "
+                      "(every 64th), local metric, OpenMP over queries"}
+    out["phase_space_clustered_2pow20_k32"] = res
+    del dpos, dmass, dvel
     return out
 
 
@@ -481,8 +530,9 @@ def run_reference(args, world, rank):
 
 def profile_case(args):
     """A small case of one kernel family, device-resident, for ncu captures: the FOF step
-    (build + FOF) or the kNN-density step on args.n clustered particles, or the batched
-    density on a power-law group batch of about args.n particles."""
+    (build + FOF), the kNN-density step or the phase-space density step (build + CalcDensity
+    with the local metric) on args.n clustered particles, or the batched density on a
+    power-law group batch of about args.n particles."""
     import torch
 
     from nbodylib_gb300 import BatchedDensity, KDTree, _build
@@ -502,6 +552,17 @@ def profile_case(args):
         out = torch.empty(len(gm), dtype=torch.float64, device="cuda")
         for _ in range(args.steps):
             B.density(32, use_graph=True, out=out)
+        torch.cuda.synchronize()
+        return
+    if args.profile == "phase":
+        from nbodylib_gb300.kdtree import TPHS
+        pos, mass, vel = syn.clustered_box(n, box, seed=2, velocities=True)
+        dpos, dmass, dvel = (torch.from_numpy(a).cuda() for a in (pos, mass, vel))
+        for _ in range(args.steps):
+            t = KDTree(dpos, dvel, dmass, BUCKET, treetype=TPHS, kerntype=0, device=True)
+            t.CalcDensity(32)
+            t.sync()
+            t.close()
         torch.cuda.synchronize()
         return
     for _ in range(args.steps):
@@ -526,7 +587,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--profile", choices=["fof", "knn", "build", "batch", "adjoint"],
+    ap.add_argument("--profile", choices=["fof", "knn", "build", "batch", "adjoint", "phase"],
                     help="run only `steps` steps of one small case (for ncu), print nothing")
     ap.add_argument("--n", type=int, default=1 << 18, help="particles for --profile")
     args = ap.parse_args()

@@ -258,6 +258,7 @@ struct nbk_tree {
     v.node = arr.node;
     v.nodex = arr.nodex;
     v.nodes6 = arr.nodes6;
+    v.nodeb6 = arr.nodeb6;
     v.n = (int)n;
     v.pstart = 0;
     v.nbase = 0;

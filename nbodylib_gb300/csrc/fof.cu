@@ -435,6 +435,15 @@ __global__ void __launch_bounds__(128) k_crit_link6(FofArgs a) {
   const V4 mv = tv.vel[self];
   const double x0[6] = {me.x, me.y, me.z, mv.x, mv.y, mv.z};
   const NodeS* N = tv.nodes6 + tv.nbase;
+  const NodeB6* B = tv.nodeb6 + tv.nbase;
+  // the comparator's weights per coordinate (FOFFunc.h:30-55): a subtree whose box bound
+  // in them is at or above 1 holds no particle the comparator accepts, so it is skipped
+  double w[6];
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    w[j] = a.cmp == 1 ? 0.0 : __ddiv_rd(1.0, a.params[6]);
+    w[3 + j] = a.cmp == 0 ? 0.0 : __ddiv_rd(1.0, a.params[a.cmp == 1 ? 6 : 7]);
+  }
   int npass = (tv.periodic && N[0].split_dim >= 0) ? 8 : 1;
   for (int pass = 0; pass < npass; pass++) {
     double x[6];
@@ -448,6 +457,14 @@ __global__ void __launch_bounds__(128) k_crit_link6(FofArgs a) {
     bool down = true;
     rd_at[0] = 0.0;
     while (true) {
+      if (down && box_lb6(x, w, B[h]) * kLbShrink >= 1.0) {
+        if (h == 0) break;
+        prev = h;
+        h = (h - 1) >> 1;
+        depth--;
+        down = false;
+        continue;
+      }
       const NodeS nd = N[h];
       if (down && nd.split_dim < 0) {
         for (int i = nd.start; i < nd.start + nd.count; i++) {

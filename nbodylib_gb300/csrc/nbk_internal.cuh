@@ -71,7 +71,8 @@ struct TreeView {
   const int* perm;
   const NodeRec* node;
   const NodeX* nodex;
-  const NodeS* nodes6;  // phase-space trees only (node/nodex are then unused)
+  const NodeS* nodes6;   // phase-space trees only (node/nodex are then unused)
+  const NodeB6* nodeb6;  // their exact bounding boxes
   int n;       // particles in this tree
   int pstart;  // absolute tree index of its first particle
   int nbase;   // index of its root in the node arrays
@@ -280,6 +281,24 @@ __device__ __forceinline__ void set6(double v[6], int d, double x) {
     if (d == k) v[k] = x;
 }
 
+
+// Lower bound of sum_j w[j] * (x[j] - y[j])^2 over the points y of the box [lo, hi] of a
+// phase-space node, rounded down. Any such sum the reference evaluates for a point of the
+// box (each difference, product and sum rounded to nearest, all terms non-negative) is at
+// least this bound times (1 - 1e-12), so a subtree whose bound times (1 - 1e-12) is at or
+// above a threshold holds no point that tests below it.
+__device__ __forceinline__ double box_lb6(const double x[6], const double w[6], const NodeB6& b) {
+  double s = 0.0;
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    double g = 0.0;
+    if (x[j] < b.lo[j]) g = __dsub_rd(b.lo[j], x[j]);
+    else if (x[j] > b.hi[j]) g = __dsub_rd(x[j], b.hi[j]);
+    s = __dadd_rd(s, __dmul_rd(__dmul_rd(w[j], g), g));
+  }
+  return s;
+}
+constexpr double kLbShrink = 1.0 - 1e-12;
 
 // ---- device error word: kernels report bounded-wait and capacity failures here
 enum DeviceErr : int {

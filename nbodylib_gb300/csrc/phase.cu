@@ -23,6 +23,13 @@
 // sets. The walk is stackless over the heap-indexed nodes (the parent of h is (h-1)/2);
 // per depth it keeps the offset sum and the overwritten offset. The plain phase-space
 // search (Aniso = -1) is exact and runs through the same walk.
+//
+// The walk skips every subtree whose particles provably cannot enter the heap: when the
+// distance bound of its bounding box (box_lb6, in the query's own metric) is at or above
+// the heap top, walking it would insert nothing and so leave the top, and with it every
+// later decision, unchanged. The reference's unscaled pruning opens far more of the tree
+// than the metric needs (the whole tree, for small velocity offsets), so this bound does
+// most of the pruning while the result stays the reference's.
 #include "nbk_build.h"
 
 namespace nbk {
@@ -105,10 +112,20 @@ __device__ void ph_walk(const TreeView& tv, PhHeap<KMAX, NT>& H, int t, int K, c
   double off[6] = {0, 0, 0, 0, 0, 0};
   double rd_at[kPhDepth], old_at[kPhDepth];
   const NodeS* N = tv.nodes6 + tv.nbase;
+  const NodeB6* B = tv.nodeb6 + tv.nbase;
   int h = 0, depth = 0, prev = -1;
   bool down = true;
   rd_at[0] = 0.0;
   while (true) {
+    if (down && box_lb6(x, m, B[h]) * kLbShrink >= top) {
+      // nothing in this subtree can enter the heap: as if walked, with no insertion
+      if (h == 0) break;
+      prev = h;
+      h = (h - 1) >> 1;
+      depth--;
+      down = false;
+      continue;
+    }
     const NodeS nd = N[h];
     if (down && nd.split_dim < 0) {  // a leaf: test its particles in tree order
       for (int i = nd.start; i < nd.start + nd.count; i++) {
