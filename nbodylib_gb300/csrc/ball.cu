@@ -69,7 +69,9 @@ __global__ void __launch_bounds__(32 * kWpb) k_ball(BallArgs a) {
   int cnt = 0;
   float thr = thresh_hi(a.r2), r2_lo = thresh_lo(a.r2);
   long long r2k = a.r2 > 0.0 ? dkey(a.r2) : 0;  // nothing is inside r2 <= 0 or NaN
-  float eps = tv.eps, two_eps = __fmul_ru(2.f, tv.eps);
+  // the query's own rounding bound, images included (it may lie outside the tree's box)
+  float eps = valid ? query_eps(tv, x0[0], x0[1], x0[2]) : tv.eps;
+  float two_eps = __fadd_ru(eps, tv.eps);
   int npass = tv.periodic ? 8 : 1;
   int near = 0;
   if (tv.periodic && valid)

@@ -111,15 +111,20 @@ template <>
 struct NodeOut<6> {
   NodeS* nodes;
   NodeB6* nodeb;
+  NodeF6* nodef;
   __device__ __forceinline__ void write(int idx, const double* lo, const double* hi, int start,
                                         int count, int dim, double split_val) const {
     NodeS r;
     NodeB6 x;
+    NodeF6 f;
 #pragma unroll
     for (int d = 0; d < 6; d++) {
       x.lo[d] = lo[d];
       x.hi[d] = hi[d];
+      f.lo[d] = __double2float_rd(lo[d]);
+      f.hi[d] = __double2float_ru(hi[d]);
     }
+    nodef[idx] = f;
     r.split_val = split_val;
     r.split_dim = dim;
     r.start = start;
@@ -712,6 +717,7 @@ struct PartOut {
   float4* posf;
   V4* vel;
   int* perm;
+  float4* velf;  // ND = 6 only
 };
 
 template <int ND>
@@ -974,6 +980,8 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_build(
     po.perm[t] = ii;
     if (ND == 6) {
       po.vel[t] = make_v4(cc[3 * K + q], cc[4 * K + q], cc[5 * K + q], 0.0);
+      po.velf[t] = make_float4(__double2float_rn(cc[3 * K + q]), __double2float_rn(cc[4 * K + q]),
+                               __double2float_rn(cc[5 * K + q]), 0.f);
     } else if (po.vel && vel_in) {
       po.vel[t] = make_v4(vel_in[3 * ii], vel_in[3 * ii + 1], vel_in[3 * ii + 2], 0.0);
     }
@@ -1223,7 +1231,7 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
                  const double* d_mass_in, const double* d_vel_in, BuiltArrays& out,
                  DevAlloc& alloc, cudaStream_t st, NodeX* root_out) {
   NodeOut<3> no{out.node, out.nodex};
-  PartOut<3> po{out.pos, out.posf, out.vel, out.perm};
+  PartOut<3> po{out.pos, out.posf, out.vel, out.perm, nullptr};
   const void* src = trees.empty() ? nullptr : (const void*)(out.nodex + trees[0].nbase);
   return build_forest_t<3>(trees, b, d_pos_in, d_mass_in, d_vel_in, no, po, alloc, st, root_out,
                            sizeof(NodeX), src);
@@ -1236,8 +1244,8 @@ int build_forest_phase(const std::vector<TreeSpec>& trees, int b, const double* 
     set_error("phase-space tree: velocities are required");
     return NBK_ERR_INVALID;
   }
-  NodeOut<6> no{out.nodes6, out.nodeb6};
-  PartOut<6> po{out.pos, out.posf, out.vel, out.perm};
+  NodeOut<6> no{out.nodes6, out.nodeb6, out.nodef6};
+  PartOut<6> po{out.pos, out.posf, out.vel, out.perm, out.velf};
   const void* src = trees.empty() ? nullptr : (const void*)(out.nodeb6 + trees[0].nbase);
   return build_forest_t<6>(trees, b, d_pos_in, d_mass_in, d_vel_in, no, po, alloc, st, root_out,
                            sizeof(NodeB6), src);

@@ -247,6 +247,7 @@ struct nbk_tree {
   double kernnorm = 0;
   double* d_kernel = nullptr;
   float eps = 0;
+  float eps6[6] = {0, 0, 0, 0, 0, 0};
   int* d_err = nullptr;
   bool dev() const { return flags & NBK_DEVICE_PTRS; }
   TreeView view() const {
@@ -259,6 +260,9 @@ struct nbk_tree {
     v.nodex = arr.nodex;
     v.nodes6 = arr.nodes6;
     v.nodeb6 = arr.nodeb6;
+    v.nodef6 = arr.nodef6;
+    v.velf = arr.velf;
+    for (int d = 0; d < 6; d++) v.eps6[d] = eps6[d];
     v.n = (int)n;
     v.pstart = 0;
     v.nbase = 0;
@@ -555,6 +559,8 @@ int nbk_create(const double* pos, const double* vel, const double* mass, int64_t
   if (treetype == NBK_TPHS) {
     NBK_TRY(dev_malloc((void**)&A.nodes6, sizeof(NodeS) * t->nslots, st));
     NBK_TRY(dev_malloc((void**)&A.nodeb6, sizeof(NodeB6) * t->nslots, st));
+    NBK_TRY(dev_malloc((void**)&A.nodef6, sizeof(NodeF6) * t->nslots, st));
+    NBK_TRY(dev_malloc((void**)&A.velf, sizeof(float4) * n, st));
     NBK_CUDA_TRY(cudaMemsetAsync(A.nodes6, 0, sizeof(NodeS) * t->nslots, st));
     NBK_CUDA_TRY(cudaMemsetAsync(A.nodeb6, 0, sizeof(NodeB6) * t->nslots, st));
   } else {
@@ -592,6 +598,12 @@ int nbk_create(const double* pos, const double* vel, const double* mass, int64_t
       rlo[d] = root.lo[d];
       rhi[d] = root.hi[d];
     }
+    // FP32 rounding bound per phase-space coordinate (position images included)
+    for (int d = 0; d < 6; d++) {
+      double m = std::max(std::fabs(root.lo[d]), std::fabs(root.hi[d])) +
+                 (d < 3 ? t->period[d] : 0.0);
+      t->eps6[d] = (float)std::ldexp(m, -23) * 1.0001f + 1e-38f;
+    }
   } else {
     // a velocity tree is the same tree over the velocities (FindNearestVel,
     // BoundaryandMeanVel, MedianVel): positions and velocities trade places on the device
@@ -626,6 +638,8 @@ int nbk_destroy(nbk_tree* t) {
   dev_free(t->arr.nodex, st);
   dev_free(t->arr.nodes6, st);
   dev_free(t->arr.nodeb6, st);
+  dev_free(t->arr.nodef6, st);
+  dev_free(t->arr.velf, st);
   // t->d_kernel belongs to the process-wide kernel cache
   dev_free(t->d_err, st);
   cudaStreamSynchronize(st);

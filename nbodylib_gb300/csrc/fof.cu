@@ -435,15 +435,19 @@ __global__ void __launch_bounds__(128) k_crit_link6(FofArgs a) {
   const V4 mv = tv.vel[self];
   const double x0[6] = {me.x, me.y, me.z, mv.x, mv.y, mv.z};
   const NodeS* N = tv.nodes6 + tv.nbase;
-  const NodeB6* B = tv.nodeb6 + tv.nbase;
-  // the comparator's weights per coordinate (FOFFunc.h:30-55): a subtree whose box bound
-  // in them is at or above 1 holds no particle the comparator accepts, so it is skipped
-  double w[6];
+  const NodeF6* F = tv.nodef6 + tv.nbase;
+  // the comparator's weights per coordinate (FOFFunc.h:30-55), rounded down: a subtree (or
+  // a particle) whose FP32 bound in them is at or above 1 + 2^-20 holds nothing the
+  // comparator accepts (its FP64 sum is >= 1), so it is skipped
+  float w[6], e32[6];
 #pragma unroll
   for (int j = 0; j < 3; j++) {
-    w[j] = a.cmp == 1 ? 0.0 : __ddiv_rd(1.0, a.params[6]);
-    w[3 + j] = a.cmp == 0 ? 0.0 : __ddiv_rd(1.0, a.params[a.cmp == 1 ? 6 : 7]);
+    w[j] = a.cmp == 1 ? 0.f : __double2float_rd(__ddiv_rd(1.0, a.params[6]));
+    w[3 + j] = a.cmp == 0 ? 0.f : __double2float_rd(__ddiv_rd(1.0, a.params[a.cmp == 1 ? 6 : 7]));
   }
+#pragma unroll
+  for (int j = 0; j < 6; j++) e32[j] = tv.eps6[j];
+  const float thr = 1.0f + 1.0f / 1048576.0f;
   int npass = (tv.periodic && N[0].split_dim >= 0) ? 8 : 1;
   for (int pass = 0; pass < npass; pass++) {
     double x[6];
@@ -451,13 +455,16 @@ __global__ void __launch_bounds__(128) k_crit_link6(FofArgs a) {
     x[3] = x0[3];
     x[4] = x0[4];
     x[5] = x0[5];
+    float q32[6];
+#pragma unroll
+    for (int j = 0; j < 6; j++) q32[j] = __double2float_rn(x[j]);
     double off[6] = {0, 0, 0, 0, 0, 0};
     double rd_at[kPhDepth], old_at[kPhDepth];
     int h = 0, depth = 0, prev = -1;
     bool down = true;
     rd_at[0] = 0.0;
     while (true) {
-      if (down && box_lb6(x, w, B[h]) * kLbShrink >= 1.0) {
+      if (down && box_lb6f(q32, w, e32, F[h]) >= thr) {
         if (h == 0) break;
         prev = h;
         h = (h - 1) >> 1;
@@ -469,6 +476,9 @@ __global__ void __launch_bounds__(128) k_crit_link6(FofArgs a) {
       if (down && nd.split_dim < 0) {
         for (int i = nd.start; i < nd.start + nd.count; i++) {
           if (i == self) continue;
+          const float4 pf = tv.posf[i], vf = tv.velf[i];
+          const float c[6] = {pf.x, pf.y, pf.z, vf.x, vf.y, vf.z};
+          if (pair_lb6f(q32, c, w, e32) >= thr) continue;
           if (crit_cmp(a.cmp, a.params, x, mv, tv.pos[i], tv.vel[i])) unite(a.parent, self, i, a.err);
         }
         if (h == 0) break;

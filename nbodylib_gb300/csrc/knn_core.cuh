@@ -72,7 +72,8 @@ __device__ void traverse(const TreeView& tv, WarpSmem<KMAX>& w, int lane, bool a
   const unsigned FULL = 0xffffffffu;
   float qx = __double2float_rn(xq[0]), qy = __double2float_rn(xq[1]),
         qz = __double2float_rn(xq[2]);
-  float eps = tv.eps, two_eps = __fmul_ru(2.f, tv.eps);
+  // the query's own rounding bound (it may lie outside the tree's box); candidates: tv.eps
+  float eps = query_eps(tv, xq[0], xq[1], xq[2]), two_eps = __fadd_ru(eps, tv.eps);
   long long topk = dkey(top);
   float thr = thresh_hi_bits(topk);
   int sp = 0;
@@ -173,8 +174,9 @@ __device__ double knn_search(const KnnArgs& a, const TreeView& tv, WarpSmem<KMAX
         float4 qf = make_float4(__double2float_rn(x0[0]), __double2float_rn(x0[1]),
                                 __double2float_rn(x0[2]), 0.f);
         float top_hi = thresh_hi_bits(dkey(top));
-        near_sq = near_walls(qf, tv.period, tv.eps, top_hi);
-        near_lin = near_walls_lin(qf, tv.period, tv.eps, top_hi);
+        float qeps = query_eps(tv, x0[0], x0[1], x0[2]);
+        near_sq = near_walls(qf, tv.period, qeps, top_hi);
+        near_lin = near_walls_lin(qf, tv.period, qeps, top_hi);
       }
       int m = kImageMask[pass];
       bool may = (m & ~((pass <= 3 || a.min_image) ? near_sq : near_lin)) == 0;

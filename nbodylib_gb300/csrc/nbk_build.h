@@ -34,6 +34,8 @@ struct BuiltArrays {
   NodeX* nodex = nullptr;
   NodeS* nodes6 = nullptr;    // phase-space trees
   NodeB6* nodeb6 = nullptr;
+  NodeF6* nodef6 = nullptr;
+  float4* velf = nullptr;
 };
 
 // Stream-ordered device allocations. Scratch allocations made through get() are freed
@@ -59,8 +61,8 @@ int build_forest(const std::vector<TreeSpec>& trees, int b, const double* d_pos_
                  const double* d_mass_in, const double* d_vel_in, BuiltArrays& out,
                  DevAlloc& alloc, cudaStream_t st, NodeX* root_out = nullptr);
 // The phase-space tree (KDTree with TreeType TPHS): the same rules over the six
-// coordinates (x, y, z, vx, vy, vz); d_vel_in is required. Fills pos, posf, vel, perm,
-// nodes6 and nodeb6; root_out receives the root's exact box.
+// coordinates (x, y, z, vx, vy, vz); d_vel_in is required. Fills pos, posf, vel, velf,
+// perm, nodes6, nodeb6 and nodef6; root_out receives the root's exact box.
 int build_forest_phase(const std::vector<TreeSpec>& trees, int b, const double* d_pos_in,
                        const double* d_mass_in, const double* d_vel_in, BuiltArrays& out,
                        DevAlloc& alloc, cudaStream_t st, NodeB6* root_out = nullptr);

@@ -62,6 +62,9 @@ struct NodeS {
 struct NodeB6 {
   double lo[6], hi[6];
 };
+struct __align__(16) NodeF6 {  // the same box in FP32, rounded outward
+  float lo[6], hi[6];
+};
 
 // Device view of one tree (or of one tree of a batch).
 struct TreeView {
@@ -73,6 +76,9 @@ struct TreeView {
   const NodeX* nodex;
   const NodeS* nodes6;   // phase-space trees only (node/nodex are then unused)
   const NodeB6* nodeb6;  // their exact bounding boxes
+  const NodeF6* nodef6;  // and the boxes in FP32
+  const float4* velf;    // vx, vy, vz rounded to nearest FP32 (phase-space trees)
+  float eps6[6];         // per coordinate: bound on |c - float(c)| (images included)
   int n;       // particles in this tree
   int pstart;  // absolute tree index of its first particle
   int nbase;   // index of its root in the node arrays
@@ -160,6 +166,15 @@ __device__ __forceinline__ float pair_d2_hi(float qx, float qy, float qz, float 
 __device__ __forceinline__ float thresh_hi(double t) {
   float f = __double2float_ru(t);
   return __fmul_ru(f, 1.0f + 1.0f / 1048576.0f);
+}
+
+// Bound on |c - float(c)| for the coordinates of a query at (x, y, z) and of its periodic
+// images: the tree-wide bound covers the tree's particles and their images, but a query
+// point may lie anywhere.
+__device__ __forceinline__ float query_eps(const TreeView& tv, double x, double y, double z) {
+  double m = fmax(fabs(x), fmax(fabs(y), fabs(z)));
+  m += fmax(tv.period[0], fmax(tv.period[1], tv.period[2]));
+  return fmaxf(tv.eps, __fmul_ru(__double2float_ru(m), 1.2e-7f));
 }
 
 // ---- integer forms for non-negative doubles (squared distances, |dv|). Their bit
@@ -299,6 +314,32 @@ __device__ __forceinline__ double box_lb6(const double x[6], const double w[6], 
   return s;
 }
 constexpr double kLbShrink = 1.0 - 1e-12;
+
+// FP32 lower bound of sum_j w[j] * gap_j^2 from a query known to within eps[j] of q[j] to
+// the FP32 box [lo, hi] (which contains the exact one); every operation rounds down.
+__device__ __forceinline__ float box_lb6f(const float q[6], const float w[6], const float eps[6],
+                                          const NodeF6& b) {
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    float g = fmaxf(0.f, fmaxf(__fsub_rd(b.lo[j], __fadd_ru(q[j], eps[j])),
+                               __fsub_rd(__fsub_rd(q[j], eps[j]), b.hi[j])));
+    s = __fadd_rd(s, __fmul_rd(__fmul_rd(w[j], g), g));
+  }
+  return s;
+}
+// FP32 lower bound of sum_j w[j] * (x_j - y_j)^2 for two points whose FP32 roundings q, c
+// are each within eps[j] of the exact coordinates.
+__device__ __forceinline__ float pair_lb6f(const float q[6], const float c[6], const float w[6],
+                                           const float eps[6]) {
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    float g = fmaxf(0.f, __fsub_rd(fabsf(__fsub_rz(q[j], c[j])), __fmul_ru(2.f, eps[j])));
+    s = __fadd_rd(s, __fmul_rd(__fmul_rd(w[j], g), g));
+  }
+  return s;
+}
 
 // ---- device error word: kernels report bounded-wait and capacity failures here
 enum DeviceErr : int {

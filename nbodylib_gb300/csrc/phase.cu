@@ -25,9 +25,10 @@
 // search (Aniso = -1) is exact and runs through the same walk.
 //
 // The walk skips every subtree whose particles provably cannot enter the heap: when the
-// distance bound of its bounding box (box_lb6, in the query's own metric) is at or above
-// the heap top, walking it would insert nothing and so leave the top, and with it every
-// later decision, unchanged. The reference's unscaled pruning opens far more of the tree
+// FP32 distance bound of its bounding box (box_lb6f, in the query's own metric, rounded
+// down) is at or above an FP32 value above the heap top, walking it would insert nothing
+// and so leave the top, and with it every later decision, unchanged. Leaf particles are
+// screened the same way (pair_lb6f) before their FP64 distance is computed. The reference's unscaled pruning opens far more of the tree
 // than the metric needs (the whole tree, for small velocity offsets), so this bound does
 // most of the pruning while the result stays the reference's.
 #include "nbk_build.h"
@@ -109,15 +110,25 @@ __device__ void ph_walk(const TreeView& tv, PhHeap<KMAX, NT>& H, int t, int K, c
   if (metric)
 #pragma unroll
     for (int k = 0; k < 6; k++) m[k] = metric[k];
+  // FP32 images of the query and of the metric (rounded down) for the bounds
+  float q32[6], w32[6], e32[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    q32[k] = __double2float_rn(x[k]);
+    w32[k] = metric ? __double2float_rd(m[k]) : 1.f;
+    // the query may lie outside the tree's box: its own rounding bound, if larger
+    e32[k] = fmaxf(tv.eps6[k], __fmul_ru(__double2float_ru(fabs(x[k])), 1.2e-7f));
+  }
+  float thr = thresh_hi_bits(dkey(top));  // FP32, above top by at least 2^-20 of it
   double off[6] = {0, 0, 0, 0, 0, 0};
   double rd_at[kPhDepth], old_at[kPhDepth];
   const NodeS* N = tv.nodes6 + tv.nbase;
-  const NodeB6* B = tv.nodeb6 + tv.nbase;
+  const NodeF6* F = tv.nodef6 + tv.nbase;
   int h = 0, depth = 0, prev = -1;
   bool down = true;
   rd_at[0] = 0.0;
   while (true) {
-    if (down && box_lb6(x, m, B[h]) * kLbShrink >= top) {
+    if (down && box_lb6f(q32, w32, e32, F[h]) >= thr) {
       // nothing in this subtree can enter the heap: as if walked, with no insertion
       if (h == 0) break;
       prev = h;
@@ -130,12 +141,16 @@ __device__ void ph_walk(const TreeView& tv, PhHeap<KMAX, NT>& H, int t, int K, c
     if (down && nd.split_dim < 0) {  // a leaf: test its particles in tree order
       for (int i = nd.start; i < nd.start + nd.count; i++) {
         if (i == target) continue;
+        const float4 pf = tv.posf[i], vf = tv.velf[i];
+        const float c[6] = {pf.x, pf.y, pf.z, vf.x, vf.y, vf.z};
+        if (pair_lb6f(q32, c, w32, e32) >= thr) continue;  // its FP64 distance is >= top
         P4 p = tv.pos[i];
         V4 v = tv.vel[i];
         double d2 = metric ? metric_d2(x, p, v, m) : phase_d2(x, p, v);
         if (d2 < top && (!need_pos || d2 > 0)) {
           ph_replace_top<KMAX, NT>(H, t, K, d2, i);
           top = H.d[0][t];
+          thr = thresh_hi_bits(dkey(top));
         }
       }
       if (h == 0) break;
