@@ -489,9 +489,10 @@ __global__ void __launch_bounds__(128) k_crit_link6(FofArgs a) {
         continue;
       }
       const int cd = nd.split_dim;
-      const double new_off = dsub(get6(x, cd), nd.split_val);
-      const int nearh = new_off < 0 ? 2 * h + 1 : 2 * h + 2;
-      const int farh = new_off < 0 ? 2 * h + 2 : 2 * h + 1;
+      const double xc = get6(x, cd);
+      const bool left_first = okey(xc) < okey(nd.split_val);  // new_off < 0
+      const int nearh = left_first ? 2 * h + 1 : 2 * h + 2;
+      const int farh = left_first ? 2 * h + 2 : 2 * h + 1;
       if (down) {
         if (depth + 1 >= kPhDepth) {
           atomicExch(a.err, kErrCapacity);
@@ -503,7 +504,10 @@ __global__ void __launch_bounds__(128) k_crit_link6(FofArgs a) {
         depth++;
         continue;
       }
-      if (prev == nearh) {
+      // a farther child that holds nothing the comparator accepts is passed over without
+      // the FP64 reachability test
+      if (prev == nearh && box_lb6f(q32, w, e32, F[farh]) < thr) {
+        const double new_off = dsub(xc, nd.split_val);
         const double old = get6(off, cd);
         const double rdf = dadd(rd_at[depth], dmul(dadd(dmul(-old, old), dmul(new_off, new_off)),
                                                    crit_invscaling(a.params, cd)));
@@ -517,7 +521,7 @@ __global__ void __launch_bounds__(128) k_crit_link6(FofArgs a) {
           down = true;
           continue;
         }
-      } else {
+      } else if (prev == farh) {
         set6(off, cd, old_at[depth]);
       }
       if (h == 0) break;

@@ -161,9 +161,11 @@ __device__ void ph_walk(const TreeView& tv, PhHeap<KMAX, NT>& H, int t, int K, c
       continue;
     }
     const int cd = nd.split_dim;
-    const double new_off = dsub(get6(x, cd), nd.split_val);
-    const int nearh = new_off < 0 ? 2 * h + 1 : 2 * h + 2;
-    const int farh = new_off < 0 ? 2 * h + 2 : 2 * h + 1;
+    const double xc = get6(x, cd);
+    // new_off = x - cut_val < 0 exactly when x < cut_val: an integer compare of order keys
+    const bool left_first = okey(xc) < okey(nd.split_val);
+    const int nearh = left_first ? 2 * h + 1 : 2 * h + 2;
+    const int farh = left_first ? 2 * h + 2 : 2 * h + 1;
     if (down) {  // the nearer child first, with the same offset sum
       if (depth + 1 >= kPhDepth) {
         atomicExch(err, kErrCapacity);
@@ -175,9 +177,12 @@ __device__ void ph_walk(const TreeView& tv, PhHeap<KMAX, NT>& H, int t, int K, c
       depth++;
       continue;
     }
-    if (prev == nearh) {
+    if (prev == nearh && box_lb6f(q32, w32, e32, F[farh]) < thr) {
       // back from the nearer child: rd += -old_off*old_off + new_off*new_off, and the
-      // farther child is opened when rd < top
+      // farther child is opened when rd < top (a farther child whose bound is above the
+      // top inserts nothing whether or not the reference opens it: it is passed over
+      // without this FP64 test)
+      const double new_off = dsub(xc, nd.split_val);
       const double old = get6(off, cd);
       const double rdf = dadd(rd_at[depth], dadd(dmul(-old, old), dmul(new_off, new_off)));
       if (rdf < top) {
@@ -190,7 +195,7 @@ __device__ void ph_walk(const TreeView& tv, PhHeap<KMAX, NT>& H, int t, int K, c
         down = true;
         continue;
       }
-    } else {
+    } else if (prev == farh) {
       set6(off, cd, old_at[depth]);  // back from the farther child: restore the offset
     }
     if (h == 0) break;
