@@ -11,7 +11,9 @@
 //            int32 ball count, ball IDs, double rho after the destructor (input order),
 //            n x 3 double CalcSmoothVel(32) with the stored densities (by ID),
 //            int32 ngroup_nn, n x int32 FOFNNCriterion(FOF3d, 16 lists) groups (by ID),
-//            n x double density after DensitySmooth(S, 16, 32) (input order)
+//            n x double density after DensitySmooth(S, 16, 32) (input order),
+//            phase-space tree (Aniso 0): n x 16 int32 FindNearest IDs, n x 16 double d2,
+//            n x double CalcDensity(16), int32 ngroup, n x int32 FOFCriterion(FOF6d)
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -100,6 +102,38 @@ int main(int argc, char** argv) {
     delete tree;
     for (int i = 0; i < n; i++) rho_smooth[i] = S[i].GetDensity();
   }
+  // a phase-space tree (TreeType TPHS, Aniso 0, the reference's default): FindNearest for
+  // every particle (the Int_t** form, rows by tree index), CalcDensity and
+  // FOFCriterion(FOF6d); the destructor restores input order again
+  std::vector<int> pnn((size_t)n * 16), pgroup(n);
+  std::vector<double> pd2((size_t)n * 16), prho(n);
+  int pngroup = 0;
+  {
+    KDTree ptree(parts.data(), n, 16, KDTree::TPHS, KDTree::KSPH, 1000, 0, 0, 0,
+                 periodic ? period : NULL);
+    std::vector<Int_t> flat((size_t)n * 16);
+    std::vector<Double_t> dflat((size_t)n * 16);
+    std::vector<Int_t*> r(n);
+    std::vector<Double_t*> dr(n);
+    for (int t = 0; t < n; t++) {
+      r[t] = &flat[(size_t)t * 16];
+      dr[t] = &dflat[(size_t)t * 16];
+    }
+    ptree.FindNearest(r.data(), dr.data(), 16);
+    for (int t = 0; t < n; t++) {
+      int id = parts[t].GetID();
+      for (int j = 0; j < 16; j++) {
+        pnn[(size_t)id * 16 + j] = parts[r[t][j]].GetID();
+        pd2[(size_t)id * 16 + j] = dr[t][j];
+      }
+    }
+    ptree.CalcDensity(16);
+    for (int t = 0; t < n; t++) prho[parts[t].GetID()] = parts[t].GetDensity();
+    Double_t par[20] = {(Double_t)KDTree::TPHS, 0.25, 0.04, 0, 0, 0, 0.25, 0.04};
+    Int_t* g6 = ptree.FOFCriterion(FOF6d, par, pngroup, 8);
+    for (int i = 0; i < n; i++) pgroup[i] = g6[i];
+    delete[] g6;
+  }
   FILE* o = fopen(argv[2], "wb");
   fwrite(&n, 4, 1, o);
   fwrite(&numnodes, 4, 1, o);
@@ -117,6 +151,11 @@ int main(int argc, char** argv) {
   fwrite(&ngroup_nn, 4, 1, o);
   fwrite(group_nn.data(), 4, n, o);
   fwrite(rho_smooth.data(), 8, n, o);
+  fwrite(pnn.data(), 4, (size_t)n * 16, o);
+  fwrite(pd2.data(), 8, (size_t)n * 16, o);
+  fwrite(prho.data(), 8, n, o);
+  fwrite(&pngroup, 4, 1, o);
+  fwrite(pgroup.data(), 4, n, o);
   fclose(o);
   printf("dropin ok: n=%d nodes=%d groups=%d\n", n, numnodes, ngroup);
   return 0;

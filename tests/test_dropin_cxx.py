@@ -94,6 +94,11 @@ def test_dropin_runs_like_the_reference(gpu, port_built, tmp_path, periodic):
     ngroup_nn = take(np.int32, 1)[0]
     group_nn = take(np.int32, n)
     rho_smooth = take(np.float64, n)
+    pnn = take(np.int32, n * 16).reshape(n, 16)
+    pd2 = take(np.float64, n * 16).reshape(n, 16)
+    prho = take(np.float64, n)
+    pngroup = take(np.int32, 1)[0]
+    pgroup = take(np.int32, n)
     per = [box] * 3 if periodic else None
     o = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, per, backend="port")
     assert nodes == o.num_nodes and leaves == o.num_leaves
@@ -120,3 +125,12 @@ def test_dropin_runs_like_the_reference(gpu, port_built, tmp_path, periodic):
     # DensitySmooth(S, 16, 32): System constructor (default Epanechnikov kernel, no period)
     rs = oracle.OracleTree(pos, vel, mass, 16, 0, 2, 1000, None, backend="port").density(32)
     assert_density_close(rho_smooth, rs, "drop-in DensitySmooth")
+    # phase-space tree with the local metric
+    mk6 = lambda: oracle.OracleTree(pos, vel, mass, 16, 3, 0, 1000, per, backend="port",
+                                    nthreads=8, aniso=0)
+    oi, od = mk6().knn(16, 0)
+    assert_knn_equal(pnn, pd2, oi, od, "drop-in phase-space FindNearest")
+    assert_density_close(prho, mk6().density(16), "drop-in phase-space CalcDensity")
+    g6, n6 = mk6().fof_criterion(2, [3, 0.25, 0.04, 0, 0, 0, 0.25, 0.04], 8, 0)
+    assert pngroup == n6
+    assert_same_partition(pgroup, g6, "drop-in phase-space FOFCriterion")
