@@ -160,3 +160,38 @@ def test_phase_and_velocity_trees_refuse_other_calls(gpu):
         KDTree(pos, vel, mass, 16, treetype=TVEL, period=[10.0] * 3)
     with pytest.raises(NbkError):
         KDTree(pos, vel, mass, 16, treetype=TPHS, aniso=1)
+
+
+@pytest.mark.parametrize("n,dup,per,k", [(12, 0, 5.0, 4), (12, 0, None, 4), (9, 0, 3.0, 3),
+                                         (300, 40, 10.0, 8), (300, 40, None, 8)])
+@pytest.mark.parametrize("aniso", [-1, 0])
+def test_phase_edge_cases_vs_restatement(gpu, port_built, n, dup, per, k, aniso):
+    """One-leaf trees (periodic ones search without images), fewer than 16 particles, exact
+    duplicates (zero distances skipped by the target searches, zero metric offsets)."""
+    from tests.test_oracle import _phase_edge_inputs
+    pos, vel, m = _phase_edge_inputs(n, dup, per or 10.0)
+    P = oracle.OracleTree(pos, vel, m, 16, 3, 0, 1000, per, backend="port", nthreads=2,
+                          aniso=aniso)
+    t = KDTree(pos, vel, m, 16, treetype=TPHS, kerntype=KSPH, aniso=aniso, period=per)
+    want_nn, want_d2 = P.knn(k)
+    nn, d2 = t.FindNearest(k)
+    ids, dd = _ids_rows(t, nn, d2)
+    assert_knn_equal(ids, dd, want_nn, want_d2, f"FindNearest n={n} dup={dup} per={per}",
+                     dropped_nearest=per is not None)
+    x = np.hstack([pos[:5], vel[:5]]) + 0.01
+    want_nn, want_d2 = P.knn_coord(x, k)
+    nn, d2 = t.FindNearestPoints(x, k)
+    assert_knn_equal(to_ids(nn, np.asarray(t.GetPerm())), d2, want_nn, want_d2,
+                     f"FindNearest(x) n={n}")
+    if aniso == 0:
+        assert_density_close(t.CalcDensity(k), P.density(k), f"CalcDensity n={n}")
+    t.close()
+
+
+def test_phase_too_few_particles_for_the_metric(gpu):
+    rng = np.random.default_rng(1)
+    pos, vel, m = rng.random((7, 3)), rng.random((7, 3)), np.ones(7)
+    t = KDTree(pos, vel, m, 16, treetype=TPHS)
+    with pytest.raises(NbkError):
+        t.FindNearest(3)  # the metric spacing needs 8 particles (the reference exits)
+    t.close()

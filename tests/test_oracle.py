@@ -312,3 +312,36 @@ def test_port_phase_space_matches_reference(ref_built, aniso, periodic):
     np.testing.assert_array_equal(da, db)
     if aniso == 0:
         np.testing.assert_array_equal(mk("ref").density(32), mk("port").density(32))
+
+
+def _phase_edge_inputs(n, dup, box, seed=3):
+    rng = np.random.default_rng(seed)
+    pos = rng.random((n, 3)) * box
+    vel = rng.normal(size=(n, 3)) * 0.3
+    m = rng.random(n) + 0.5
+    if dup:  # exact duplicates: zero distances, ties, a metric spacing over zero offsets
+        pos[n // 2: n // 2 + dup] = pos[:dup]
+        vel[n // 2: n // 2 + dup] = vel[:dup]
+    return pos, vel, m
+
+
+PHASE_EDGE_CASES = [(12, 0, 5.0, 4), (12, 0, None, 4), (9, 0, 3.0, 3), (300, 40, 10.0, 8),
+                    (300, 40, None, 8)]
+
+
+@pytest.mark.parametrize("n,dup,per,k", PHASE_EDGE_CASES)
+@pytest.mark.parametrize("aniso", [-1, 0])
+def test_port_phase_space_edge_cases_match_reference(ref_built, n, dup, per, k, aniso):
+    """Trees that are one leaf (periodic: no images), fewer than 16 particles, exact
+    duplicates: FindNearest(tt), FindNearest(x) and CalcDensity bit-identical."""
+    pos, vel, m = _phase_edge_inputs(n, dup, per or 10.0)
+    mk = lambda be: oracle.OracleTree(pos, vel, m, 16, 3, 0, 1000, per, backend=be, nthreads=2,
+                                      aniso=aniso)
+    R, P = mk("ref"), mk("port")
+    for (a, da), (b, db) in ((R.knn(k), P.knn(k)),
+                             (R.knn_coord(np.hstack([pos[:5], vel[:5]]) + 0.01, k),
+                              P.knn_coord(np.hstack([pos[:5], vel[:5]]) + 0.01, k))):
+        np.testing.assert_array_equal(da, db)
+        np.testing.assert_array_equal(a, b)
+    if aniso == 0:
+        np.testing.assert_array_equal(mk("ref").density(k), mk("port").density(k))
