@@ -328,6 +328,8 @@ def components(args, lib):
             "roofline_fp64": fp64_roofline(20 * k, n, kd_ms),
             "phase_ms": {kk: round(v, 4) for kk, v in ph.items()},
         }
+        if not args.no_cpu:
+            out[name]["cpu"] = cpu_knn_density(pos, mass, per, k, full_density=n <= 65536)
         del dpos, dmass
 
     # 256^3 clustered particles in L=250 with velocities: CalcDensity(64), then
@@ -400,6 +402,8 @@ def components(args, lib):
         "batched_queries_per_s": len(gm) / (graph_ms / 1e3),
         "target": "batched >= 5x the per-tree loop",
     }
+    if not args.no_cpu:
+        out["batched_20000_groups_k32"]["cpu"] = cpu_batched(gp, gm, off)
     del B, Bt, rho, dgp, dgm, doff
 
     # adjoint: d(sum w log rho)/d(x, m) with frozen neighbour lists against the forward
@@ -473,6 +477,55 @@ def components(args, lib):
     out["phase_space_clustered_2pow20_k32"] = res
     del dpos, dmass, dvel
     return out
+
+
+def cpu_knn_density(pos, mass, per, k, full_density):
+    """The C restatement on the host cores for a kNN-density component: tree build and
+    FindNearest(k) for every particle with all OpenMP threads (as the reference's test
+    loops them), and CalcDensity(k), serial as the reference ships it, where the set is
+    small enough to finish in a second or two."""
+    import oracle
+    oracle.build(ref=False)
+    threads = os.cpu_count() or 1
+    n = len(mass)
+    t0 = time.perf_counter()
+    o = oracle.OracleTree(pos, None, mass, BUCKET, 0, 0, 1000, per, backend="port",
+                          nthreads=threads)
+    t1 = time.perf_counter()
+    o.knn(k)
+    t2 = time.perf_counter()
+    res = {"kind": "port", "cores": threads, "build_s": t1 - t0,
+           "findnearest_queries_per_s": n / (t2 - t1)}
+    if full_density:
+        o.density(k)
+        t3 = time.perf_counter()
+        res["density_serial_queries_per_s"] = n / (t3 - t2)
+        res["step_queries_per_s"] = n / (t3 - t0 - (t2 - t1))
+    o.close()
+    return res
+
+
+def cpu_batched(gp, gm, off, sample=2000):
+    """The per-group loop of the reference's pattern (one KDTree + CalcDensity(min(32,
+    n-1)) per group) on the C restatement, serial, over every 10th of the first
+    10*sample groups."""
+    import oracle
+    oracle.build(ref=False)
+    t0 = time.perf_counter()
+    parts = 0
+    for g in range(0, min(10 * sample, len(off) - 1), 10):
+        a, b = int(off[g]), int(off[g + 1])
+        if b - a < 2:
+            continue
+        o = oracle.OracleTree(gp[a:b], None, gm[a:b], BUCKET, 0, 0, 1000, None, backend="port",
+                              nthreads=1)
+        o.density(min(32, b - a - 1))
+        o.close()
+        parts += b - a
+    dt = time.perf_counter() - t0
+    return {"kind": "port", "cores": 1, "particles_per_s": parts / dt,
+            "sample": f"every 10th of the first {10 * sample} groups ({parts} particles), "
+                      "build + density per group, one core"}
 
 
 def cpu_baseline_fof(pos, mass, ll):
