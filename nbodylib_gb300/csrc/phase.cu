@@ -224,15 +224,13 @@ __device__ void ph_walk_images(const TreeView& tv, PhHeap<KMAX, NT>& H, int t, i
   }
 }
 
-// CalculateMetricSpacing: the 8 nearest in plain phase space around x (a particle at x
-// itself included); the six direct offsets to the second nearest (or the next one whose
-// offsets are all non-zero) give metric[j] = 1/sr0[j]^2. Uses the first 8 heap rows.
+// CalculateMetricSpacing, second half: from the 8 nearest in plain phase space around x
+// (held in the first 8 heap rows; a particle at x itself included), the six direct
+// offsets to the second nearest (or the next one whose offsets are all non-zero) give
+// metric[j] = 1/sr0[j]^2. Returns false when fewer than 8 particles exist.
 template <int KMAX, int NT>
-__device__ bool ph_metric_spacing(const TreeView& tv, PhHeap<KMAX, NT>& H, int t,
-                                  const double x[6], bool periodic, double metric[6], int* err) {
-  ph_fill<KMAX, NT>(H, t, 8);
-  double top = kMaxValue;
-  ph_walk_images<KMAX, NT>(tv, H, t, 8, x, nullptr, false, periodic, top, err);
+__device__ bool ph_spacing_from_heap(const TreeView& tv, const PhHeap<KMAX, NT>& H, int t,
+                                     const double x[6], double metric[6]) {
   // the reference pops the heap into ID[7..0]: ID ascending by distance
   double d[8];
   int id[8];
@@ -249,7 +247,7 @@ __device__ bool ph_metric_spacing(const TreeView& tv, PhHeap<KMAX, NT>& H, int t
       id[b] = id[b - 1];
       id[b - 1] = ti;
     }
-  if (id[0] < 0) return false;  // fewer than 8 particles (the reference exits)
+  if (id[0] < 0) return false;
   double sr0[6] = {0, 0, 0, 0, 0, 0};
   double kvol = 0.0;
   for (int ivol = 1; kvol == 0.0 && ivol < 8; ivol++) {
@@ -268,63 +266,217 @@ __device__ bool ph_metric_spacing(const TreeView& tv, PhHeap<KMAX, NT>& H, int t
   return true;
 }
 
-template <int KMAX, int NT>
-__global__ void __launch_bounds__(NT) k_phase(PhaseArgs pa) {
+// ---- the warp-cooperative exact search
+// One warp serves 32 queries that are consecutive in tree order; it walks the tree once
+// for all of them (a node is opened when any lane's FP32 bound in its own weights is
+// below its heap top), stages each opened leaf's FP32 coordinates in shared memory, and
+// every lane tests them against its own query, exactly (FP64, the reference's arithmetic)
+// for the particles its FP32 screen keeps. The result is each lane's exact k nearest.
+// That is the reference's answer for the plain phase distance, and for the local metric
+// whenever every metric weight is at least 1 + 1e-9: the reference's unscaled offset sum
+// is then below the metric distance of every particle of a cell it prunes, so it never
+// prunes a particle that belongs in the heap. Lanes with a smaller weight walk the tree
+// alone in the reference's order (ph_walk).
+constexpr int kPhStack = 64;
+
+template <int KMAX>
+struct PhWarp {
+  PhHeap<KMAX, 32> H;
+  float4 sp[32], sv[32];  // FP32 position / velocity of the staged leaf particles
+  int stk[kPhStack];
+};
+
+template <int KMAX>
+__device__ void ph_coop(const TreeView& tv, PhWarp<KMAX>& w, int lane, bool active,
+                        const double x[6], const double* metric, const float w32[6], int skip,
+                        bool need_pos, int K, double& top, int* err) {
+  const unsigned FULL = 0xffffffffu;
+  float q32[6], e32[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    q32[k] = __double2float_rn(x[k]);
+    e32[k] = fmaxf(tv.eps6[k], __fmul_ru(__double2float_ru(fabs(x[k])), 1.2e-7f));
+  }
+  float thr = thresh_hi_bits(dkey(top));
+  const NodeS* N = tv.nodes6 + tv.nbase;
+  const NodeF6* F = tv.nodef6 + tv.nbase;
+  double m[6] = {1, 1, 1, 1, 1, 1};
+  if (metric)
+#pragma unroll
+    for (int k = 0; k < 6; k++) m[k] = metric[k];
+  if (lane == 0) w.stk[0] = 0;
+  int sp = 1;
+  __syncwarp();
+  while (sp > 0) {
+    const int h = w.stk[sp - 1];
+    sp--;
+    __syncwarp();
+    const bool need = active && box_lb6f(q32, w32, e32, F[h]) < thr;
+    const unsigned want = __ballot_sync(FULL, need);
+    if (!want) continue;
+    const NodeS nd = N[h];
+    if (nd.split_dim < 0) {
+      for (int c0 = 0; c0 < nd.count; c0 += 32) {
+        const int mm = min(32, nd.count - c0);
+        if (lane < mm) {
+          w.sp[lane] = tv.posf[nd.start + c0 + lane];
+          w.sv[lane] = tv.velf[nd.start + c0 + lane];
+        }
+        __syncwarp();
+        if (need) {
+          for (int j = 0; j < mm; j++) {
+            const int ti = nd.start + c0 + j;
+            if (ti == skip) continue;
+            const float4 a = w.sp[j], b = w.sv[j];
+            const float c[6] = {a.x, a.y, a.z, b.x, b.y, b.z};
+            if (pair_lb6f(q32, c, w32, e32) >= thr) continue;
+            const P4 p = tv.pos[ti];
+            const V4 v = tv.vel[ti];
+            const double d2 = metric ? metric_d2(x, p, v, m) : phase_d2(x, p, v);
+            if (d2 < top && (!need_pos || d2 > 0)) {
+              ph_replace_top<KMAX, 32>(w.H, lane, K, d2, ti);
+              top = w.H.d[0][lane];
+              thr = thresh_hi_bits(dkey(top));
+            }
+          }
+        }
+        __syncwarp();
+      }
+      continue;
+    }
+    const int hl = 2 * h + 1, hr = 2 * h + 2;
+    const float dl = active ? box_lb6f(q32, w32, e32, F[hl]) : FLT_MAX;
+    const float dr = active ? box_lb6f(q32, w32, e32, F[hr]) : FLT_MAX;
+    const unsigned bl = __ballot_sync(FULL, active && dl < thr);
+    const unsigned br = __ballot_sync(FULL, active && dr < thr);
+    const int leader = __ffs(want) - 1;
+    const float dl0 = __shfl_sync(FULL, dl, leader), dr0 = __shfl_sync(FULL, dr, leader);
+    if (sp + 2 > kPhStack) {
+      if (lane == 0) atomicExch(err, kErrCapacity);
+      return;
+    }
+    // the farther child (for the first wanting lane) is pushed first, so the nearer opens first
+    const bool lfirst = dl0 <= dr0;
+    const int first = lfirst ? hr : hl, second = lfirst ? hl : hr;
+    const bool fneed = lfirst ? br != 0 : bl != 0, sneed = lfirst ? bl != 0 : br != 0;
+    if (fneed) {
+      if (lane == 0) w.stk[sp] = first;
+      sp++;
+    }
+    if (sneed) {
+      if (lane == 0) w.stk[sp] = second;
+      sp++;
+    }
+    __syncwarp();
+  }
+}
+
+// The coordinate form with the seven ungated position images of a periodic tree (a tree
+// that is one leaf searches x alone), for the warp.
+template <int KMAX>
+__device__ void ph_coop_images(const TreeView& tv, PhWarp<KMAX>& w, int lane, bool active,
+                               const double x[6], const double* metric, const float w32[6],
+                               bool need_pos, bool periodic, int K, double& top, int* err) {
+  ph_coop<KMAX>(tv, w, lane, active, x, metric, w32, -1, need_pos, K, top, err);
+  if (!periodic || tv.nodes6[tv.nbase].split_dim < 0) return;
+  for (int pass = 1; pass < 8; pass++) {
+    double xp[6];
+    reflect(x, xp, tv.period, kImageMask[pass]);
+    xp[3] = x[3];
+    xp[4] = x[4];
+    xp[5] = x[5];
+    ph_coop<KMAX>(tv, w, lane, active, xp, metric, w32, -1, need_pos, K, top, err);
+  }
+}
+
+template <int KMAX>
+__host__ __device__ constexpr int ph_warps_per_block() {
+  return KMAX <= 16 ? 8 : (KMAX <= 32 ? 4 : (KMAX <= 64 ? 2 : 1));
+}
+
+template <int KMAX>
+__global__ void __launch_bounds__(32 * ph_warps_per_block<KMAX>()) k_phase(PhaseArgs pa) {
+  constexpr int WPB = ph_warps_per_block<KMAX>();
   const KnnArgs& a = pa.k;
   const TreeView& tv = a.tv;
   extern __shared__ __align__(16) unsigned char smem[];
-  PhHeap<KMAX, NT>& H = *reinterpret_cast<PhHeap<KMAX, NT>*>(smem);
-  const int t = threadIdx.x;
-  const int q = blockIdx.x * NT + t;
-  if (q >= a.nq) return;
+  PhWarp<KMAX>& w = reinterpret_cast<PhWarp<KMAX>*>(smem)[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const int gw = blockIdx.x * WPB + (threadIdx.x >> 5);
+  if (gw * 32 >= a.nq) return;  // whole warps only
+  const int q = gw * 32 + lane;
+  bool valid = q < a.nq;
   // the query: a tree particle (qmode 0: q0 + q; 2: qidx[q]) or a phase-space point
   int self = -1;
-  double x[6];
-  if (a.qmode == 1) {
+  double x[6] = {0, 0, 0, 0, 0, 0};
+  if (valid && a.qmode == 1) {
 #pragma unroll
     for (int j = 0; j < 6; j++) x[j] = a.qx[6 * (size_t)q + j];
-  } else {
-    int ti = a.qmode == 0 ? a.q0 + q : a.qidx[q];
+  } else if (valid) {
+    const int ti = a.qmode == 0 ? a.q0 + q : a.qidx[q];
     if (ti < 0 || ti >= tv.n) {
       atomicExch(a.err, kErrTarget);
-      return;
+      valid = false;
+    } else {
+      self = tv.pstart + ti;
+      const P4 p = tv.pos[self];
+      const V4 v = tv.vel[self];
+      x[0] = p.x;
+      x[1] = p.y;
+      x[2] = p.z;
+      x[3] = v.x;
+      x[4] = v.y;
+      x[5] = v.z;
     }
-    self = tv.pstart + ti;
-    P4 p = tv.pos[self];
-    V4 v = tv.vel[self];
-    x[0] = p.x;
-    x[1] = p.y;
-    x[2] = p.z;
-    x[3] = v.x;
-    x[4] = v.y;
-    x[5] = v.z;
   }
   const int K = a.kheap;
   const bool periodic = a.periodic != 0;
-  double metric[6];
-  if (pa.metric && !ph_metric_spacing<KMAX, NT>(tv, H, t, x, pa.spacing_periodic != 0, metric,
-                                                a.err)) {
-    atomicExch(a.err, kErrTooFew);
-    return;
+  const float ones[6] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f};
+  double metric[6] = {1, 1, 1, 1, 1, 1};
+  float w32[6] = {1.f, 1.f, 1.f, 1.f, 1.f, 1.f};
+  bool coop = valid;
+  if (pa.metric) {
+    // CalculateMetricSpacing: the exact 8 nearest in plain phase space (a coordinate search)
+    if (valid) ph_fill<KMAX, 32>(w.H, lane, 8);
+    double top8 = kMaxValue;
+    ph_coop_images<KMAX>(tv, w, lane, valid, x, nullptr, ones, false, pa.spacing_periodic != 0,
+                         8, top8, a.err);
+    if (valid && !ph_spacing_from_heap<KMAX, 32>(tv, w.H, lane, x, metric)) {
+      atomicExch(a.err, kErrTooFew);
+      valid = false;
+    }
+    double mmin = metric[0], mmax = metric[0];
+#pragma unroll
+    for (int j = 0; j < 6; j++) {
+      mmin = fmin(mmin, metric[j]);
+      mmax = fmax(mmax, metric[j]);
+      w32[j] = __double2float_rd(metric[j]);
+    }
+    coop = valid && mmin >= 1.0 + 1e-9 && mmax < INFINITY;
   }
   const double* mp = pa.metric ? metric : nullptr;
-  ph_fill<KMAX, NT>(H, t, K);
+  if (valid) ph_fill<KMAX, 32>(w.H, lane, K);
   double top = kMaxValue;
   if (self >= 0 && !periodic) {
     // the target forms: the target itself and distance 0 are skipped
-    ph_walk<KMAX, NT>(tv, H, t, K, x, mp, self, true, top, a.err);
+    ph_coop<KMAX>(tv, w, lane, coop, x, mp, w32, self, true, K, top, a.err);
+    if (valid && !coop) ph_walk<KMAX, 32>(tv, w.H, lane, K, x, mp, self, true, top, a.err);
   } else {
     // the coordinate forms (also a periodic target search): the local metric skips
     // distance 0, the plain distance skips nothing
-    ph_walk_images<KMAX, NT>(tv, H, t, K, x, mp, pa.metric != 0, periodic, top, a.err);
+    ph_coop_images<KMAX>(tv, w, lane, coop, x, mp, w32, pa.metric != 0, periodic, K, top,
+                         a.err);
+    if (valid && !coop)
+      ph_walk_images<KMAX, 32>(tv, w.H, lane, K, x, mp, pa.metric != 0, periodic, top, a.err);
   }
+  if (!valid) return;
   if (pa.epi == kPhNN) {
     // LoadNN: the heap popped into rows [kout-1 .. 0]; a heap of kout + 1 drops its nearest
     double d[KMAX];
     int id[KMAX];
     for (int s = 0; s < K; s++) {
-      d[s] = H.d[s][t];
-      id[s] = H.i[s][t];
+      d[s] = w.H.d[s][lane];
+      id[s] = w.H.i[s][lane];
     }
     for (int s = 1; s < K; s++)
       for (int b = s; b > 0 && d[b] < d[b - 1]; b--) {
@@ -346,7 +498,7 @@ __global__ void __launch_bounds__(NT) k_phase(PhaseArgs pa) {
   // CalcDensity / CalcDensityParticle: h = 0.5 sqrt(top), norm = h^-6 times the product
   // of sqrt(metric[j]) (KDCalcSmoothQuantities.cxx:251-270)
   for (int s = 0; s < K; s++)
-    if (H.i[s][t] < 0) {
+    if (w.H.i[s][lane] < 0) {
       atomicExch(a.err, kErrTooFew);
       return;
     }
@@ -367,28 +519,29 @@ __global__ void __launch_bounds__(NT) k_phase(PhaseArgs pa) {
   const double mi = tv.pos[self].m;
   double acc = 0.0;
   for (int s = 0; s < K; s++) {
-    const int j = H.i[s][t];
-    const double rij = __dsqrt_rn(H.d[s][t]);
-    const double w = dmul(wsm_line(__ddiv_rn(rij, hh), kr, inv_delta, a.kernel), wnorm);
+    const int j = w.H.i[s][lane];
+    const double rij = __dsqrt_rn(w.H.d[s][lane]);
+    const double wv = dmul(wsm_line(__ddiv_rn(rij, hh), kr, inv_delta, a.kernel), wnorm);
     const double mj = tv.pos[j].m;
-    acc = dadd(acc, dmul(w, mj));
-    if (scatter) atomicAdd(&a.rho[j - tv.pstart], dmul(w, mi));
+    acc = dadd(acc, dmul(wv, mj));
+    if (scatter) atomicAdd(&a.rho[j - tv.pstart], dmul(wv, mi));
   }
   if (scatter) atomicAdd(&a.rho[self - tv.pstart], acc);
   else a.rho[q] = acc;
 }
 
-template <int KMAX, int NT>
+template <int KMAX>
 int launch_phase_t(const PhaseArgs& pa, cudaStream_t st) {
-  size_t sm = sizeof(PhHeap<KMAX, NT>);
+  constexpr int WPB = ph_warps_per_block<KMAX>();
+  size_t sm = sizeof(PhWarp<KMAX>) * WPB;
   static bool attr_set = false;
   if (!attr_set) {
-    NBK_CUDA_TRY(cudaFuncSetAttribute(k_phase<KMAX, NT>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    NBK_CUDA_TRY(cudaFuncSetAttribute(k_phase<KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)sm));
     attr_set = true;
   }
-  unsigned blocks = (unsigned)((pa.k.nq + NT - 1) / NT);
-  k_phase<KMAX, NT><<<blocks, NT, sm, st>>>(pa);
+  unsigned warps = (unsigned)((pa.k.nq + 31) / 32);
+  k_phase<KMAX><<<(warps + WPB - 1) / WPB, 32 * WPB, sm, st>>>(pa);
   note_launch();
   NBK_CUDA_TRY(cudaGetLastError());
   return NBK_OK;
@@ -405,10 +558,10 @@ int launch_phase(const PhaseArgs& pa, cudaStream_t st) {
     return NBK_ERR_UNSUPPORTED;
   }
   // heaps hold at least the 8 entries of the metric spacing
-  if (K <= 16) return launch_phase_t<16, 256>(pa, st);
-  if (K <= 32) return launch_phase_t<32, 128>(pa, st);
-  if (K <= 64) return launch_phase_t<64, 64>(pa, st);
-  return launch_phase_t<128, 32>(pa, st);
+  if (K <= 16) return launch_phase_t<16>(pa, st);
+  if (K <= 32) return launch_phase_t<32>(pa, st);
+  if (K <= 64) return launch_phase_t<64>(pa, st);
+  return launch_phase_t<128>(pa, st);
 }
 
 }  // namespace nbk
