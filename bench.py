@@ -429,6 +429,52 @@ def components(args, lib):
     }
     del dpos, dmass, w
 
+    # FOFCriterion with the FOF6d comparator on the physical tree of the same particles
+    # with velocities: linking length ll in position (search region the same, so every
+    # link is found from both ends), 0.2 in velocity
+    pos, mass, vel = syn.clustered_box(N_FOF, BOX, seed=2, velocities=True)
+    dpos, dmass, dvel = (torch.from_numpy(a).cuda() for a in (pos, mass, vel))
+    ll = syn.linking_length(N_FOF, BOX)
+    crit = [0, ll * ll, 0, 0, 0, 0, ll * ll, 0.04]
+
+    def crit_step():
+        t = KDTree(dpos, dvel, dmass, BUCKET, kerntype=0, period=[BOX] * 3, device=True)
+        g, ng = t.FOFCriterion(2, crit, MINNUM)
+        t.sync()
+        t.close()
+        return ng
+
+    ngc = crit_step()
+    crit_ms = _timed(crit_step, reps, flush)
+    phc = _trace(lib, crit_step)
+    out["fof_criterion_fof6d_clustered_2pow20"] = {
+        "n": N_FOF, "params": crit, "minnum": MINNUM, "groups": int(ngc),
+        "step_build_plus_fofcriterion_ms": crit_ms,
+        "particles_per_s_step": N_FOF / (crit_ms / 1e3),
+        "phase_ms": {kk: round(v, 4) for kk, v in phc.items()}}
+    if not args.no_cpu:
+        # the reference's breadth-first FOFCriterion tests every particle within ll of each
+        # member (no whole-node shortcut), so the CPU sample is the same recipe at 2^15
+        # particles and the same number density
+        import oracle
+        oracle.build(ref=False)
+        threads = os.cpu_count() or 1
+        ns = 1 << 15
+        bs = BOX * (ns / N_FOF) ** (1.0 / 3.0)
+        ps, ms, vs = syn.clustered_box(ns, bs, seed=2, velocities=True)
+        lls = syn.linking_length(ns, bs)
+        t0 = time.perf_counter()
+        o = oracle.OracleTree(ps, vs, ms, BUCKET, 0, 0, 1000, [bs] * 3, backend="port",
+                              nthreads=threads)
+        o.fof_criterion(2, [0, lls * lls, 0, 0, 0, 0, lls * lls, 0.04], MINNUM, 0)
+        dt = time.perf_counter() - t0
+        o.close()
+        out["fof_criterion_fof6d_clustered_2pow20"]["cpu"] = {
+            "particles_per_s": ns / dt, "cores": threads, "kind": "port",
+            "sample": "the same recipe at 2^15 particles and the same number density: build "
+                      "with all OpenMP threads + serial FOFCriterion"}
+    del dpos, dmass, dvel
+
     # phase-space tree (TreeType TPHS) on the 2^20 clustered particles with velocities:
     # build + CalcDensity(32) with the local metric (the reference's default), and
     # FindNearest(32) with the local metric and with the plain phase distance; every query

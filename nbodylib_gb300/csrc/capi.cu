@@ -1451,6 +1451,16 @@ int nbk_fof_criterion(nbk_tree* t, int comparator, const double* params, int32_t
   a.crit = 1;
   a.cmp = comparator;
   for (int i = 0; i < 8; i++) a.params[i] = p[i];
+  {
+    // the position search distance^2 of FOFSearchCriterion (its invscaling, from
+    // params[0]); when FOF3d / FOF6d accept only pairs inside it, reachability follows
+    // from the comparator and the warp-cooperative search applies
+    int tt = (int)p[0];
+    double s1 = (tt == NBK_TPHYS || tt == NBK_TPHS) ? p[1] : (tt == NBK_TVEL ? p[2] : 1.0);
+    a.crit_contained = t->treetype == NBK_TPHYS &&
+                       (comparator == NBK_FOF3D || comparator == NBK_FOF6D) && p[6] > 0 &&
+                       s1 > 0 && p[6] <= s1 && (comparator != NBK_FOF6D || p[7] > 0);
+  }
   a.parent = parent;
   a.err = t->d_err;
   int ng = 0;

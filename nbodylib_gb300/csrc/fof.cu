@@ -18,6 +18,9 @@
 //     root order -- the reference's numbering (discovery order in tree order).
 // All FP32 shortcuts are conservative (directed rounding), so the linked pairs are
 // exactly those the FP64 test links.
+#include <cmath>
+#include <cstring>
+
 #include "nbk_build.h"
 
 namespace nbk {
@@ -112,11 +115,41 @@ __device__ __forceinline__ float boxbox_d2_lo(const NodeRec& r, const float qlo[
   return __fadd_rd(__fadd_rd(__fmul_rd(g[0], g[0]), __fmul_rd(g[1], g[1])), __fmul_rd(g[2], g[2]));
 }
 
+// ---- FOFCriterion (KDFOF.cxx:157-265). The comparators of FOFFunc.h:30-55, in the
+// reference's operation order: total += (a-b)*(a-b)/params[6] per dimension (FOF6d
+// interleaves position and velocity terms), linked when total < 1.
+__device__ __forceinline__ bool crit_cmp(int cmp, const double* p, const double xa[3],
+                                         const V4& va, const P4& xb, const V4& vb) {
+  double total = 0.0;
+  double xb3[3] = {xb.x, xb.y, xb.z}, va3[3] = {va.x, va.y, va.z}, vb3[3] = {vb.x, vb.y, vb.z};
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    if (cmp == 0 || cmp == 2) {
+      double d = dsub(xa[j], xb3[j]);
+      total = dadd(total, __ddiv_rn(dmul(d, d), p[6]));
+    }
+    if (cmp == 1) {
+      double d = dsub(va3[j], vb3[j]);
+      total = dadd(total, __ddiv_rn(dmul(d, d), p[6]));
+    }
+    if (cmp == 2) {
+      double d = dsub(va3[j], vb3[j]);
+      total = dadd(total, __ddiv_rn(dmul(d, d), p[7]));
+    }
+  }
+  return total < 1.0;
+}
+
 // 2. One warp links 32 consecutive particles. The traversal is frontier-parallel: each
 // step pops up to 32 nodes from the warp's stack, lane i loads node i, drops it when it
 // lies farther than ll from the box around all of the warp's query points, and for a
 // compact node chases its union-find root, so the dependent loads of up to 32 nodes
 // overlap. The surviving nodes are then tested against every lane's own query.
+//
+// CRIT3D: FOFCriterion with FOF3d inside its search region, run as FOF with
+// ll^2 = params[6]; the FP32 decisions are the same (their 2^-20 margins cover the
+// rounding of the comparator's divisions) and the pairs left to FP64 take the comparator.
+template <bool CRIT3D>
 __global__ void __launch_bounds__(32 * kWpb, 4) k_link(FofArgs a) {
   __shared__ FofSmem sm[kWpb];
   const unsigned FULL = 0xffffffffu;
@@ -243,7 +276,8 @@ __global__ void __launch_bounds__(32 * kWpb, 4) k_link(FofArgs a) {
                 bool in = pair_d2_hi(qx, qy, qz, cf.x, cf.y, cf.z, two_eps) < ll2_lo;
                 if (!in) {
                   P4 c = tv.pos[ti];
-                  in = dkey(dist2_exact(xq[0], xq[1], xq[2], c.x, c.y, c.z)) < ll2k;
+                  if (CRIT3D) in = crit_cmp(0, a.params, xq, make_v4(0, 0, 0, 0), c, make_v4(0, 0, 0, 0));
+                  else in = dkey(dist2_exact(xq[0], xq[1], xq[2], c.x, c.y, c.z)) < ll2k;
                 }
                 if (in) {
                   int rt = find_root(a.parent, pj, a.err);
@@ -275,31 +309,6 @@ __global__ void __launch_bounds__(32 * kWpb, 4) k_link(FofArgs a) {
     }
     if (sp > 0 && lane == 0) atomicExch(a.err, kErrIterCap);
   }
-}
-
-// ---- FOFCriterion (KDFOF.cxx:157-265). The comparators of FOFFunc.h:30-55, in the
-// reference's operation order: total += (a-b)*(a-b)/params[6] per dimension (FOF6d
-// interleaves position and velocity terms), linked when total < 1.
-__device__ __forceinline__ bool crit_cmp(int cmp, const double* p, const double xa[3],
-                                         const V4& va, const P4& xb, const V4& vb) {
-  double total = 0.0;
-  double xb3[3] = {xb.x, xb.y, xb.z}, va3[3] = {va.x, va.y, va.z}, vb3[3] = {vb.x, vb.y, vb.z};
-#pragma unroll
-  for (int j = 0; j < 3; j++) {
-    if (cmp == 0 || cmp == 2) {
-      double d = dsub(xa[j], xb3[j]);
-      total = dadd(total, __ddiv_rn(dmul(d, d), p[6]));
-    }
-    if (cmp == 1) {
-      double d = dsub(va3[j], vb3[j]);
-      total = dadd(total, __ddiv_rn(dmul(d, d), p[6]));
-    }
-    if (cmp == 2) {
-      double d = dsub(va3[j], vb3[j]);
-      total = dadd(total, __ddiv_rn(dmul(d, d), p[7]));
-    }
-  }
-  return total < 1.0;
 }
 
 // Node pruning of SplitNode::FOFSearchCriterion (KDSplitNode.cxx:991-1028): the far child
@@ -364,10 +373,18 @@ __global__ void __launch_bounds__(128) k_crit_link(FofArgs a) {
   double x0[3] = {me.x, me.y, me.z};
   int stk_h[kStack];
   double stk_rd[kStack], stk_off[kStack][3];
+  // FOF3d and FOF6d accept a pair only if sum dx^2 / params[6] < 1 (FOFFunc.h:30-55): a
+  // subtree (or particle) whose FP32 bound of that sum is at or above 1 + 2^-20 holds
+  // nothing to link and is passed over (FOFVel is not bounded by positions)
+  const float wpos = a.cmp == 1 ? 0.f : __double2float_rd(__ddiv_rd(1.0, a.params[6]));
+  const float thr1 = 1.0f + 1.0f / 1048576.0f;
   int npass = tv.periodic ? 8 : 1;
   for (int pass = 0; pass < npass; pass++) {
     double xq[3] = {x0[0], x0[1], x0[2]};
     if (pass > 0) reflect(x0, xq, tv.period, kImageMask[pass]);  // ungated (:1649-1681)
+    const float qx = __double2float_rn(xq[0]), qy = __double2float_rn(xq[1]),
+                qz = __double2float_rn(xq[2]);
+    const float eps = query_eps(tv, xq[0], xq[1], xq[2]), two_eps = __fadd_ru(eps, tv.eps);
     int sp = 0;
     stk_h[0] = 0;
     stk_rd[0] = 0.0;
@@ -379,9 +396,15 @@ __global__ void __launch_bounds__(128) k_crit_link(FofArgs a) {
       double rd = stk_rd[sp];
       double off[3] = {stk_off[sp][0], stk_off[sp][1], stk_off[sp][2]};
       NodeRec r = tv.node[tv.nbase + h];
+      if (wpos > 0.f && __fmul_rd(wpos, box_d2_lo(qx, qy, qz, eps, r)) >= thr1) continue;
       if (r.count <= tv.b) {
         for (int i = r.start; i < r.start + r.count; i++) {
           if (i == self) continue;
+          if (wpos > 0.f) {
+            const float4 cf = tv.posf[i];
+            if (__fmul_rd(wpos, pair_d2_lo(qx, qy, qz, cf.x, cf.y, cf.z, two_eps)) >= thr1)
+              continue;
+          }
           P4 xb = tv.pos[i];
           V4 vb = tv.vel ? tv.vel[i] : make_v4(0, 0, 0, 0);
           if (crit_cmp(a.cmp, a.params, xq, mv, xb, vb)) unite(a.parent, self, i, a.err);
@@ -417,6 +440,140 @@ __global__ void __launch_bounds__(128) k_crit_link(FofArgs a) {
       sp++;
     }
   }
+}
+
+// FOFCriterion when the comparator's region lies inside the search region (FOF3d or
+// FOF6d, params[6] at most the position search distance^2): every accepted pair is then
+// reachable from both of its ends (the reference's offset sum to a cell is at most the
+// scaled distance to any particle in it), so the reference's groups are the connected
+// components of the accepted pairs and any complete search finds them. One warp serves 32
+// consecutive particles: it walks the tree once for all of them (a node is opened when
+// any lane's FP32 bound of the position part, sum dx^2 / params[6], is below 1), stages
+// each opened leaf's FP32 positions, FP32 velocities and parents in shared memory, and each
+// lane decides its pairs with FP32 lower and upper bounds of the comparator's sum; only
+// pairs within a few FP32 ulps of 1 take the reference's FP64 comparator. Pairs already in
+// one component are skipped through the staged parents.
+constexpr int kCritStack = 128;
+struct CritSmem {
+  float4 sp[32], sv[32];
+  int par[32];
+  int stk[kCritStack];
+};
+
+__global__ void __launch_bounds__(32 * kWpb) k_crit_warp(FofArgs a) {
+  __shared__ CritSmem sm[kWpb];
+  const unsigned FULL = 0xffffffffu;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  CritSmem& w = sm[warp];
+  const TreeView& tv = a.tv;
+  const int q = (blockIdx.x * kWpb + warp) * 32 + lane;
+  if ((blockIdx.x * kWpb + warp) * 32 >= tv.n) return;
+  const bool valid = q < tv.n;
+  const int self = tv.pstart + (valid ? q : 0);
+  const P4 me = tv.pos[self];
+  const V4 mv = tv.vel ? tv.vel[self] : make_v4(0, 0, 0, 0);
+  const double x0[3] = {me.x, me.y, me.z};
+  const bool use_v = a.cmp == 2;
+  // the comparator's weights, rounded down (lower bounds) and up (upper bounds)
+  const float wp_lo = __double2float_rd(__ddiv_rd(1.0, a.params[6]));
+  const float wp_hi = __double2float_ru(__ddiv_ru(1.0, a.params[6]));
+  const float wv_lo = use_v ? __double2float_rd(__ddiv_rd(1.0, a.params[7])) : 0.f;
+  const float wv_hi = use_v ? __double2float_ru(__ddiv_ru(1.0, a.params[7])) : 0.f;
+  const float thr_hi = 1.0f + 1.0f / 1048576.0f, thr_lo = 1.0f - 1.0f / 1048576.0f;
+  const float qvx = __double2float_rn(mv.x), qvy = __double2float_rn(mv.y),
+              qvz = __double2float_rn(mv.z);
+  const float two_eps_v = __fmul_ru(2.f, a.eps_v);
+  int myroot = find_root(a.parent, self, a.err);
+  const int npass = tv.periodic ? 8 : 1;
+  for (int pass = 0; pass < npass; pass++) {
+    double xq[3] = {x0[0], x0[1], x0[2]};
+    if (pass > 0) reflect(x0, xq, tv.period, kImageMask[pass]);  // ungated (:1649-1681)
+    const float qx = __double2float_rn(xq[0]), qy = __double2float_rn(xq[1]),
+                qz = __double2float_rn(xq[2]);
+    const float eps = query_eps(tv, xq[0], xq[1], xq[2]), two_eps = __fadd_ru(eps, tv.eps);
+    if (lane == 0) w.stk[0] = 0;
+    int sp = 1;
+    __syncwarp();
+    while (sp > 0) {
+      const int h = w.stk[sp - 1];
+      sp--;
+      __syncwarp();
+      const NodeRec r = tv.node[tv.nbase + h];
+      const bool need = valid && __fmul_rd(wp_lo, box_d2_lo(qx, qy, qz, eps, r)) < thr_hi;
+      if (!__any_sync(FULL, need)) continue;
+      if (r.count > tv.b) {
+        if (sp + 2 > kCritStack) {
+          if (lane == 0) atomicExch(a.err, kErrCapacity);
+          return;
+        }
+        if (lane == 0) {
+          w.stk[sp] = 2 * h + 2;
+          w.stk[sp + 1] = 2 * h + 1;
+        }
+        sp += 2;
+        __syncwarp();
+        continue;
+      }
+      for (int c0 = 0; c0 < r.count; c0 += 32) {
+        const int mm = min(32, r.count - c0);
+        if (lane < mm) {
+          const int i = r.start + c0 + lane;
+          w.sp[lane] = tv.posf[i];
+          if (use_v) {
+            const V4 v = tv.vel[i];
+            w.sv[lane] = make_float4(__double2float_rn(v.x), __double2float_rn(v.y),
+                                     __double2float_rn(v.z), 0.f);
+          }
+          w.par[lane] = ld_parent(a.parent, i);
+        }
+        __syncwarp();
+        if (need) {
+          for (int jj = 0; jj < mm; jj++) {
+            const int ti = r.start + c0 + jj;
+            if (ti == self || (pass == 0 && ti < self)) continue;  // direct pass: each pair once
+            const int pj = w.par[jj];
+            if (pj == myroot || ti == myroot) continue;
+            const float4 cf = w.sp[jj];
+            float lo = __fmul_rd(wp_lo, pair_d2_lo(qx, qy, qz, cf.x, cf.y, cf.z, two_eps));
+            if (lo >= thr_hi) continue;
+            float hi = __fmul_ru(wp_hi, pair_d2_hi(qx, qy, qz, cf.x, cf.y, cf.z, two_eps));
+            if (use_v) {
+              const float4 cv = w.sv[jj];
+              lo = __fadd_rd(lo, __fmul_rd(wv_lo, pair_d2_lo(qvx, qvy, qvz, cv.x, cv.y, cv.z,
+                                                             two_eps_v)));
+              if (lo >= thr_hi) continue;
+              hi = __fadd_ru(hi, __fmul_ru(wv_hi, pair_d2_hi(qvx, qvy, qvz, cv.x, cv.y, cv.z,
+                                                             two_eps_v)));
+            }
+            bool in = hi < thr_lo;
+            if (!in) in = crit_cmp(a.cmp, a.params, xq, mv, tv.pos[ti], tv.vel ? tv.vel[ti] : mv);
+            if (in) {
+              int rt = find_root(a.parent, pj, a.err);
+              if (rt != myroot) myroot = find_root(a.parent, myroot, a.err);
+              if (rt != myroot) {
+                unite(a.parent, self, ti, a.err);
+                myroot = find_root(a.parent, self, a.err);
+              }
+            }
+          }
+        }
+        __syncwarp();
+      }
+    }
+  }
+}
+
+// max |v| over the velocities (non-negative floats order like their bits)
+__global__ void k_vel_absmax(const V4* vel, int n, unsigned* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float m = 0.f;
+  if (i < n) {
+    V4 v = vel[i];
+    m = fmaxf(fabsf(__double2float_ru(fabs(v.x))),
+              fmaxf(fabsf(__double2float_ru(fabs(v.y))), fabsf(__double2float_ru(fabs(v.z)))));
+  }
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
 }
 
 // FOFCriterion on a phase-space tree (KDFOF.cxx:157-265 with FOFSearchCriterion[Periodic],
@@ -680,9 +837,14 @@ int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tr
   NBK_TRY(alloc.get((void**)&bsum, sizeof(int) * (nb + 1)));
   NBK_TRY(alloc.get((void**)&d_total, sizeof(int)));
   k_iota<<<(n + 255) / 256, 256, 0, st>>>(a.parent, n); note_launch();
-  if (!a.crit) {
+  // FOFCriterion with FOF3d inside its search region links exactly the pairs with
+  // sum dx^2 / params[6] < 1: the FOF kernels with ll^2 = params[6]
+  const bool fof3d = a.crit == 1 && a.crit_contained && a.cmp == 0 && !a.tv.nodes6;
+  FofArgs f = a;
+  if (fof3d) f.ll2 = a.params[6];
+  if (!a.crit || fof3d) {
     Phase ph("fof_prelink", st);
-    k_prelink<<<(n + 255) / 256, 256, 0, st>>>(a); note_launch();
+    k_prelink<<<(n + 255) / 256, 256, 0, st>>>(f); note_launch();
     k_compress<<<(n + 255) / 256, 256, 0, st>>>(a.parent, n); note_launch();
   }
   int warps = (n + 31) / 32;
@@ -692,12 +854,32 @@ int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tr
   } else if (a.crit && a.tv.nodes6) {
     Phase ph("fof_criterion_link", st);
     k_crit_link6<<<(n + 127) / 128, 128, 0, st>>>(a); note_launch();
+  } else if (fof3d) {
+    Phase ph("fof_criterion_link", st);
+    k_link<true><<<(warps + kWpb - 1) / kWpb, 32 * kWpb, 0, st>>>(f); note_launch();
+  } else if (a.crit && a.crit_contained) {
+    Phase ph("fof_criterion_link", st);
+    FofArgs b = a;
+    if (a.cmp == 2) {
+      // FP32 rounding bound of the velocities: max |v| * 2^-23
+      unsigned* d_m;
+      NBK_TRY(alloc.get((void**)&d_m, sizeof(unsigned)));
+      NBK_CUDA_TRY(cudaMemsetAsync(d_m, 0, sizeof(unsigned), st));
+      k_vel_absmax<<<(n + 255) / 256, 256, 0, st>>>(a.tv.vel, n, d_m); note_launch();
+      unsigned hm = 0;
+      NBK_CUDA_TRY(cudaMemcpyAsync(&hm, d_m, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+      NBK_CUDA_TRY(cudaStreamSynchronize(st));
+      float vmax;
+      memcpy(&vmax, &hm, sizeof(float));
+      b.eps_v = std::ldexp(vmax, -23) * 1.0001f + 1e-38f;
+    }
+    k_crit_warp<<<(warps + kWpb - 1) / kWpb, 32 * kWpb, 0, st>>>(b); note_launch();
   } else if (a.crit) {
     Phase ph("fof_criterion_link", st);
     k_crit_link<<<(n + 127) / 128, 128, 0, st>>>(a); note_launch();
   } else {
     Phase ph("fof_link", st);
-    k_link<<<(warps + kWpb - 1) / kWpb, 32 * kWpb, 0, st>>>(a); note_launch();
+    k_link<false><<<(warps + kWpb - 1) / kWpb, 32 * kWpb, 0, st>>>(a); note_launch();
   }
   Phase ph_label("fof_label", st);
   NBK_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(int) * n, st));

@@ -177,3 +177,26 @@ def test_fof_criterion_vs_oracle(gpu, port_built, periodic, cmp):
     gg, ng = t.FOFCriterion(cmp, params, 10)
     assert ng == no
     assert_same_partition(gg, go, f"FOFCriterion cmp={cmp}")
+
+
+
+def test_fof_criterion_reachability_vs_oracle(gpu, port_built):
+    """FOF3d with params[6] above the search distance^2 params[1]: which pairs the reference
+    links then depends on its cut-plane reachability, which the per-particle walk
+    reproduces. On this uniform non-periodic set no group of the reference takes a
+    particle of an earlier one, so its groups are the components of the reachable links
+    (in general they are not: with such parameters the reference's breadth-first groups
+    depend on their visiting order; with periods this same set already differs by one
+    group)."""
+    n = 4000
+    pos, mass = syn.uniform_box(n, 10.0, seed=5)
+    vel = np.zeros((n, 3))
+    per = None
+    ll = syn.linking_length(n, 10.0, 0.8)
+    params = [0, (0.9 * ll) ** 2, 0, 0, 0, 0, ll * ll, 0]
+    o = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, per, backend="port")
+    go, no = o.fof_criterion(0, params, 5)
+    t = KDTree(pos, vel, mass, 16, kerntype=0, period=per)
+    gg, ng = t.FOFCriterion(0, params, 5)
+    assert ng == no
+    assert_same_partition(gg, go, "FOFCriterion FOF3d, params[6] > params[1]")
