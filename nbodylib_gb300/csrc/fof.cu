@@ -18,8 +18,10 @@
 //     root order -- the reference's numbering (discovery order in tree order).
 // All FP32 shortcuts are conservative (directed rounding), so the linked pairs are
 // exactly those the FP64 test links.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "nbk_build.h"
 
@@ -442,17 +444,6 @@ __global__ void __launch_bounds__(128) k_crit_link(FofArgs a) {
   }
 }
 
-// FOFCriterion when the comparator's region lies inside the search region (FOF3d or
-// FOF6d, params[6] at most the position search distance^2): every accepted pair is then
-// reachable from both of its ends (the reference's offset sum to a cell is at most the
-// scaled distance to any particle in it), so the reference's groups are the connected
-// components of the accepted pairs and any complete search finds them. One warp serves 32
-// consecutive particles: it walks the tree once for all of them (a node is opened when
-// any lane's FP32 bound of the position part, sum dx^2 / params[6], is below 1), stages
-// each opened leaf's FP32 positions, FP32 velocities and parents in shared memory, and each
-// lane decides its pairs with FP32 lower and upper bounds of the comparator's sum; only
-// pairs within a few FP32 ulps of 1 take the reference's FP64 comparator. Pairs already in
-// one component are skipped through the staged parents.
 constexpr int kCritStack = 128;
 struct CritSmem {
   float4 sp[32], sv[32];
@@ -460,7 +451,15 @@ struct CritSmem {
   int stk[kCritStack];
 };
 
-__global__ void __launch_bounds__(32 * kWpb) k_crit_warp(FofArgs a) {
+// FOFCriterion with FOF6d inside its search region on a physical tree: the accepted
+// pairs are those with sum dx^2 / params[6] + sum dv^2 / params[7] < 1, a unit ball of a
+// scaled phase space, whose components do not depend on the tree searched. They are found
+// on a phase-space tree built for the call over the same particles (its splits follow the
+// velocities where those spread more, so the search prunes in velocity too): one warp per
+// 32 particles walks it with FP32 bounds of the comparator's sum and unites the accepted
+// pairs (the reference's comparator in FP64 for pairs within a few FP32 ulps of 1); the
+// components are then carried over to the physical tree's indices.
+__global__ void __launch_bounds__(32 * kWpb) k_crit6_warp(FofArgs a) {
   __shared__ CritSmem sm[kWpb];
   const unsigned FULL = 0xffffffffu;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -471,26 +470,36 @@ __global__ void __launch_bounds__(32 * kWpb) k_crit_warp(FofArgs a) {
   const bool valid = q < tv.n;
   const int self = tv.pstart + (valid ? q : 0);
   const P4 me = tv.pos[self];
-  const V4 mv = tv.vel ? tv.vel[self] : make_v4(0, 0, 0, 0);
+  const V4 mv = tv.vel[self];
   const double x0[3] = {me.x, me.y, me.z};
-  const bool use_v = a.cmp == 2;
-  // the comparator's weights, rounded down (lower bounds) and up (upper bounds)
-  const float wp_lo = __double2float_rd(__ddiv_rd(1.0, a.params[6]));
-  const float wp_hi = __double2float_ru(__ddiv_ru(1.0, a.params[6]));
-  const float wv_lo = use_v ? __double2float_rd(__ddiv_rd(1.0, a.params[7])) : 0.f;
-  const float wv_hi = use_v ? __double2float_ru(__ddiv_ru(1.0, a.params[7])) : 0.f;
+  float w_lo[6], w_hi[6];
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    w_lo[j] = __double2float_rd(__ddiv_rd(1.0, a.params[6]));
+    w_hi[j] = __double2float_ru(__ddiv_ru(1.0, a.params[6]));
+    w_lo[3 + j] = __double2float_rd(__ddiv_rd(1.0, a.params[7]));
+    w_hi[3 + j] = __double2float_ru(__ddiv_ru(1.0, a.params[7]));
+  }
   const float thr_hi = 1.0f + 1.0f / 1048576.0f, thr_lo = 1.0f - 1.0f / 1048576.0f;
-  const float qvx = __double2float_rn(mv.x), qvy = __double2float_rn(mv.y),
-              qvz = __double2float_rn(mv.z);
-  const float two_eps_v = __fmul_ru(2.f, a.eps_v);
+  const NodeS* N = tv.nodes6 + tv.nbase;
+  const NodeF6* F = tv.nodef6 + tv.nbase;
   int myroot = find_root(a.parent, self, a.err);
-  const int npass = tv.periodic ? 8 : 1;
+  const int npass = (tv.periodic && N[0].split_dim >= 0) ? 8 : 1;
   for (int pass = 0; pass < npass; pass++) {
-    double xq[3] = {x0[0], x0[1], x0[2]};
-    if (pass > 0) reflect(x0, xq, tv.period, kImageMask[pass]);  // ungated (:1649-1681)
-    const float qx = __double2float_rn(xq[0]), qy = __double2float_rn(xq[1]),
-                qz = __double2float_rn(xq[2]);
-    const float eps = query_eps(tv, xq[0], xq[1], xq[2]), two_eps = __fadd_ru(eps, tv.eps);
+    double xq[6] = {x0[0], x0[1], x0[2], mv.x, mv.y, mv.z};
+    bool active = valid;
+    if (pass > 0) {
+      // an image links only if its position part can stay below 1: sval^2 < params[6]
+      const double sval = reflect(x0, xq, tv.period, kImageMask[pass]);
+      active = active && a.params[6] > dmul(sval, sval);
+    }
+    if (!__any_sync(FULL, active)) continue;
+    float q32[6], e32[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      q32[k] = __double2float_rn(xq[k]);
+      e32[k] = fmaxf(tv.eps6[k], __fmul_ru(__double2float_ru(fabs(xq[k])), 1.2e-7f));
+    }
     if (lane == 0) w.stk[0] = 0;
     int sp = 1;
     __syncwarp();
@@ -498,10 +507,10 @@ __global__ void __launch_bounds__(32 * kWpb) k_crit_warp(FofArgs a) {
       const int h = w.stk[sp - 1];
       sp--;
       __syncwarp();
-      const NodeRec r = tv.node[tv.nbase + h];
-      const bool need = valid && __fmul_rd(wp_lo, box_d2_lo(qx, qy, qz, eps, r)) < thr_hi;
+      const bool need = active && box_lb6f(q32, w_lo, e32, F[h]) < thr_hi;
       if (!__any_sync(FULL, need)) continue;
-      if (r.count > tv.b) {
+      const NodeS nd = N[h];
+      if (nd.split_dim >= 0) {
         if (sp + 2 > kCritStack) {
           if (lane == 0) atomicExch(a.err, kErrCapacity);
           return;
@@ -514,39 +523,26 @@ __global__ void __launch_bounds__(32 * kWpb) k_crit_warp(FofArgs a) {
         __syncwarp();
         continue;
       }
-      for (int c0 = 0; c0 < r.count; c0 += 32) {
-        const int mm = min(32, r.count - c0);
+      for (int c0 = 0; c0 < nd.count; c0 += 32) {
+        const int mm = min(32, nd.count - c0);
         if (lane < mm) {
-          const int i = r.start + c0 + lane;
+          const int i = nd.start + c0 + lane;
           w.sp[lane] = tv.posf[i];
-          if (use_v) {
-            const V4 v = tv.vel[i];
-            w.sv[lane] = make_float4(__double2float_rn(v.x), __double2float_rn(v.y),
-                                     __double2float_rn(v.z), 0.f);
-          }
+          w.sv[lane] = tv.velf[i];
           w.par[lane] = ld_parent(a.parent, i);
         }
         __syncwarp();
         if (need) {
           for (int jj = 0; jj < mm; jj++) {
-            const int ti = r.start + c0 + jj;
+            const int ti = nd.start + c0 + jj;
             if (ti == self || (pass == 0 && ti < self)) continue;  // direct pass: each pair once
             const int pj = w.par[jj];
             if (pj == myroot || ti == myroot) continue;
-            const float4 cf = w.sp[jj];
-            float lo = __fmul_rd(wp_lo, pair_d2_lo(qx, qy, qz, cf.x, cf.y, cf.z, two_eps));
-            if (lo >= thr_hi) continue;
-            float hi = __fmul_ru(wp_hi, pair_d2_hi(qx, qy, qz, cf.x, cf.y, cf.z, two_eps));
-            if (use_v) {
-              const float4 cv = w.sv[jj];
-              lo = __fadd_rd(lo, __fmul_rd(wv_lo, pair_d2_lo(qvx, qvy, qvz, cv.x, cv.y, cv.z,
-                                                             two_eps_v)));
-              if (lo >= thr_hi) continue;
-              hi = __fadd_ru(hi, __fmul_ru(wv_hi, pair_d2_hi(qvx, qvy, qvz, cv.x, cv.y, cv.z,
-                                                             two_eps_v)));
-            }
-            bool in = hi < thr_lo;
-            if (!in) in = crit_cmp(a.cmp, a.params, xq, mv, tv.pos[ti], tv.vel ? tv.vel[ti] : mv);
+            const float4 cp = w.sp[jj], cv = w.sv[jj];
+            const float c[6] = {cp.x, cp.y, cp.z, cv.x, cv.y, cv.z};
+            if (pair_lb6f(q32, c, w_lo, e32) >= thr_hi) continue;
+            bool in = pair_ub6f(q32, c, w_hi, e32) < thr_lo;
+            if (!in) in = crit_cmp(2, a.params, xq, mv, tv.pos[ti], tv.vel[ti]);
             if (in) {
               int rt = find_root(a.parent, pj, a.err);
               if (rt != myroot) myroot = find_root(a.parent, myroot, a.err);
@@ -563,18 +559,37 @@ __global__ void __launch_bounds__(32 * kWpb) k_crit_warp(FofArgs a) {
   }
 }
 
-// max |v| over the velocities (non-negative floats order like their bits)
-__global__ void k_vel_absmax(const V4* vel, int n, unsigned* out) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  float m = 0.f;
-  if (i < n) {
-    V4 v = vel[i];
-    m = fmaxf(fabsf(__double2float_ru(fabs(v.x))),
-              fmaxf(fabsf(__double2float_ru(fabs(v.y))), fabsf(__double2float_ru(fabs(v.z)))));
+// The phase-space tree's components carried to the physical tree: each particle is united
+// with its component's root (perm6: phase-space tree index -> physical tree index).
+__global__ void k_carry_roots(const int* parent6, const int* perm6, int* parent, int n,
+                              int* err) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  int r = j;
+  for (int it = 0; it < kCap; it++) {
+    int p = parent6[r];
+    if (p == r) break;
+    r = p;
   }
-  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+  if (r != j) unite(parent, perm6[j], perm6[r], err);
 }
+
+// Positions, velocities and masses of a tree, in its order, as n x 3 arrays (the input
+// layout of a build).
+__global__ void k_unpack(const P4* pos, const V4* vel, double* p3, double* v3, double* m, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  P4 p = pos[i];
+  V4 v = vel[i];
+  p3[3 * (size_t)i] = p.x;
+  p3[3 * (size_t)i + 1] = p.y;
+  p3[3 * (size_t)i + 2] = p.z;
+  v3[3 * (size_t)i] = v.x;
+  v3[3 * (size_t)i + 1] = v.y;
+  v3[3 * (size_t)i + 2] = v.z;
+  m[i] = p.m;
+}
+
 
 // FOFCriterion on a phase-space tree (KDFOF.cxx:157-265 with FOFSearchCriterion[Periodic],
 // KDSplitNode.cxx:991-1030, 1649-1682, KDLeafNode.cxx:591-619): every particle walks the
@@ -820,6 +835,74 @@ __global__ void k_relabel(int* group, const int* newlbl, int n) {
 
 }  // namespace
 
+// FOF6d inside its search region on a physical tree (see k_crit6_warp): builds the
+// phase-space tree of the same particles, links on it, and unites the physical tree's
+// parent forest accordingly.
+static int link_fof6d_phase_tree(const FofArgs& a, DevAlloc& alloc, cudaStream_t st) {
+  const int n = a.tv.n;
+  const int b = a.tv.b;
+  double *p3, *v3, *m;
+  NBK_TRY(alloc.get((void**)&p3, sizeof(double) * 3 * (size_t)n));
+  NBK_TRY(alloc.get((void**)&v3, sizeof(double) * 3 * (size_t)n));
+  NBK_TRY(alloc.get((void**)&m, sizeof(double) * (size_t)n));
+  k_unpack<<<(n + 255) / 256, 256, 0, st>>>(a.tv.pos + a.tv.pstart, a.tv.vel + a.tv.pstart, p3,
+                                             v3, m, n);
+  note_launch();
+  const int64_t slots = heap_slots(n, b);
+  BuiltArrays A6;
+  NBK_TRY(alloc.get((void**)&A6.pos, sizeof(P4) * (size_t)n));
+  NBK_TRY(alloc.get((void**)&A6.posf, sizeof(float4) * (size_t)n));
+  NBK_TRY(alloc.get((void**)&A6.vel, sizeof(V4) * (size_t)n));
+  NBK_TRY(alloc.get((void**)&A6.velf, sizeof(float4) * (size_t)n));
+  NBK_TRY(alloc.get((void**)&A6.perm, sizeof(int) * (size_t)n));
+  NBK_TRY(alloc.get((void**)&A6.nodes6, sizeof(NodeS) * (size_t)slots));
+  NBK_TRY(alloc.get((void**)&A6.nodeb6, sizeof(NodeB6) * (size_t)slots));
+  NBK_TRY(alloc.get((void**)&A6.nodef6, sizeof(NodeF6) * (size_t)slots));
+  NBK_CUDA_TRY(cudaMemsetAsync(A6.nodes6, 0, sizeof(NodeS) * (size_t)slots, st));
+  NodeB6 root;
+  {
+    DevAlloc alloc6;  // the build releases its own scratch when it ends
+    alloc6.st = st;
+    std::vector<TreeSpec> trees{{0, n, 0}};
+    NBK_TRY(build_forest_phase(trees, b, p3, m, v3, A6, alloc6, st, &root));
+  }
+  FofArgs f = a;
+  TreeView& v = f.tv;
+  v = TreeView{};
+  v.pos = A6.pos;
+  v.posf = A6.posf;
+  v.vel = A6.vel;
+  v.velf = A6.velf;
+  v.perm = A6.perm;
+  v.nodes6 = A6.nodes6;
+  v.nodeb6 = A6.nodeb6;
+  v.nodef6 = A6.nodef6;
+  v.n = n;
+  v.b = b;
+  v.periodic = a.tv.periodic;
+  for (int d = 0; d < 3; d++) v.period[d] = a.tv.period[d];
+  for (int d = 0; d < 6; d++) {
+    double mx = std::max(std::fabs(root.lo[d]), std::fabs(root.hi[d])) +
+                (d < 3 ? v.period[d] : 0.0);
+    v.eps6[d] = (float)std::ldexp(mx, -23) * 1.0001f + 1e-38f;
+  }
+  v.eps = a.tv.eps;
+  int* parent6;
+  NBK_TRY(alloc.get((void**)&parent6, sizeof(int) * (size_t)n));
+  k_iota<<<(n + 255) / 256, 256, 0, st>>>(parent6, n);
+  note_launch();
+  f.parent = parent6;
+  const int warps = (n + 31) / 32;
+  k_crit6_warp<<<(warps + kWpb - 1) / kWpb, 32 * kWpb, 0, st>>>(f);
+  note_launch();
+  // the phase-space tree's "input" order is the physical tree's order: perm6 maps to it
+  k_carry_roots<<<(n + 255) / 256, 256, 0, st>>>(parent6, A6.perm, a.parent + a.tv.pstart, n,
+                                                 a.err);
+  note_launch();
+  NBK_CUDA_TRY(cudaGetLastError());
+  return NBK_OK;
+}
+
 int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tree,
             int* h_ngroup, DevAlloc& alloc, cudaStream_t st) {
   (void)nnodes;
@@ -857,23 +940,9 @@ int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tr
   } else if (fof3d) {
     Phase ph("fof_criterion_link", st);
     k_link<true><<<(warps + kWpb - 1) / kWpb, 32 * kWpb, 0, st>>>(f); note_launch();
-  } else if (a.crit && a.crit_contained) {
+  } else if (a.crit && a.crit_contained && a.cmp == 2) {
     Phase ph("fof_criterion_link", st);
-    FofArgs b = a;
-    if (a.cmp == 2) {
-      // FP32 rounding bound of the velocities: max |v| * 2^-23
-      unsigned* d_m;
-      NBK_TRY(alloc.get((void**)&d_m, sizeof(unsigned)));
-      NBK_CUDA_TRY(cudaMemsetAsync(d_m, 0, sizeof(unsigned), st));
-      k_vel_absmax<<<(n + 255) / 256, 256, 0, st>>>(a.tv.vel, n, d_m); note_launch();
-      unsigned hm = 0;
-      NBK_CUDA_TRY(cudaMemcpyAsync(&hm, d_m, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-      NBK_CUDA_TRY(cudaStreamSynchronize(st));
-      float vmax;
-      memcpy(&vmax, &hm, sizeof(float));
-      b.eps_v = std::ldexp(vmax, -23) * 1.0001f + 1e-38f;
-    }
-    k_crit_warp<<<(warps + kWpb - 1) / kWpb, 32 * kWpb, 0, st>>>(b); note_launch();
+    NBK_TRY(link_fof6d_phase_tree(a, alloc, st));
   } else if (a.crit) {
     Phase ph("fof_criterion_link", st);
     k_crit_link<<<(n + 127) / 128, 128, 0, st>>>(a); note_launch();

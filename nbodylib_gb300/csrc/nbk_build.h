@@ -174,7 +174,6 @@ struct FofArgs {
   int crit_contained;  // crit 1: every pair the comparator accepts lies inside the search
                        //   region (FOF3d / FOF6d with params[6] <= the position search
                        //   distance^2), so reachability follows from the comparator
-  float eps_v;         // crit 1: bound on |v - float(v)| for the velocities
 };
 int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tree,
             int* h_ngroup, DevAlloc& alloc, cudaStream_t st);

@@ -341,6 +341,20 @@ __device__ __forceinline__ float pair_lb6f(const float q[6], const float c[6], c
   return s;
 }
 
+// FP32 upper bound of sum_j w[j] * (x_j - y_j)^2 (w rounded up), the counterpart of
+// pair_lb6f: below a threshold under 1 it proves the FP64 sum is below 1.
+__device__ __forceinline__ float pair_ub6f(const float q[6], const float c[6], const float w[6],
+                                           const float eps[6]) {
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    float g = __fadd_ru(q[j] >= c[j] ? __fsub_ru(q[j], c[j]) : __fsub_ru(c[j], q[j]),
+                        __fmul_ru(2.f, eps[j]));
+    s = __fadd_ru(s, __fmul_ru(__fmul_ru(w[j], g), g));
+  }
+  return s;
+}
+
 // ---- device error word: kernels report bounded-wait and capacity failures here
 enum DeviceErr : int {
   kErrNone = 0,
