@@ -1457,9 +1457,15 @@ int nbk_fof_criterion(nbk_tree* t, int comparator, const double* params, int32_t
     // from the comparator and the warp-cooperative search applies
     int tt = (int)p[0];
     double s1 = (tt == NBK_TPHYS || tt == NBK_TPHS) ? p[1] : (tt == NBK_TVEL ? p[2] : 1.0);
-    a.crit_contained = t->treetype == NBK_TPHYS &&
-                       (comparator == NBK_FOF3D || comparator == NBK_FOF6D) && p[6] > 0 &&
-                       s1 > 0 && p[6] <= s1 && (comparator != NBK_FOF6D || p[7] > 0);
+    if (t->treetype == NBK_TPHYS) {
+      a.crit_contained = (comparator == NBK_FOF3D || comparator == NBK_FOF6D) && p[6] > 0 &&
+                         s1 > 0 && p[6] <= s1 && (comparator != NBK_FOF6D || p[7] > 0);
+    } else {
+      // a phase-space tree also cuts velocities, scaled by 1/params[2] for TPHS params
+      double s2 = tt == NBK_TPHS ? p[2] : s1;
+      a.crit_contained = comparator == NBK_FOF6D && p[6] > 0 && p[7] > 0 && s1 > 0 && s2 > 0 &&
+                         p[6] <= s1 && p[7] <= s2;
+    }
   }
   a.parent = parent;
   a.err = t->d_err;

@@ -934,6 +934,10 @@ int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tr
   if (a.crit == 2) {
     Phase ph("fof_nn_link", st);
     k_nn_link<<<(n + 255) / 256, 256, 0, st>>>(a); note_launch();
+  } else if (a.crit && a.tv.nodes6 && a.crit_contained) {
+    // FOF6d inside the search region on a phase-space tree: the warp search directly
+    Phase ph("fof_criterion_link", st);
+    k_crit6_warp<<<(warps + kWpb - 1) / kWpb, 32 * kWpb, 0, st>>>(a); note_launch();
   } else if (a.crit && a.tv.nodes6) {
     Phase ph("fof_criterion_link", st);
     k_crit_link6<<<(n + 127) / 128, 128, 0, st>>>(a); note_launch();
