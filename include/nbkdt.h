@@ -62,6 +62,10 @@ extern "C" {
 /* ---- kNN variants ---- */
 #define NBK_FINDNEAREST 0    /* KDTree::FindNearest(tt, ...)    (KDFindNearest.cxx:247-318) */
 #define NBK_FINDNEARESTPOS 1 /* KDTree::FindNearestPos(tt, ...) (KDFindNearest.cxx:320-334) */
+#define NBK_FINDNEARESTVEL 2 /* KDTree::FindNearestVel(tt, ...) (KDFindNearest.cxx:335-346),
+                                velocity trees */
+#define NBK_FINDNEARESTPHASE 3 /* KDTree::FindNearestPhase(tt, ...) (KDFindNearest.cxx:347-361),
+                                  phase-space trees: the plain phase distance whatever Aniso */
 
 /* ---- periodic image modes ---- */
 /* Reproduce the reference's image gates exactly, including its comparison of a squared
@@ -152,7 +156,8 @@ int nbk_get_kernel(const nbk_tree* tree, double* table, double* kernnorm);
  * k nearest neighbours of every particle. Replaces KDTree::FindNearest(Int_t** nn,
  * Double_t** dist2, Int_t Nsearch) and FindNearestPos(Int_t**, Double_t**, Int_t)
  * (KDFindNearest.cxx:444-456), i.e. FindNearest(tt)/FindNearestPos(tt) for every tt.
- * variant: NBK_FINDNEAREST or NBK_FINDNEARESTPOS; periodic_mode as above.
+ * variant: NBK_FINDNEAREST, NBK_FINDNEARESTPOS (physical trees), NBK_FINDNEARESTVEL
+ * (velocity trees) or NBK_FINDNEARESTPHASE (phase-space trees); periodic_mode as above.
  * nn, d2: n x k, row t = the particle at tree index t; neighbours are tree indices in
  * ascending squared distance. Non-periodic trees exclude the particle itself and any
  * particle at distance 0 (KDLeafNode.cxx:19-21); periodic FindNearest drops the nearest
@@ -180,6 +185,12 @@ int nbk_knn_points(nbk_tree* tree, const double* x, int64_t nq, int k, int perio
    x, y, z, vx, vy, vz (phase-space tree: the plain or local-metric search with the
    ungated position images of a periodic tree, KDSplitNode.cxx:1153-1218). */
 int nbk_knn_coords(nbk_tree* tree, const double* x, int64_t nq, int k, int32_t* nn, double* d2);
+
+/* KDTree::FindNearestPhase(Double_t* x, Double_t* v, ...) (KDFindNearest.cxx:542-560) on a
+   phase-space tree: the plain phase distance around nq points (x, y, z, vx, vy, vz per
+   row), with the ungated position images of a periodic tree, whatever the tree's Aniso. */
+int nbk_knn_phase_points(nbk_tree* tree, const double* x, int64_t nq, int k, int32_t* nn,
+                         double* d2);
 
 /*
  * SPH density of every particle. Replaces KDTree::CalcDensity(Int_t Nsmooth)

@@ -163,6 +163,32 @@ class KDTree {
   void FindNearestPos(Coordinate x, Int_t* nn, Double_t* dist2, Int_t Nsearch = 64) {
     FindNearestPos(x.GetCoord(), nn, dist2, Nsearch);
   }
+  // velocity trees: FindNearestVel (KDFindNearest.cxx:335-346, 451-453, 530-541)
+  void FindNearestVel(Int_t tt, Int_t* nn, Double_t* dist2, Int_t Nsearch = 64) {
+    knn_one(tt, nn, dist2, Nsearch, NBK_FINDNEARESTVEL);
+  }
+  void FindNearestVel(Int_t** nn, Double_t** dist2, Int_t Nsearch = 64) {
+    knn_all(nn, dist2, Nsearch, NBK_FINDNEARESTVEL);
+  }
+  void FindNearestVel(Double_t* v, Int_t* nn, Double_t* dist2, Int_t Nsearch = 64) {
+    if (treetype_ != TVEL)
+      throw nbkdt::Error(NBK_ERR_UNSUPPORTED, "FindNearestVel(v) runs on velocity trees only");
+    FindNearest(v, nn, dist2, Nsearch);
+  }
+  // phase-space trees: FindNearestPhase, the plain phase distance whatever Aniso
+  // (KDFindNearest.cxx:347-361, 454-456, 542-560)
+  void FindNearestPhase(Int_t tt, Int_t* nn, Double_t* dist2, Int_t Nsearch = 64) {
+    knn_one(tt, nn, dist2, Nsearch, NBK_FINDNEARESTPHASE);
+  }
+  void FindNearestPhase(Int_t** nn, Double_t** dist2, Int_t Nsearch = 64) {
+    knn_all(nn, dist2, Nsearch, NBK_FINDNEARESTPHASE);
+  }
+  void FindNearestPhase(Double_t* x, Double_t* v, Int_t* nn, Double_t* dist2, Int_t Nsearch = 64) {
+    Double_t xv[6] = {x[0], x[1], x[2], v[0], v[1], v[2]};
+    std::vector<int32_t> n32(Nsearch);
+    nbkdt::check(nbk_knn_phase_points(tree_, xv, 1, Nsearch, n32.data(), dist2));
+    for (Int_t j = 0; j < Nsearch; j++) nn[j] = n32[j];
+  }
 
   // ---- ball search (KDTree.h:341-373)
   void SearchBallPos(Int_t tt, Double_t fdist2, Int_t imark, Int_t* nn, Double_t* dist2) {

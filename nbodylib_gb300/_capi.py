@@ -40,6 +40,7 @@ SIGNATURES = {
     "nbk_knn": (c_int, [c_vp, c_int, c_int, c_int, c_vp, c_vp]),
     "nbk_knn_points": (c_int, [c_vp, c_vp, c_i64, c_int, c_int, c_vp, c_vp]),
     "nbk_knn_coords": (c_int, [c_vp, c_vp, c_i64, c_int, c_vp, c_vp]),
+    "nbk_knn_phase_points": (c_int, [c_vp, c_vp, c_i64, c_int, c_vp, c_vp]),
     "nbk_knn_targets": (c_int, [c_vp, c_vp, c_i64, c_int, c_int, c_int, c_vp, c_vp]),
     "nbk_density": (c_int, [c_vp, c_int, c_vp]),
     "nbk_density_noalloc": (c_int, [c_vp, c_int, c_vp]),

@@ -693,7 +693,7 @@ int nbk_get_kernel(const nbk_tree* t, double* table, double* kernnorm) {
 // (phase.cu). A periodic target search grows the heap by one and drops its nearest entry
 // (KDFindNearest.cxx:250, 310).
 static int phase_nn(nbk_tree* t, int qmode, const int* dq, const double* dx, int64_t nq, int k,
-                    int* dnn, double* dd2) {
+                    int* dnn, double* dd2, bool metric) {
   PhaseArgs pa{};
   pa.k = base_args(t);
   pa.k.periodic = t->periodic ? 1 : 0;
@@ -705,18 +705,26 @@ static int phase_nn(nbk_tree* t, int qmode, const int* dq, const double* dx, int
   pa.k.nq = (int)nq;
   pa.k.nn = dnn;
   pa.k.d2 = dd2;
-  pa.metric = t->aniso == 0;
+  pa.metric = metric ? 1 : 0;
   pa.spacing_periodic = t->periodic ? 1 : 0;
   pa.epi = kPhNN;
   return launch_phase(pa, t->st);
 }
 
 static int knn_variant_ok(const nbk_tree* t, int variant, const char* what) {
-  if (t->treetype != NBK_TPHYS && variant != NBK_FINDNEAREST) {
-    set_error(std::string(what) + ": FindNearestPos runs on physical trees only");
+  if (variant < NBK_FINDNEAREST || variant > NBK_FINDNEARESTPHASE) {
+    set_error(std::string(what) + ": unknown variant");
+    return NBK_ERR_INVALID;
+  }
+  static const int tree_of[4] = {-1, NBK_TPHYS, NBK_TVEL, NBK_TPHS};
+  static const char* name_of[4] = {"", "FindNearestPos", "FindNearestVel", "FindNearestPhase"};
+  if (variant != NBK_FINDNEAREST && t->treetype != tree_of[variant]) {
+    set_error(std::string(what) + ": " + name_of[variant] + " runs on " +
+              (variant == NBK_FINDNEARESTPOS ? "physical" :
+               variant == NBK_FINDNEARESTVEL ? "velocity" : "phase-space") + " trees only");
     return NBK_ERR_UNSUPPORTED;
   }
-  if (t->treetype == NBK_TPHS && t->n < 8 && t->aniso == 0) {
+  if (t->treetype == NBK_TPHS && t->n < 8 && t->aniso == 0 && variant == NBK_FINDNEAREST) {
     set_error(std::string(what) + ": the local metric needs at least 8 particles (the reference exits)");
     return NBK_ERR_TOO_FEW;
   }
@@ -730,10 +738,6 @@ int nbk_knn(nbk_tree* t, int k, int variant, int periodic_mode, int32_t* nn, dou
     set_error("nbk_knn: k must be >= 1 and outputs non-null");
     return NBK_ERR_INVALID;
   }
-  if (variant != NBK_FINDNEAREST && variant != NBK_FINDNEARESTPOS) {
-    set_error("nbk_knn: unknown variant");
-    return NBK_ERR_INVALID;
-  }
   NBK_TRY(knn_variant_ok(t, variant, "nbk_knn"));
   Stage S(t);
   int *dnn;
@@ -742,7 +746,8 @@ int nbk_knn(nbk_tree* t, int k, int variant, int periodic_mode, int32_t* nn, dou
   NBK_TRY(S.out(d2, (size_t)t->n * k, &dd2));
   NBK_TRY(clear_err(t));
   if (t->treetype == NBK_TPHS) {
-    NBK_TRY(phase_nn(t, 0, nullptr, nullptr, t->n, k, dnn, dd2));
+    NBK_TRY(phase_nn(t, 0, nullptr, nullptr, t->n, k, dnn, dd2,
+                     t->aniso == 0 && variant != NBK_FINDNEARESTPHASE));
     NBK_TRY(S.finish());
     if (!t->dev()) NBK_TRY(check_err(t, "nbk_knn"));
     return NBK_OK;
@@ -775,10 +780,6 @@ int nbk_knn_targets(nbk_tree* t, const int32_t* targets, int64_t nt, int k, int 
     set_error("nbk_knn_targets: invalid argument");
     return NBK_ERR_INVALID;
   }
-  if (variant != NBK_FINDNEAREST && variant != NBK_FINDNEARESTPOS) {
-    set_error("nbk_knn_targets: unknown variant");
-    return NBK_ERR_INVALID;
-  }
   NBK_TRY(knn_variant_ok(t, variant, "nbk_knn_targets"));
   if (nt == 0) return NBK_OK;
   if (!t->dev())
@@ -796,7 +797,8 @@ int nbk_knn_targets(nbk_tree* t, const int32_t* targets, int64_t nt, int k, int 
   NBK_TRY(S.out(d2, (size_t)nt * k, &dd2));
   NBK_TRY(clear_err(t));
   if (t->treetype == NBK_TPHS) {
-    NBK_TRY(phase_nn(t, 2, dt, nullptr, nt, k, dnn, dd2));
+    NBK_TRY(phase_nn(t, 2, dt, nullptr, nt, k, dnn, dd2,
+                     t->aniso == 0 && variant != NBK_FINDNEARESTPHASE));
     NBK_TRY(S.finish());
     if (!t->dev()) NBK_TRY(check_err(t, "nbk_knn_targets"));
     return NBK_OK;
@@ -877,7 +879,7 @@ int nbk_knn_coords(nbk_tree* t, const double* x, int64_t nq, int k, int32_t* nn,
   NBK_TRY(S.out(d2, (size_t)nq * k, &dd2));
   NBK_TRY(clear_err(t));
   if (t->treetype == NBK_TPHS) {
-    NBK_TRY(phase_nn(t, 1, nullptr, dx, nq, k, dnn, dd2));
+    NBK_TRY(phase_nn(t, 1, nullptr, dx, nq, k, dnn, dd2, t->aniso == 0));
   } else {  // velocity tree (never periodic): FindNearestVel(x) over the swapped arrays
     KnnArgs a = base_args(t);
     a.kheap = k;
@@ -893,6 +895,31 @@ int nbk_knn_coords(nbk_tree* t, const double* x, int64_t nq, int k, int32_t* nn,
   }
   NBK_TRY(S.finish());
   if (!t->dev()) NBK_TRY(check_err(t, "nbk_knn_coords"));
+  return NBK_OK;
+  API_END
+}
+
+int nbk_knn_phase_points(nbk_tree* t, const double* x, int64_t nq, int k, int32_t* nn,
+                         double* d2) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  if (k < 1 || !x || !nn || !d2 || nq < 0) {
+    set_error("nbk_knn_phase_points: invalid argument");
+    return NBK_ERR_INVALID;
+  }
+  NBK_TRY(knn_variant_ok(t, NBK_FINDNEARESTPHASE, "nbk_knn_phase_points"));
+  if (nq == 0) return NBK_OK;
+  Stage S(t);
+  const double* dx;
+  int* dnn;
+  double* dd2;
+  NBK_TRY(S.in(x, (size_t)nq * 6, &dx));
+  NBK_TRY(S.out(nn, (size_t)nq * k, &dnn));
+  NBK_TRY(S.out(d2, (size_t)nq * k, &dd2));
+  NBK_TRY(clear_err(t));
+  NBK_TRY(phase_nn(t, 1, nullptr, dx, nq, k, dnn, dd2, false));
+  NBK_TRY(S.finish());
+  if (!t->dev()) NBK_TRY(check_err(t, "nbk_knn_phase_points"));
   return NBK_OK;
   API_END
 }

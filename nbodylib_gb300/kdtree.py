@@ -16,7 +16,7 @@ from . import _capi
 
 TPHYS, TPROJ, TVEL, TPHS, TMETRIC = 0, 1, 2, 3, 4
 KSPH, KGAUSS, KEPAN, KTH = 0, 1, 2, 3
-FINDNEAREST, FINDNEARESTPOS = 0, 1
+FINDNEAREST, FINDNEARESTPOS, FINDNEARESTVEL, FINDNEARESTPHASE = 0, 1, 2, 3
 PERIODIC_REF, PERIODIC_MIN_IMAGE = 0, 1
 FOF3D, FOFVEL, FOF6D = 0, 1, 2
 DEVICE_PTRS = 1
@@ -149,6 +149,33 @@ class KDTree:
         d2 = self._empty((nq, k), np.float64)
         _capi.check(self._lib.nbk_knn_points(self._h, _ptr(x), nq, k, periodic_mode, _ptr(nn),
                                              _ptr(d2)))
+        return nn, d2
+
+    def FindNearestPhase(self, k):
+        """FindNearestPhase(tt) for every particle of a phase-space tree: the plain phase
+        distance whatever the tree's aniso (KDFindNearest.cxx:347-361)."""
+        nn = self._empty((self.n, k), np.int32)
+        d2 = self._empty((self.n, k), np.float64)
+        _capi.check(self._lib.nbk_knn(self._h, k, FINDNEARESTPHASE, PERIODIC_REF, _ptr(nn),
+                                      _ptr(d2)))
+        return nn, d2
+
+    def FindNearestVel(self, k):
+        """FindNearestVel(tt) for every particle of a velocity tree."""
+        nn = self._empty((self.n, k), np.int32)
+        d2 = self._empty((self.n, k), np.float64)
+        _capi.check(self._lib.nbk_knn(self._h, k, FINDNEARESTVEL, PERIODIC_REF, _ptr(nn),
+                                      _ptr(d2)))
+        return nn, d2
+
+    def FindNearestPhasePoints(self, x, k):
+        """FindNearestPhase(Double_t *x, Double_t *v) for rows (x, y, z, vx, vy, vz)."""
+        if not self.device:
+            x = np.ascontiguousarray(x, np.float64).reshape(-1, 6)
+        nq = x.shape[0]
+        nn = self._empty((nq, k), np.int32)
+        d2 = self._empty((nq, k), np.float64)
+        _capi.check(self._lib.nbk_knn_phase_points(self._h, _ptr(x), nq, k, _ptr(nn), _ptr(d2)))
         return nn, d2
 
     def FindNearestTargets(self, targets, k, variant=FINDNEAREST, periodic_mode=PERIODIC_REF):

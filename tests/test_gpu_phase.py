@@ -195,3 +195,31 @@ def test_phase_too_few_particles_for_the_metric(gpu):
     with pytest.raises(NbkError):
         t.FindNearest(3)  # the metric spacing needs 8 particles (the reference exits)
     t.close()
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_findnearestphase_and_vel_variants_vs_reference_golden(gpu, periodic):
+    """KDTree::FindNearestPhase on a tree built with the local metric (Aniso 0) searches
+    with the plain phase distance, so it returns the reference's plain results; and
+    FindNearestVel on a velocity tree is its FindNearest."""
+    g = golden("phase_space")
+    tag = "plain" + ("_per" if periodic else "")
+    t = _gpu_tree(g, TPHS, 0, periodic)
+    k = g[f"phs_{tag}_nn"].shape[1]
+    nn, d2 = t.FindNearestPhase(k)
+    ids, dd = _ids_rows(t, nn, d2)
+    assert_knn_equal(ids, dd, g[f"phs_{tag}_nn"], g[f"phs_{tag}_d2"], f"FindNearestPhase {tag}")
+    nn, d2 = t.FindNearestPhasePoints(g["points6"], k)
+    assert_knn_equal(to_ids(nn, np.asarray(t.GetPerm())), d2, g[f"phs_{tag}_pt_nn"],
+                     g[f"phs_{tag}_pt_d2"], f"FindNearestPhase(x, v) {tag}")
+    with pytest.raises(NbkError):
+        t.FindNearestVel(k)
+    t.close()
+    if not periodic:
+        tv = _gpu_tree(g, TVEL, 0, False)
+        nn, d2 = tv.FindNearestVel(int(g["vel_nn"].shape[1]))
+        ids, dd = _ids_rows(tv, nn, d2)
+        assert_knn_equal(ids, dd, g["vel_nn"], g["vel_d2"], "FindNearestVel")
+        with pytest.raises(NbkError):
+            tv.FindNearestPhase(4)
+        tv.close()
