@@ -21,6 +21,7 @@ import ctypes
 import json
 import os
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -61,7 +62,10 @@ class ClockSampler:
     def __init__(self, index=0):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        # raw samples go to NBKDT_CLOCKS_DIR (default: the system temp directory); the
+        # summary goes into the JSON line
+        out_dir = os.environ.get("NBKDT_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(out_dir, f"clocks_bench_{os.getpid()}.csv")
 
     def __enter__(self):
         try:
