@@ -202,6 +202,7 @@ __global__ void __launch_bounds__(32 * kWpb, 4) k_link(FofArgs a) {
     int sp = 1;
     if (lane == 0) w.stk[0] = 0;
     __syncwarp();
+    const int first = tv.pstart + (blockIdx.x * kWpb + warp) * 32;  // lane 0's particle
     for (int guard = 0; sp > 0 && guard < (1 << 26); guard++) {
       // above kBatchLimit entries pop one node at a time: a depth-first descent from
       // there adds at most the tree depth, so the stack never exceeds kFStack
@@ -212,7 +213,10 @@ __global__ void __launch_bounds__(32 * kWpb, 4) k_link(FofArgs a) {
       if (lane < m) {
         h = w.stk[sp - 1 - lane];
         r = tv.node[tv.nbase + h];
-        keep = boxbox_d2_lo(r, qlo, qhi) < thr;
+        // direct pass: a node wholly before the warp's first particle in tree order only
+        // holds pairs that particle's own search tests (each pair once, from its lower
+        // index), so it is not opened
+        keep = boxbox_d2_lo(r, qlo, qhi) < thr && (pass != 0 || r.start + r.count - 1 > first);
         cpt = keep && node_compact(r, ll2_lo);
         if (cpt) root = find_root(a.parent, r.start, a.err);
       }
