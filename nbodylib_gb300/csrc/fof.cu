@@ -488,6 +488,7 @@ __global__ void __launch_bounds__(32 * kWpb) k_crit6_warp(FofArgs a) {
   const NodeS* N = tv.nodes6 + tv.nbase;
   const NodeF6* F = tv.nodef6 + tv.nbase;
   int myroot = find_root(a.parent, self, a.err);
+  const int first = tv.pstart + (blockIdx.x * kWpb + warp) * 32;  // lane 0's particle
   const int npass = (tv.periodic && N[0].split_dim >= 0) ? 8 : 1;
   for (int pass = 0; pass < npass; pass++) {
     double xq[6] = {x0[0], x0[1], x0[2], mv.x, mv.y, mv.z};
@@ -511,9 +512,12 @@ __global__ void __launch_bounds__(32 * kWpb) k_crit6_warp(FofArgs a) {
       const int h = w.stk[sp - 1];
       sp--;
       __syncwarp();
-      const bool need = active && box_lb6f(q32, w_lo, e32, F[h]) < thr_hi;
-      if (!__any_sync(FULL, need)) continue;
       const NodeS nd = N[h];
+      // direct pass: nodes wholly before the warp's first particle hold only pairs tested
+      // from their lower index
+      const bool need = active && box_lb6f(q32, w_lo, e32, F[h]) < thr_hi &&
+                        (pass != 0 || nd.start + nd.count - 1 > first);
+      if (!__any_sync(FULL, need)) continue;
       if (nd.split_dim >= 0) {
         if (sp + 2 > kCritStack) {
           if (lane == 0) atomicExch(a.err, kErrCapacity);
