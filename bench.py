@@ -35,9 +35,9 @@ N_FOF = 1 << 20
 BOX = 100.0
 MINNUM = 20
 BUCKET = 16
-# DRAM bytes of one k_link launch at 2^20 particles: 241.7 MB measured by ncu on the same
+# DRAM bytes of one k_link launch at 2^20 particles: 240.4 MB measured by ncu on the same
 # recipe at 2^22 particles (the bench's --profile fof case), divided by 4
-K_LINK_DRAM_BYTES_PER_LAUNCH = 241.678e6 / 4
+K_LINK_DRAM_BYTES_PER_LAUNCH = 240.435e6 / 4
 
 
 def log(*a):
