@@ -113,8 +113,12 @@ def dist_setup():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
+        import torch
         import torch.distributed as dist
-        dist.init_process_group("nccl")
+        # replicas only: the process group carries the barrier and the max over ranks
+        backend = os.environ.get("NBKDT_DIST_BACKEND") or (
+            "nccl" if torch.cuda.is_available() else "gloo")
+        dist.init_process_group(backend)
     return world, rank, local
 
 
@@ -129,7 +133,8 @@ def max_over_ranks(x, world):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
