@@ -58,7 +58,7 @@ __device__ void run_warp(const KnnArgs& a, const TreeView& tv, WarpSmem<KMAX>& w
     for (int s = 0; s < K; s++) {
       double d2 = w.hd[s][lane];
       int j = w.hi[s][lane];
-      double q = dmul(__dsqrt_rn(d2), ih);
+      double q = dmul(sqrt_newton(d2), ih);
       double wij = dmul(wsm_line(q, kr, inv_delta, T), wnorm);
       double mj = tv.pos[j].m;
       acc = dadd(acc, dmul(wij, mj));
@@ -76,7 +76,7 @@ __device__ void run_warp(const KnnArgs& a, const TreeView& tv, WarpSmem<KMAX>& w
     V4 vi = tv.vel[self];
     for (int s = 0; s < K; s++) {
       V4 vj = tv.vel[w.hi[s][lane]];
-      w.hd[s][lane] = __dsqrt_rn(dist2_exact(vi.x, vi.y, vi.z, vj.x, vj.y, vj.z));
+      w.hd[s][lane] = sqrt_newton(dist2_exact(vi.x, vi.y, vi.z, vj.x, vj.y, vj.z));
     }
     int ns = a.nsmooth;
     if (ns < K) {

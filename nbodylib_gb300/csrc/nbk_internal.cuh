@@ -355,6 +355,19 @@ __device__ __forceinline__ float pair_ub6f(const float q[6], const float c[6], c
   return s;
 }
 
+// sqrt(x) for the kernel interpolation, to about 2e-14 relative: the FP32 square root as
+// the start and one Newton-Raphson (Heron) step in FP64, q0 + (x - q0^2) / (2 q0), whose
+// correction uses an FP32 reciprocal (its error only scales the already small correction).
+// Outside the FP32 normal range it falls back to the FP64 square root.
+__device__ __forceinline__ double sqrt_newton(double x) {
+  const float xf = __double2float_rn(x);
+  if (!(xf > 1e-30f && xf < 1e30f)) return __dsqrt_rn(x);
+  const float q0f = sqrtf(xf);
+  const double q0 = (double)q0f;
+  const double half_inv = (double)__fdividef(0.5f, q0f);
+  return __fma_rn(__fma_rn(-q0, q0, x), half_inv, q0);
+}
+
 // ---- device error word: kernels report bounded-wait and capacity failures here
 enum DeviceErr : int {
   kErrNone = 0,
