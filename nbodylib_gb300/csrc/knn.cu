@@ -55,11 +55,16 @@ __device__ void run_warp(const KnnArgs& a, const TreeView& tv, WarpSmem<KMAX>& w
     double norm = dmul(dmul(ih, ih), ih);  // 1 / h^3 (the reference takes pow(h, 3))
     double wnorm = EPI == kEpiDensPart ? norm : 0.5 * norm;
     double acc = 0.0;
+    const long long topk = dkey(top);
     for (int s = 0; s < K; s++) {
       double d2 = w.hd[s][lane];
       int j = w.hi[s][lane];
+      // the farthest neighbour sits at q = 2 exactly in the reference's arithmetic (the
+      // table's last entry, 0 for the compact kernels); the product with 1/h could land
+      // an ulp below it, in the previous cell
       double q = dmul(sqrt_newton(d2), ih);
-      double wij = dmul(wsm_line(q, kr, inv_delta, T), wnorm);
+      double wq = dkey(d2) == topk ? T[kr - 1] : wsm_line(q, kr, inv_delta, T);
+      double wij = dmul(wq, wnorm);
       double mj = tv.pos[j].m;
       acc = dadd(acc, dmul(wij, mj));
       if (EPI != kEpiDensPart) {
@@ -98,8 +103,10 @@ __device__ void run_warp(const KnnArgs& a, const TreeView& tv, WarpSmem<KMAX>& w
     double norm = dmul(dmul(ih, ih), ih);
     double acc = 0.0;
     for (int s = 0; s < ns; s++) {
-      double q = dmul(w.hd[s][lane], ih);
-      acc = dadd(acc, dmul(wsm_line(q, kr, inv_delta, T), norm));
+      const double vd = w.hd[s][lane];
+      double q = dmul(vd, ih);
+      double wq = dkey(vd) == vmaxk ? T[kr - 1] : wsm_line(q, kr, inv_delta, T);  // q = 2
+      acc = dadd(acc, dmul(wq, norm));
     }
     if (EPI == kEpiVelPart) a.vden[qi] = acc;
     else a.vden[self] = acc;

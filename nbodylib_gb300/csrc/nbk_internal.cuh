@@ -368,6 +368,16 @@ __device__ __forceinline__ double sqrt_newton(double x) {
   return __fma_rn(__fma_rn(-q0, q0, x), half_inv, q0);
 }
 
+// W(q) at q = sqrt(d2) / h with h = sqrt(top) / 2 (ih = 1/h): the farthest neighbour
+// (d2 == top) is at q = 2 exactly in the reference's arithmetic, the table's last entry
+// (0 for the compact kernels); the product with 1/h could land an ulp below, in the
+// previous cell.
+__device__ __forceinline__ double w_at_d2(double d2, long long topk, double ih, int size,
+                                          double inv_delta, const double* img) {
+  if (dkey(d2) == topk) return img[size - 1];
+  return wsm_line(dmul(__dsqrt_rn(d2), ih), size, inv_delta, img);
+}
+
 // ---- device error word: kernels report bounded-wait and capacity failures here
 enum DeviceErr : int {
   kErrNone = 0,

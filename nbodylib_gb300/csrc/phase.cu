@@ -518,10 +518,14 @@ __global__ void __launch_bounds__(32 * ph_warps_per_block<KMAX>()) k_phase(Phase
   const double wnorm = scatter ? dmul(0.5, norm) : norm;
   const double mi = tv.pos[self].m;
   double acc = 0.0;
+  const long long topk = dkey(top);
   for (int s = 0; s < K; s++) {
     const int j = w.H.i[s][lane];
     const double rij = __dsqrt_rn(w.H.d[s][lane]);
-    const double wv = dmul(wsm_line(__ddiv_rn(rij, hh), kr, inv_delta, a.kernel), wnorm);
+    // the farthest neighbour: q = 2 exactly, the table's last entry
+    const double wq = dkey(w.H.d[s][lane]) == topk ? a.kernel[kr - 1]
+                                                    : wsm_line(__ddiv_rn(rij, hh), kr, inv_delta, a.kernel);
+    const double wv = dmul(wq, wnorm);
     const double mj = tv.pos[j].m;
     acc = dadd(acc, dmul(wv, mj));
     if (scatter) atomicAdd(&a.rho[j - tv.pstart], dmul(wv, mi));

@@ -68,7 +68,9 @@ __device__ void smooth_warp(const SmoothArgs& s, const TreeView& tv, WarpSmem<KM
       int j = w.hi[q][lane];
       P4 pj = tv.pos[j];
       double rij = __dsqrt_rn(dist2_exact(pi.x, pi.y, pi.z, pj.x, pj.y, pj.z));
-      double vw = dmul(wsm_line(dmul(w.hd[q][lane], vih), kr, inv_delta, T), vnorm);
+      const double vd = w.hd[q][lane];  // the largest |dv| is at q = 2 exactly
+      double vw = dmul(dkey(vd) == vmaxk ? T[kr - 1] : wsm_line(dmul(vd, vih), kr, inv_delta, T),
+                       vnorm);
       double wij = dmul(wsm_line(dmul(rij, ih), kr, inv_delta, T), norm);
       acc = dadd(acc, dmul(vw, dmul(wij / ri, pi.m)));
     }
@@ -79,6 +81,7 @@ __device__ void smooth_warp(const SmoothArgs& s, const TreeView& tv, WarpSmem<KM
 
   // the SPH weights of the Nsmooth nearest: h = half the largest distance
   double ih = 1.0 / (0.5 * __dsqrt_rn(top));
+  const long long topk = dkey(top);
   double norm = dmul(dmul(ih, ih), ih);
   constexpr bool kSym = SM == kSmVel || SM == kSmVelDisp || SM == kSmVelSkew || SM == kSmVelKurt;
   double wnorm = kSym ? 0.5 * norm : norm;  // the symmetric forms carry the 1/2
@@ -98,7 +101,7 @@ __device__ void smooth_warp(const SmoothArgs& s, const TreeView& tv, WarpSmem<KM
     for (int q = 0; q < K; q++) {
       int j = w.hi[q][lane];
       int jd = tv.perm[j];
-      double wij = dmul(wsm_line(dmul(__dsqrt_rn(w.hd[q][lane]), ih), kr, inv_delta, T), wnorm);
+      double wij = dmul(w_at_d2(w.hd[q][lane], topk, ih, kr, inv_delta, T), wnorm);
       P4 pj = tv.pos[j];
       V4 vj = tv.vel[j];
       const double vj3[3] = {vj.x, vj.y, vj.z};
@@ -152,7 +155,7 @@ __device__ void smooth_warp(const SmoothArgs& s, const TreeView& tv, WarpSmem<KM
   for (int q = 0; q < K; q++) {
     int j = w.hi[q][lane];
     int jd = tv.perm[j];
-    double wij = dmul(wsm_line(dmul(__dsqrt_rn(w.hd[q][lane]), ih), kr, inv_delta, T), wnorm);
+    double wij = dmul(w_at_d2(w.hd[q][lane], topk, ih, kr, inv_delta, T), wnorm);
     double ta = dmul(wij / s.rho[jd], tv.pos[j].m);
     if (SM == kSmVelOne || SM == kSmVelDispOne) {
       V4 vj = tv.vel[j];
