@@ -367,6 +367,33 @@ def components(args, lib):
         "roofline_fp64_density": fp64_roofline(20 * 64, n3, ph3.get("knn_density", float("nan"))),
         "phase_ms": {kk: round(v, 4) for kk, v in ph3.items()},
     }
+    if not args.no_cpu:
+        # the reference's CalcDensity / CalcVelDensity are serial loops over particles: the
+        # CPU figure is their per-particle forms on 2000 sampled particles of the full tree
+        import oracle
+        oracle.build(ref=False)
+        threads = os.cpu_count() or 1
+        pos, mass, vel = syn.clustered_box(n3, 250.0, seed=3, velocities=True)
+        t0 = time.perf_counter()
+        o = oracle.OracleTree(pos, vel, mass, BUCKET, 0, 0, 1000, None, backend="port",
+                              nthreads=threads)
+        tb = time.perf_counter() - t0
+        ids = np.random.default_rng(3).choice(n3, 2000, replace=False)
+        t0 = time.perf_counter()
+        for i in ids:
+            o.density_particle(int(i), 64)
+        td = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        for i in ids:
+            o.veldensity_particle(int(i), 64, 64)
+        tv = time.perf_counter() - t0
+        o.close()
+        del pos, mass, vel
+        out["clustered_256cubed_k64_density_veldensity"]["cpu"] = {
+            "kind": "port", "cores": threads, "build_s": tb,
+            "density_queries_per_s": len(ids) / td, "veldensity_queries_per_s": len(ids) / tv,
+            "sample": "tree build with all OpenMP threads; CalcDensityParticle(64) and "
+                      "CalcVelDensityParticle(64, 64) at 2000 random particles, serial"}
     del dpos, dmass, dvel
     torch.cuda.empty_cache()
 
