@@ -558,6 +558,108 @@ def components(args, lib):
                       "(every 64th), local metric, OpenMP over queries"}
     out["phase_space_clustered_2pow20_k32"] = res
     del dpos, dmass, dvel
+    out.update(components_ball_smooth_fofnn(args, lib, flush, reps))
+    return out
+
+
+def components_ball_smooth_fofnn(args, lib, flush, reps):
+    """Ball search, the SPH smoothing family and FOF over neighbour lists, each with the
+    C restatement timed beside it:
+
+    * SearchBallPosTagged(i, r^2) for every particle of a 2^20 uniform periodic unit box,
+      r such that a ball holds 32 particles on average (CSR output of tree indices);
+    * CalcSmoothVel(32) + CalcSmoothVelDisp(32) with the density from CalcDensity(32), on
+      the 2^20 clustered particles with velocities;
+    * FOFNNCriterion (FOF3d, ll = 0.2 mean spacing, minnum 20) over the same tree's
+      FindNearest(16) lists."""
+    import torch
+
+    from nbodylib_gb300 import KDTree
+    from nbodylib_gb300 import synthetic as syn
+    out = {}
+    threads = os.cpu_count() or 1
+    if not args.no_cpu:
+        import oracle
+        oracle.build(ref=False)
+
+    nb = N_FOF
+    pos, mass = syn.uniform_box(nb, 1.0, seed=7)
+    r2 = (3.0 * 32 / (4.0 * np.pi * nb)) ** (2.0 / 3.0)
+    dpos, dmass = torch.from_numpy(pos).cuda(), torch.from_numpy(mass).cuda()
+    t = KDTree(dpos, None, dmass, BUCKET, kerntype=0, period=[1.0] * 3, device=True)
+    tgt = torch.arange(nb, dtype=torch.int32, device="cuda")
+    offs, _ = t.SearchBallPosTagged(tgt, r2)
+    t.sync()
+    pairs = int(offs[-1].item())
+    ball_ms = _timed(lambda: (t.SearchBallPosTagged(tgt, r2), t.sync()), reps, flush)
+    t.close()
+    res = {"n": nb, "fdist2": r2, "found": pairs, "mean_per_ball": pairs / nb,
+           "ms": ball_ms, "queries_per_s": nb / (ball_ms / 1e3),
+           "found_per_s": pairs / (ball_ms / 1e3),
+           "note": "count pass + fill pass through the public call, output allocated per call"}
+    if not args.no_cpu:
+        o = oracle.OracleTree(pos, None, mass, BUCKET, 0, 0, 1000, [1.0] * 3, backend="port",
+                              nthreads=threads)
+        sub = range(0, nb, 64)
+        t0 = time.perf_counter()
+        for i in sub:
+            o.ball_tagged(i, r2)
+        dt = time.perf_counter() - t0
+        o.close()
+        res["cpu"] = {"kind": "port", "cores": 1, "queries_per_s": len(sub) / dt,
+                      "sample": f"SearchBallPosTagged at every 64th particle ({len(sub)}), "
+                                "serial calls"}
+    out["ball_uniform_2pow20_periodic_32_per_ball"] = res
+    del dpos, dmass, tgt
+
+    pos, mass, vel = syn.clustered_box(N_FOF, BOX, seed=2, velocities=True)
+    dpos, dmass, dvel = (torch.from_numpy(a).cuda() for a in (pos, mass, vel))
+    t = KDTree(dpos, dvel, dmass, BUCKET, kerntype=0, device=True)
+    rho = t.CalcDensity(32)
+
+    def smooth():
+        sv = t.CalcSmoothVel(32, rho)
+        t.CalcSmoothVelDisp(sv, 32, rho)
+        t.sync()
+
+    smooth()
+    sm_ms = _timed(smooth, reps, flush)
+    phs = _trace(lib, smooth)
+    res = {"n": N_FOF, "k": 32, "smoothvel_plus_disp_ms": sm_ms,
+           "particles_per_s": N_FOF / (sm_ms / 1e3),
+           "phase_ms": {kk: round(v, 4) for kk, v in phs.items()}}
+    ll = syn.linking_length(N_FOF, BOX)
+    params = [0, 0, 0, 0, 0, 0, ll * ll, 0]
+    nn16, _ = t.FindNearest(16)
+    _, ngn = t.FOFNNCriterion(0, params, nn16, MINNUM)
+    t.sync()
+    fnn_ms = _timed(lambda: (t.FOFNNCriterion(0, params, nn16, MINNUM), t.sync()), reps, flush)
+    resf = {"n": N_FOF, "numnn": 16, "params": params, "minnum": MINNUM, "groups": int(ngn),
+            "fofnn_ms": fnn_ms, "particles_per_s": N_FOF / (fnn_ms / 1e3),
+            "note": "the lists come from FindNearest(16) on the same tree, outside the timing"}
+    rho_h = rho.cpu().numpy()
+    t.close()
+    if not args.no_cpu:
+        o = oracle.OracleTree(pos, vel, mass, BUCKET, 0, 0, 1000, None, backend="port",
+                              nthreads=threads)
+        t0 = time.perf_counter()
+        sv = o.smooth_vel_moments(0, 32, rho=rho_h)
+        o.smooth_vel_moments(1, 32, rho=rho_h, smvel=sv)
+        dt = time.perf_counter() - t0
+        res["cpu"] = {"kind": "port", "cores": 1, "particles_per_s": N_FOF / dt,
+                      "sample": "the full CalcSmoothVel(32) + CalcSmoothVelDisp(32) with the "
+                                "given density, serial as the reference ships them"}
+        pn, _ = o.tree_knn(16)
+        t0 = time.perf_counter()
+        o.fof_nn(0, params, pn, MINNUM)
+        dt = time.perf_counter() - t0
+        o.close()
+        resf["cpu"] = {"kind": "port", "cores": 1, "particles_per_s": N_FOF / dt,
+                       "sample": "the full FOFNNCriterion over the same lists, serial as shipped"}
+    out["smoothvel_veldisp_clustered_2pow20_k32"] = res
+    out["fofnn_fof3d_clustered_2pow20_k16"] = resf
+    del dpos, dmass, dvel, rho
+    torch.cuda.empty_cache()
     return out
 
 

@@ -12,24 +12,40 @@
 //   dL/dx_i += [sum_j c_ij dw/dh] (1/2) (x_i - x_K)/r_iK   (and the opposite on x_K).
 // The backward kernel recomputes every weight from the saved neighbour lists (4 B per
 // neighbour) instead of storing weights; one thread per particle, FP64 atomics for the
-// contributions that land on other particles.
+// contributions that land on other particles. The quotients that do not depend on the
+// pair (g_i = w_i / rho_i, the table slopes (T[c+1]-T[c])/delta, -0.5 h^-3 / h) are
+// formed once, so a pair costs two FP64 divisions and one square root.
+#include <algorithm>
+
 #include "nbk_build.h"
 
 namespace nbk {
 
 namespace {
 
+// g_i = w_i / rho_i in place of w_i (tree order), and the slope of every table cell
+// (0 for the last entry, whose cell the forward pass never interpolates).
+__global__ void k_adjoint_prep(double* wg, const double* __restrict__ rho, int64_t n,
+                               const double* __restrict__ T, int kr, double* slope) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) wg[i] = wg[i] / rho[i];
+  if (i < kr) {
+    double delta = 2.0 / (double)(kr - 1);
+    slope[i] = i < kr - 1 ? (T[i + 1] - T[i]) / delta : 0.0;
+  }
+}
+
 __global__ void __launch_bounds__(128) k_adjoint(TreeView tv, int K, const int* __restrict__ nn,
-                                                 const double* __restrict__ wt,
-                                                 const double* __restrict__ rho,
-                                                 const double* __restrict__ T, int kr,
+                                                 const double* __restrict__ g,
+                                                 const double* __restrict__ T,
+                                                 const double* __restrict__ slope, int kr,
                                                  double* gpos, double* gmass) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= tv.n) return;
   int ti = tv.pstart + i;
   const int* row = nn + (size_t)i * K;
   P4 xi = tv.pos[ti];
-  double gi = wt[ti] / rho[ti];
+  double gi = g[ti];
   // farthest neighbour: the one that set h_i in the forward pass
   double best = -1.0;
   int kf = row[0];
@@ -45,6 +61,7 @@ __global__ void __launch_bounds__(128) k_adjoint(TreeView tv, int K, const int* 
   double hh = 0.5 * rk;
   double norm = 1.0 / pow(hh, 3.0);
   double delta = 2.0 / (double)(kr - 1);
+  double nh = -0.5 * norm / hh;  // dw/dh = nh (3 T + q T'), dw/dr = -nh T'
   double A = 0.0, gmi = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
   for (int s = 0; s < K; s++) {
     int j = row[s];
@@ -54,14 +71,14 @@ __global__ void __launch_bounds__(128) k_adjoint(TreeView tv, int K, const int* 
     double q = rij / hh;
     int c = (int)(q * 0.5 * (double)(kr - 1));
     double Tq = wsm(q, c, kr, delta, T);
-    double Tp = (c < kr - 1) ? (T[c + 1] - T[c]) / delta : 0.0;
+    double Tp = slope[c < kr - 1 ? c : kr - 1];
     double w = 0.5 * Tq * norm;
-    double gj = wt[j] / rho[j];
+    double gj = g[j];
     double cij = gi * xj.m + gj * xi.m;
     atomicAdd(&gmass[j], gi * w);
     gmi += gj * w;
-    double dwdr = 0.5 * norm * Tp / hh;
-    double dwdh = -0.5 * norm / hh * (3.0 * Tq + q * Tp);
+    double dwdr = -nh * Tp;
+    double dwdh = nh * (3.0 * Tq + q * Tp);
     A += cij * dwdh;
     double coef = cij * dwdr / rij;
     gx += coef * dx;
@@ -85,14 +102,19 @@ __global__ void __launch_bounds__(128) k_adjoint(TreeView tv, int K, const int* 
 
 }  // namespace
 
-int run_density_adjoint(const TreeView& tv, int k, const int* d_nn, const double* d_w_tree,
+int run_density_adjoint(const TreeView& tv, int k, const int* d_nn, double* d_w_tree,
                         const double* d_rho_tree, const double* kernel, int kernres,
-                        double* d_gpos_tree, double* d_gmass_tree, cudaStream_t st) {
+                        double* d_slope, double* d_gpos_tree, double* d_gmass_tree,
+                        cudaStream_t st) {
   if (tv.n == 0) return NBK_OK;
   NBK_CUDA_TRY(cudaMemsetAsync(d_gpos_tree, 0, sizeof(double) * 3 * tv.n, st));
   NBK_CUDA_TRY(cudaMemsetAsync(d_gmass_tree, 0, sizeof(double) * tv.n, st));
   Phase ph("adjoint_backward", st);
-  k_adjoint<<<(tv.n + 127) / 128, 128, 0, st>>>(tv, k, d_nn, d_w_tree, d_rho_tree, kernel, kernres,
+  int64_t m = std::max<int64_t>(tv.n, kernres);
+  k_adjoint_prep<<<(unsigned)((m + 255) / 256), 256, 0, st>>>(d_w_tree, d_rho_tree, tv.n, kernel,
+                                                               kernres, d_slope);
+  note_launch();
+  k_adjoint<<<(tv.n + 127) / 128, 128, 0, st>>>(tv, k, d_nn, d_w_tree, kernel, d_slope, kernres,
                                                 d_gpos_tree, d_gmass_tree);
   note_launch();
   NBK_CUDA_TRY(cudaGetLastError());

@@ -1615,8 +1615,9 @@ int nbk_density_adjoint(nbk_tree* t, int k, const double* w, double* rho, double
   NBK_TRY(S.out(grad_pos, 3 * t->n, &dgp));
   NBK_TRY(S.out(grad_mass, t->n, &dgm));
   int* nn;
-  double *trho, *tw, *tgp, *tgm;
+  double *trho, *tw, *tgp, *tgm, *tslope;
   NBK_TRY(S.alloc.get((void**)&nn, sizeof(int) * t->n * k));
+  NBK_TRY(S.alloc.get((void**)&tslope, sizeof(double) * t->kernres));
   NBK_TRY(S.alloc.get((void**)&trho, sizeof(double) * t->n));
   NBK_TRY(S.alloc.get((void**)&tw, sizeof(double) * t->n));
   NBK_TRY(S.alloc.get((void**)&tgp, sizeof(double) * 3 * t->n));
@@ -1636,7 +1637,8 @@ int nbk_density_adjoint(nbk_tree* t, int k, const double* w, double* rho, double
   NBK_TRY(launch_knn(a, kEpiDensSave, t->st));
   k_gather_d<<<(unsigned)((t->n + 255) / 256), 256, 0, t->st>>>(dw, t->arr.perm, tw, t->n);
   note_launch();
-  NBK_TRY(run_density_adjoint(a.tv, k, nn, tw, trho, t->d_kernel, t->kernres, tgp, tgm, t->st));
+  NBK_TRY(run_density_adjoint(a.tv, k, nn, tw, trho, t->d_kernel, t->kernres, tslope, tgp, tgm,
+                              t->st));
   NBK_TRY(scatter_to_input_order(trho, t->arr.perm, drho, t->n, 1, t->st));
   NBK_TRY(scatter_to_input_order(tgp, t->arr.perm, dgp, t->n, 3, t->st));
   NBK_TRY(scatter_to_input_order(tgm, t->arr.perm, dgm, t->n, 1, t->st));

@@ -184,9 +184,11 @@ int run_ball(const TreeView& tv, int qmode, const int* qidx, const double* qx, i
 int run_ball_mark(const TreeView& tv, int target, double fdist2, int imark, int* d_mark,
                   double* d_dist2, const int* d_perm, int target_search, cudaStream_t st);
 
-int run_density_adjoint(const TreeView& tv, int k, const int* d_nn, const double* d_w_tree,
+// d_w_tree is overwritten with w / rho; d_slope holds kernres doubles of scratch.
+int run_density_adjoint(const TreeView& tv, int k, const int* d_nn, double* d_w_tree,
                         const double* d_rho_tree, const double* kernel, int kernres,
-                        double* d_gpos_tree, double* d_gmass_tree, cudaStream_t st);
+                        double* d_slope, double* d_gpos_tree, double* d_gmass_tree,
+                        cudaStream_t st);
 
 void kernel_table(int kerntype, int kernres, int nd, std::vector<double>& T, double& norm);
 void kernel_device_image(const std::vector<double>& T, std::vector<double>& img);
