@@ -234,6 +234,21 @@ int nbk_density_veldensity(nbk_tree* tree, int k, int nsmooth, double* rho, doub
 int nbk_veldensity_particles(nbk_tree* tree, const int32_t* targets, int64_t ntargets,
                              int nsmooth, int nsearch, double* out);
 
+/* SPH density at arbitrary coordinates. Replaces KDTree::CalcDensityPosition
+   (KDCalcSmoothQuantities.cxx:1092-1148) on physical trees: the coordinate search
+   (FindNearestPos(x): nothing excluded, never periodic), then the gather of
+   CalcDensityParticle. x: nq rows of 3. NBK_ERR_UNSUPPORTED on velocity trees (the
+   reference scales by metric factors it never sets there, :1125-1130) and phase-space
+   trees; NBK_ERR_TOO_FEW when k exceeds the particle count. */
+int nbk_density_points(nbk_tree* tree, const double* x, int64_t nq, int k, double* out);
+
+/* Velocity density at arbitrary coordinates with given velocities. Replaces
+   KDTree::CalcVelDensityPosition (KDCalcSmoothQuantities.cxx:1149-1207), physical trees:
+   FindNearestPos(x) with nsearch, then as nbk_veldensity_particles with |v - v_j|.
+   x, v: nq rows of 3. */
+int nbk_veldensity_points(nbk_tree* tree, const double* x, const double* v, int64_t nq,
+                          int nsmooth, int nsearch, double* out);
+
 /*
  * SPH smoothing over the Nsmooth nearest neighbours (KDCalcSmoothQuantities.cxx). In all
  * of them rho holds the particles' densities in input order (the reference's

@@ -240,6 +240,27 @@ class KDTree {
     nbkdt::check(nbk_veldensity_particles(tree_, &t, 1, Nsmooth, Nsearch, &out));
     return out;
   }
+  // CalcDensityPosition / CalcVelDensityPosition (KDTree.h:432-438), physical trees; the
+  // velocity argument of CalcDensityPosition only matters for phase-space trees.
+  Double_t CalcDensityPosition(Double_t* x, Int_t Nsmooth = 64, Double_t* v = NULL) {
+    (void)v;
+    double out = 0;
+    nbkdt::check(nbk_density_points(tree_, x, 1, Nsmooth, &out));
+    return out;
+  }
+  Double_t CalcDensityPosition(Coordinate x, Int_t Nsmooth = 64, Coordinate v = Coordinate(0.)) {
+    return CalcDensityPosition(x.GetCoord(), Nsmooth, v.GetCoord());
+  }
+  Double_t CalcVelDensityPosition(Double_t* x, Double_t* v, Int_t Nsmooth = 64,
+                                  Int_t Nsearch = 64) {
+    double out = 0;
+    nbkdt::check(nbk_veldensity_points(tree_, x, v, 1, Nsmooth, Nsearch, &out));
+    return out;
+  }
+  Double_t CalcVelDensityPosition(Coordinate x, Coordinate v, Int_t Nsmooth = 64,
+                                  Int_t Nsearch = 64) {
+    return CalcVelDensityPosition(x.GetCoord(), v.GetCoord(), Nsmooth, Nsearch);
+  }
 
   // ---- SPH smoothing (KDTree.h:413-464, KDCalcSmoothQuantities.cxx). densityset == 1 uses
   // the densities stored in the particles (by CalcDensity), as the reference does; any

@@ -48,6 +48,8 @@ SIGNATURES = {
     "nbk_veldensity": (c_int, [c_vp, c_int, c_int, c_vp]),
     "nbk_density_veldensity": (c_int, [c_vp, c_int, c_int, c_vp, c_vp]),
     "nbk_veldensity_particles": (c_int, [c_vp, c_vp, c_i64, c_int, c_int, c_vp]),
+    "nbk_density_points": (c_int, [c_vp, c_vp, c_i64, c_int, c_vp]),
+    "nbk_veldensity_points": (c_int, [c_vp, c_vp, c_vp, c_i64, c_int, c_int, c_vp]),
     "nbk_smooth_vel": (c_int, [c_vp, c_int, c_vp, c_vp]),
     "nbk_smooth_vel_disp": (c_int, [c_vp, c_int, c_vp, c_vp, c_vp]),
     "nbk_smooth_vel_skew": (c_int, [c_vp, c_int, c_vp, c_vp, c_vp, c_vp]),

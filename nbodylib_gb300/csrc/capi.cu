@@ -1329,6 +1329,71 @@ int nbk_veldensity_particles(nbk_tree* t, const int32_t* targets, int64_t nt, in
   API_END
 }
 
+// CalcDensityPosition / CalcVelDensityPosition (KDCalcSmoothQuantities.cxx:1092-1207):
+// coordinate queries on a physical tree, nothing excluded, never periodic; the density is
+// the gather of CalcDensityParticle, the velocity density uses the given velocities.
+static int positions_common(nbk_tree* t, const double* x, const double* v, int64_t nq, int k,
+                            int nsmooth, double* out, int epi) {
+  if (!x || !out || nq < 0 || k < 1 || (epi == kEpiVelPart && !v)) {
+    set_error("position density: invalid argument");
+    return NBK_ERR_INVALID;
+  }
+  if (t->treetype != NBK_TPHYS) {
+    // velocity trees: the reference scales the normalisation by metric factors it never
+    // sets (KDCalcSmoothQuantities.cxx:1125-1130); phase-space trees: not supported here
+    set_error("position density runs on physical trees only");
+    return NBK_ERR_UNSUPPORTED;
+  }
+  if (epi == kEpiVelPart && !t->has_vel) {
+    set_error("velocity density needs velocities at nbk_create");
+    return NBK_ERR_INVALID;
+  }
+  if (k > t->n) {
+    set_error("position density: k exceeds the number of particles");
+    return NBK_ERR_TOO_FEW;
+  }
+  if (nq == 0) return NBK_OK;
+  Stage S(t);
+  const double *dx, *dv = nullptr;
+  double* dout;
+  NBK_TRY(S.in(x, (size_t)nq * 3, &dx));
+  if (epi == kEpiVelPart) NBK_TRY(S.in(v, (size_t)nq * 3, &dv));
+  NBK_TRY(S.out(out, nq, &dout));
+  NBK_TRY(clear_err(t));
+  KnnArgs a = base_args(t);
+  a.tv.periodic = 0;
+  a.kheap = k;
+  a.kout = k;
+  a.exclude_self = 0;
+  a.qmode = 1;
+  a.qx = dx;
+  a.qv = dv;
+  a.nq = (int)nq;
+  a.nsmooth = nsmooth;
+  a.rho = dout;
+  a.vden = dout;
+  NBK_TRY(launch_knn(a, epi, t->st));
+  NBK_TRY(S.finish());
+  if (!t->dev()) NBK_TRY(check_err(t, "position density"));
+  return NBK_OK;
+}
+
+int nbk_density_points(nbk_tree* t, const double* x, int64_t nq, int k, double* out) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  return positions_common(t, x, nullptr, nq, k, k, out, kEpiDensPart);
+  API_END
+}
+
+int nbk_veldensity_points(nbk_tree* t, const double* x, const double* v, int64_t nq,
+                          int nsmooth, int nsearch, double* out) {
+  API_BEGIN
+  NBK_TRY(check_tree(t));
+  if (nsmooth > nsearch) nsmooth = nsearch;
+  return positions_common(t, x, v, nq, nsearch, nsmooth, out, kEpiVelPart);
+  API_END
+}
+
 static int ball_common(nbk_tree* t, int qmode, const int32_t* targets, const double* x,
                        int64_t nq, double fdist2, int64_t* offsets, int32_t* out,
                        int64_t out_capacity, int64_t* total) {

@@ -1,7 +1,8 @@
 // k-nearest-neighbour queries and the SPH quantities built on them: the per-particle
 // loops of CalcDensity, CalcVelDensity, CalcDensityParticle and CalcVelDensityParticle
-// (KDCalcSmoothQuantities.cxx:203-389, 768-920) as epilogues of the warp search of
-// knn_core.cuh.
+// (KDCalcSmoothQuantities.cxx:203-389, 768-920) and the coordinate forms
+// CalcDensityPosition / CalcVelDensityPosition (:1092-1207) as epilogues of the warp
+// search of knn_core.cuh.
 #include <algorithm>
 
 #include "knn_core.cuh"
@@ -45,7 +46,8 @@ __device__ void run_warp(const KnnArgs& a, const TreeView& tv, WarpSmem<KMAX>& w
       return;
     }
   const double* T = a.kernel;
-  P4 me = tv.pos[self];
+  P4 me{};  // the query particle (a coordinate query has none: self = -1)
+  if (self >= 0) me = tv.pos[self];
   if (EPI == kEpiDensity || EPI == kEpiDensVel || EPI == kEpiDensPart || EPI == kEpiDensSave) {
     // KDCalcSmoothQuantities.cxx:260-286
     // One reciprocal per query replaces the per-neighbour divisions (r/h and the table
@@ -78,7 +80,9 @@ __device__ void run_warp(const KnnArgs& a, const TreeView& tv, WarpSmem<KMAX>& w
   if (EPI == kEpiDensVel || EPI == kEpiVel || EPI == kEpiVelPart) {
     // KDCalcSmoothQuantities.cxx:354-383: |dv| of the Nsearch neighbours, keep the
     // Nsmooth smallest, h = 0.5 max, sum Wsm(|dv|/h) h^-3 with unit weights.
-    V4 vi = tv.vel[self];
+    V4 vi = self >= 0 ? tv.vel[self]
+                      : make_v4(a.qv[3 * (size_t)qi], a.qv[3 * (size_t)qi + 1],
+                                a.qv[3 * (size_t)qi + 2], 0.0);
     for (int s = 0; s < K; s++) {
       V4 vj = tv.vel[w.hi[s][lane]];
       w.hd[s][lane] = sqrt_newton(dist2_exact(vi.x, vi.y, vi.z, vj.x, vj.y, vj.z));

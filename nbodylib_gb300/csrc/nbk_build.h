@@ -99,6 +99,7 @@ struct KnnArgs {
   double* rho;        // tree order (scatter) or query order (particle variants)
   double* vden;
   int* err;
+  const double* qv;   // query velocities of coordinate queries (CalcVelDensityPosition)
 };
 int launch_knn(const KnnArgs& a, int epi, cudaStream_t st);
 

@@ -230,6 +230,21 @@ class KDTree:
                                                        nsmooth, nsearch, _ptr(out)))
         return out
 
+    def CalcDensityPosition(self, x, k=64):
+        """CalcDensityPosition at each row of x (n, 3), physical trees."""
+        x = self._pts(x)
+        out = self._empty(x.shape[0], np.float64)
+        _capi.check(self._lib.nbk_density_points(self._h, _ptr(x), x.shape[0], k, _ptr(out)))
+        return out
+
+    def CalcVelDensityPosition(self, x, v, nsmooth=64, nsearch=64):
+        """CalcVelDensityPosition at each row of x with the velocity in the same row of v."""
+        x, v = self._pts(x), self._pts(v)
+        out = self._empty(x.shape[0], np.float64)
+        _capi.check(self._lib.nbk_veldensity_points(self._h, _ptr(x), _ptr(v), x.shape[0],
+                                                    nsmooth, nsearch, _ptr(out)))
+        return out
+
     # ---- SPH smoothing (KDCalcSmoothQuantities.cxx:393-766, 922-1091, 1209-1306,
     # 1539-1700). rho: densities in input order (the reference's densityset = 1, i.e. what
     # CalcDensity returned), or None to compute CalcDensity(Nsmooth) first. Targets are

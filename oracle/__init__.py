@@ -65,6 +65,9 @@ def _lib(backend: str) -> ctypes.CDLL:
         "veldensity": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, _c_dbl_p]),
         "density_particle": (ctypes.c_double, [vp, ctypes.c_int, ctypes.c_int]),
         "veldensity_particle": (ctypes.c_double, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+        "density_position": (ctypes.c_double, [vp, _c_dbl_p, ctypes.c_int]),
+        "veldensity_position": (ctypes.c_double, [vp, _c_dbl_p, _c_dbl_p, ctypes.c_int,
+                                                  ctypes.c_int]),
         "fof": (ctypes.c_int, [vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, _c_int_p, _c_int_p]),
         "fof_criterion": (ctypes.c_int, [vp, ctypes.c_int, _c_dbl_p, ctypes.c_int, ctypes.c_int,
                                          _c_int_p, _c_int_p]),
@@ -282,6 +285,15 @@ class OracleTree:
 
     def veldensity_particle(self, pid, nsmooth, nsearch):
         return self._f("veldensity_particle")(self._h, int(pid), nsmooth, nsearch)
+
+    def density_position(self, x, k):
+        """CalcDensityPosition(x, k) (physical or velocity tree; x in the tree's space)."""
+        return self._f("density_position")(self._h, _dp(self._arr(x, (3,))), k)
+
+    def veldensity_position(self, x, v, nsmooth, nsearch):
+        """CalcVelDensityPosition(x, v, nsmooth, nsearch) (physical tree)."""
+        return self._f("veldensity_position")(self._h, _dp(self._arr(x, (3,))),
+                                              _dp(self._arr(v, (3,))), nsmooth, nsearch)
 
     def fof(self, ll, minnum=8, order=0):
         g = np.empty(self.n, np.int32)

@@ -937,6 +937,92 @@ double pt_veldensity_particle(PTree* t, int id, int nsmooth, int nsearch) {
     return status ? NAN : v;
 }
 
+/* KDTree::CalcDensityPosition (KDCalcSmoothQuantities.cxx:1092-1148) for physical trees:
+   the coordinate search (FindNearestPos(x): nothing excluded, never periodic), then the
+   gather of CalcDensityParticle with the particle masses. NAN when fewer than k particles
+   exist, and for other tree types: for velocity trees the reference multiplies the
+   normalisation by metric factors it never sets (:1125-1130); phase-space trees are not
+   restated. */
+double pt_density_position(PTree* t, const double* x, int k) {
+    if (t->treetype != TPHYS) return NAN;
+    PQ pq;
+    pq_init(&pq, k);
+    for (int j = 0; j < k; j++) pq_push(&pq, -1, MAXVALUE);
+    double off[6] = {0, 0, 0, 0, 0, 0};
+    double xq[6] = {x[0], x[1], x[2], 0, 0, 0};
+    knn_coord(t, 0, 0.0, &pq, off, xq);
+    double delta = 2.0 / (double)(t->kernres - 1);
+    double hi = 0.5 * sqrt(pq_top(&pq));
+    double norm = 1.0 / pow(hi, (double)(t->nd * 1.));
+    double den = 0.;
+    for (int j = 0; j < k; j++) {
+        if (pq_topq(&pq) == -1) {
+            den = NAN;
+            break;
+        }
+        double rij = sqrt(pq_top(&pq));
+        double wij =
+            wsm(rij / hi, (int)(rij / hi * 0.5 * (t->kernres - 1)), t->kernres, delta, t->kernel) *
+            norm;
+        den += wij * t->p[pq_topq(&pq)].mass;
+        pq_pop(&pq);
+    }
+    pq_free(&pq);
+    return den;
+}
+
+/* KDTree::CalcVelDensityPosition (KDCalcSmoothQuantities.cxx:1149-1207), physical tree:
+   FindNearestPos(x) with nsearch, |v - v_j| for the given velocity v, the nsmooth smallest
+   kept, h = 0.5 max, unit weights. NAN as above or for a non-physical tree. */
+double pt_veldensity_position(PTree* t, const double* x, const double* v, int nsmooth,
+                              int nsearch) {
+    if (t->treetype != TPHYS) return NAN;
+    if (nsmooth > nsearch) nsmooth = nsearch;
+    PQ pq, pq2;
+    pq_init(&pq, nsearch);
+    pq_init(&pq2, nsmooth);
+    for (int j = 0; j < nsearch; j++) pq_push(&pq, -1, MAXVALUE);
+    double off[6] = {0, 0, 0, 0, 0, 0};
+    double xq[6] = {x[0], x[1], x[2], 0, 0, 0};
+    knn_coord(t, 0, 0.0, &pq, off, xq);
+    int* nnids = (int*)malloc(sizeof(int) * (size_t)nsearch);
+    double* vdist = (double*)malloc(sizeof(double) * (size_t)nsearch);
+    double vden = 0.;
+    int bad = 0;
+    for (int j = 0; j < nsearch; j++) {
+        if (pq_topq(&pq) == -1) {
+            bad = 1;
+            break;
+        }
+        nnids[j] = pq_topq(&pq);
+        vdist[j] = sqrt(dist2_n(v, t->p[nnids[j]].vel, 3));
+        pq_pop(&pq);
+    }
+    if (!bad) {
+        for (int j = 0; j < nsmooth; j++) pq_push(&pq2, -1, MAXVALUE);
+        for (int j = 0; j < nsearch; j++)
+            if (vdist[j] < pq_top(&pq2)) {
+                pq_pop(&pq2);
+                pq_push(&pq2, nnids[j], vdist[j]);
+            }
+        double delta = 2.0 / (double)(t->kernres - 1);
+        double hi = 0.5 * pq_top(&pq2);
+        double norm = 1.0 / pow(hi, (double)(t->nd * 1.));
+        for (int j = 0; j < nsmooth; j++) {
+            double rij = pq_top(&pq2);
+            vden += wsm(rij / hi, (int)(rij / hi * 0.5 * (t->kernres - 1)), t->kernres, delta,
+                        t->kernel) *
+                    norm;
+            pq_pop(&pq2);
+        }
+    }
+    free(nnids);
+    free(vdist);
+    pq_free(&pq);
+    pq_free(&pq2);
+    return bad ? NAN : vden;
+}
+
 /* ---------------------------------------------------------------- ball search */
 /* Node::__checkboundaries (KDNode.h:280-291) as FlagNodeForSearchBallPos /
    FlagNodeForFOFSearchBall use it for non-adaptive trees (farthest2 = -1):

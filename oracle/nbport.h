@@ -47,6 +47,9 @@ int pt_density(PTree* t, int k, double* rho, int* nn_ids);
 int pt_veldensity(PTree* t, int nsmooth, int nsearch, double* out);
 double pt_density_particle(PTree* t, int id, int k);
 double pt_veldensity_particle(PTree* t, int id, int nsmooth, int nsearch);
+double pt_density_position(PTree* t, const double* x, int k);
+double pt_veldensity_position(PTree* t, const double* x, const double* v, int nsmooth,
+                              int nsearch);
 int pt_fof(PTree* t, double ll, int minnum, int order, int* group, int* ngroup);
 /* cmp: 0 FOF3d, 1 FOFVel, 2 FOF6d (src/KDTree/FOFFunc.h:30-55). params as the reference. */
 int pt_fof_criterion(PTree* t, int cmp, const double* params, int minnum, int order, int* group,

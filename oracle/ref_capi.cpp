@@ -204,6 +204,19 @@ double ref_veldensity_particle(void* h, int id, int nsmooth, int nsearch) {
     return r->tree->CalcVelDensityParticle(r->tree_of_id[id], nsmooth, nsearch);
 }
 
+double ref_density_position(void* h, const double* x, int k) {
+    RefTree* r = (RefTree*)h;
+    Double_t xq[3] = {x[0], x[1], x[2]};
+    return r->tree->CalcDensityPosition(xq, k, (Double_t*)NULL);
+}
+
+double ref_veldensity_position(void* h, const double* x, const double* v, int nsmooth,
+                               int nsearch) {
+    RefTree* r = (RefTree*)h;
+    Double_t xq[3] = {x[0], x[1], x[2]}, vq[3] = {v[0], v[1], v[2]};
+    return r->tree->CalcVelDensityPosition(xq, vq, nsmooth, nsearch);
+}
+
 int ref_fof(void* h, double ll, int minnum, int order, int* group, int* ngroup) {
     RefTree* r = (RefTree*)h;
     Int_t ng = 0;

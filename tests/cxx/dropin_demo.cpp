@@ -13,7 +13,9 @@
 //            int32 ngroup_nn, n x int32 FOFNNCriterion(FOF3d, 16 lists) groups (by ID),
 //            n x double density after DensitySmooth(S, 16, 32) (input order),
 //            phase-space tree (Aniso 0): n x 16 int32 FindNearest IDs, n x 16 double d2,
-//            n x double CalcDensity(16), int32 ngroup, n x int32 FOFCriterion(FOF6d)
+//            n x double CalcDensity(16), int32 ngroup, n x int32 FOFCriterion(FOF6d),
+//            100 x double CalcDensityPosition(x + 0.01, 32) and 100 x double
+//            CalcVelDensityPosition(x + 0.01, v, 16, 32) of IDs 0..99
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -47,6 +49,7 @@ int main(int argc, char** argv) {
   std::vector<int> group(n), nnid((size_t)n * 16), ballid, group_nn(n);
   int ngroup_nn = 0;
   std::vector<double> rho(n), d2((size_t)n * 16), rho_after(n), smvel(3 * (size_t)n);
+  std::vector<double> posden(100), posvden(100);
   int numnodes, numleaves, ngroup = 0;
   {
     KDTree tree(parts.data(), n, 16, KDTree::TPHYS, KDTree::KSPH, 1000, 0, 0, 0,
@@ -89,6 +92,18 @@ int main(int argc, char** argv) {
     while (parts[t0].GetID() != 0) t0++;
     std::vector<Int_t> tagged = tree.SearchBallPosTagged(t0, 4 * ll * ll);
     for (Int_t t : tagged) ballid.push_back(parts[t].GetID());
+    // CalcDensityPosition / CalcVelDensityPosition next to the first 100 particles (by ID)
+    for (int t = 0; t < n; t++) {
+      int id = parts[t].GetID();
+      if (id >= 100) continue;
+      Double_t x[3], vq[3];
+      for (int k = 0; k < 3; k++) {
+        x[k] = parts[t].GetPosition(k) + 0.01;
+        vq[k] = parts[t].GetVelocity(k);
+      }
+      posden[id] = tree.CalcDensityPosition(x, 32);
+      posvden[id] = tree.CalcVelDensityPosition(x, vq, 16, 32);
+    }
   }
   // the destructor restored input order
   for (int i = 0; i < n; i++) rho_after[i] = parts[i].GetDensity();
@@ -156,6 +171,8 @@ int main(int argc, char** argv) {
   fwrite(prho.data(), 8, n, o);
   fwrite(&pngroup, 4, 1, o);
   fwrite(pgroup.data(), 4, n, o);
+  fwrite(posden.data(), 8, 100, o);
+  fwrite(posvden.data(), 8, 100, o);
   fclose(o);
   printf("dropin ok: n=%d nodes=%d groups=%d\n", n, numnodes, ngroup);
   return 0;

@@ -167,6 +167,26 @@ def smoothing():
                 phys_nsearch=32, veldensity_phys=vphys, veldensity_phys_id=vphys_id, **one)
 
 
+def position_density():
+    """CalcDensityPosition and CalcVelDensityPosition (KDCalcSmoothQuantities.cxx:
+    1092-1207) on a periodic physical tree of clustered particles (both forms ignore the
+    period): at particle positions, random points in the box and points outside it, with
+    random velocities."""
+    pos, mass, vel = syn.clustered_box(3000, 40.0, seed=31, velocities=True)
+    per = [40.0] * 3
+    t = ref_tree(pos, vel, mass, 16, 0, per)
+    rng = np.random.default_rng(32)
+    pts = np.concatenate([pos[:10], rng.random((30, 3)) * 40.0,
+                          rng.random((5, 3)) * 10.0 + 45.0])
+    pv = rng.normal(size=(len(pts), 3))
+    return dict(pos=pos, vel=vel, mass=mass, period=np.asarray(per), b=16, points=pts,
+                point_vel=pv,
+                dens_k32=np.array([t.density_position(x, 32) for x in pts]),
+                dens_k8=np.array([t.density_position(x, 8) for x in pts]),
+                veldens_16_32=np.array([t.veldensity_position(x, v, 16, 32)
+                                        for x, v in zip(pts, pv)]))
+
+
 def phase_space():
     """Phase-space (TPHS) and velocity (TVEL) trees on clustered particles with velocities:
     the tree, FindNearest(tt) and FindNearest(x) with the plain phase distance
@@ -223,7 +243,8 @@ def phase_space():
 
 FIXTURES = [("uniform_periodic", uniform_periodic), ("clustered", clustered),
             ("nonperiodic", nonperiodic), ("tiny_periodic", tiny_periodic),
-            ("smoothing", smoothing), ("phase_space", phase_space)]
+            ("smoothing", smoothing), ("phase_space", phase_space),
+            ("position_density", position_density)]
 
 
 def main(names=None):

@@ -99,6 +99,8 @@ def test_dropin_runs_like_the_reference(gpu, port_built, tmp_path, periodic):
     prho = take(np.float64, n)
     pngroup = take(np.int32, 1)[0]
     pgroup = take(np.int32, n)
+    posden = take(np.float64, 100)
+    posvden = take(np.float64, 100)
     per = [box] * 3 if periodic else None
     o = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, per, backend="port")
     assert nodes == o.num_nodes and leaves == o.num_leaves
@@ -134,3 +136,9 @@ def test_dropin_runs_like_the_reference(gpu, port_built, tmp_path, periodic):
     g6, n6 = mk6().fof_criterion(2, [3, 0.25, 0.04, 0, 0, 0, 0.25, 0.04], 8, 0)
     assert pngroup == n6
     assert_same_partition(pgroup, g6, "drop-in phase-space FOFCriterion")
+    # CalcDensityPosition / CalcVelDensityPosition next to the first 100 particles
+    op = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, per, backend="port")
+    assert_density_close(posden, [op.density_position(pos[i] + 0.01, 32) for i in range(100)],
+                         "drop-in CalcDensityPosition")
+    assert_density_close(posvden, [op.veldensity_position(pos[i] + 0.01, vel[i], 16, 32)
+                                   for i in range(100)], "drop-in CalcVelDensityPosition")

@@ -87,3 +87,78 @@ def test_density_full_size_sampled(gpu, port_built):
     assert_density_close(got, want, "sampled particle density")
     rho = t.CalcDensity(32)
     assert np.all(rho > 0) and np.all(np.isfinite(rho))
+
+
+def test_256cubed_sampled(gpu, port_built):
+    """The largest configuration, 256^3 = 16,777,216 clustered particles in L = 250 with
+    velocities, k = 64: FindNearest(x) at 1000 sampled particles' positions,
+    CalcDensityParticle(64) and CalcVelDensityParticle(64, 64) at the same particles
+    against the restatement, and a checksum of the full scatter density: with equal
+    masses, every pair's half-weight is added once at each end, so sum_i CalcDensity_i
+    equals sum_i CalcDensityParticle_i."""
+    from tests.helpers import assert_knn_equal, to_ids
+    n = 1 << 24
+    pos, mass, vel = syn.clustered_box(n, 250.0, seed=3, velocities=True)
+    assert np.all(mass == mass[0])
+    t = KDTree(pos, vel, mass, 16, kerntype=0)
+    o = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, None, backend="port", nthreads=16)
+    ids = np.random.default_rng(11).choice(n, 1000, replace=False)
+    perm = np.asarray(t.GetPerm())
+    inv = np.argsort(perm)
+    x = pos[ids]
+    nn, d2 = t.FindNearestPoints(x, 64)
+    want_nn, want_d2 = o.knn_coord(x, 64)
+    assert_knn_equal(to_ids(np.asarray(nn), perm), d2, want_nn, want_d2, "FindNearest(x) 256^3")
+    got = t.CalcDensityParticle(inv[ids], 64)
+    want = np.array([o.density_particle(int(i), 64) for i in ids])
+    assert_density_close(got, want, "CalcDensityParticle 256^3")
+    got = t.CalcVelDensityParticle(inv[ids], 64, 64)
+    want = np.array([o.veldensity_particle(int(i), 64, 64) for i in ids])
+    assert_density_close(got, want, "CalcVelDensityParticle 256^3")
+    o.close()
+    rho = np.asarray(t.CalcDensity(64))
+    gather = np.asarray(t.CalcDensityParticle(np.arange(n, dtype=np.int32), 64))
+    assert np.all(rho > 0) and np.all(np.isfinite(rho))
+    assert abs(rho.sum() - gather.sum()) <= 1e-10 * gather.sum()
+    t.close()
+
+
+def test_position_density_golden_and_restatement(gpu, port_built):
+    """CalcDensityPosition / CalcVelDensityPosition against the reference's outputs in the
+    fixture (period ignored; points at particles, inside and outside the box), then on
+    2^17 clustered particles at 4000 points against the restatement, host and device
+    buffers; refused on velocity trees and for k above the particle count."""
+    import torch
+    g = golden("position_density")
+    t = KDTree(g["pos"], g["vel"], g["mass"], int(g["b"]), kerntype=0, period=g["period"])
+    pts, pv = g["points"], g["point_vel"]
+    assert_density_close(t.CalcDensityPosition(pts, 32), g["dens_k32"], "position k=32")
+    assert_density_close(t.CalcDensityPosition(pts, 8), g["dens_k8"], "position k=8")
+    assert_density_close(t.CalcVelDensityPosition(pts, pv, 16, 32), g["veldens_16_32"],
+                         "vel position 16/32")
+    with pytest.raises(NbkError):
+        t.CalcDensityPosition(pts, len(g["mass"]) + 1)
+    t.close()
+    from nbodylib_gb300.kdtree import TVEL
+    tv = KDTree(g["pos"], g["vel"], g["mass"], 16, treetype=TVEL, kerntype=0)
+    with pytest.raises(NbkError):
+        tv.CalcDensityPosition(pv, 8)
+    tv.close()
+
+    n = 1 << 17
+    pos, mass, vel = syn.clustered_box(n, 50.0, seed=35, velocities=True)
+    rng = np.random.default_rng(36)
+    pts = np.concatenate([pos[::64], rng.random((2000, 3)) * 50.0])
+    pv = rng.normal(size=(len(pts), 3))
+    P = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, None, backend="port")
+    t = KDTree(pos, vel, mass, 16, kerntype=0)
+    assert_density_close(t.CalcDensityPosition(pts, 40),
+                         [P.density_position(x, 40) for x in pts], "position 2^17")
+    want_v = [P.veldensity_position(x, v, 24, 48) for x, v in zip(pts, pv)]
+    assert_density_close(t.CalcVelDensityPosition(pts, pv, 24, 48), want_v, "vel position 2^17")
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    td = KDTree(dev(pos), dev(vel), dev(mass), 16, kerntype=0, device=True)
+    got = td.CalcVelDensityPosition(dev(pts), dev(pv), 24, 48).cpu().numpy()
+    assert_density_close(got, want_v, "vel position 2^17, device buffers")
+    t.close()
+    td.close()

@@ -225,6 +225,40 @@ def test_port_matches_golden_smoothing(port_built):
                           g["veldensity_phys"])
 
 
+def test_port_matches_golden_position_density(port_built):
+    """CalcDensityPosition / CalcVelDensityPosition: the restatement reproduces the
+    reference's outputs bit for bit (period ignored, points inside and outside the box);
+    velocity and phase-space trees are not restated (NaN)."""
+    g = golden("position_density")
+    P = oracle.OracleTree(g["pos"], g["vel"], g["mass"], int(g["b"]), 0, 0, 1000, g["period"],
+                          backend="port")
+    pts, pv = g["points"], g["point_vel"]
+    assert np.array_equal([P.density_position(x, 32) for x in pts], g["dens_k32"])
+    assert np.array_equal([P.density_position(x, 8) for x in pts], g["dens_k8"])
+    assert np.array_equal([P.veldensity_position(x, v, 16, 32) for x, v in zip(pts, pv)],
+                          g["veldens_16_32"])
+    V = oracle.OracleTree(g["pos"], g["vel"], g["mass"], int(g["b"]), 2, 0, 1000, None,
+                          backend="port")
+    assert np.isnan(V.density_position(pv[0], 8))
+
+
+def test_port_position_density_matches_reference(ref_built):
+    pos, mass, vel = syn.clustered_box(4000, 30.0, seed=33, velocities=True)
+    rng = np.random.default_rng(34)
+    pts = np.concatenate([pos[::200], rng.random((20, 3)) * 30.0])
+    pv = rng.normal(size=(len(pts), 3))
+    for per in (None, [30.0] * 3):
+        P = oracle.OracleTree(pos, vel, mass, 8, 0, 0, 1000, per, backend="port")
+        R = oracle.OracleTree(pos, vel, mass, 8, 0, 0, 1000, per, backend="ref")
+        # k >= 2: with k = 1 at a particle's own position h = 0, and the reference's table
+        # index (int)(0/0) falls outside its table
+        for k in (2, 20, 64):
+            assert np.array_equal([P.density_position(x, k) for x in pts],
+                                  [R.density_position(x, k) for x in pts])
+        assert np.array_equal([P.veldensity_position(x, v, 10, 40) for x, v in zip(pts, pv)],
+                              [R.veldensity_position(x, v, 10, 40) for x, v in zip(pts, pv)])
+
+
 @pytest.mark.parametrize("cmp", [0, 1, 2])
 def test_port_fof_nn_matches_reference(ref_built, cmp):
     """FOFNNCriterion and FOFNNDistCriterion over FindNearest lists: the restatement gives
