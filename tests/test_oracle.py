@@ -242,6 +242,28 @@ def test_port_matches_golden_position_density(port_built):
     assert np.isnan(V.density_position(pv[0], 8))
 
 
+def test_port_noncubic_period_matches_reference(ref_built):
+    """A different period per dimension, particles crowding the faces: FindNearest and
+    FindNearestPos (the reference's image gates) and FOF."""
+    rng = np.random.default_rng(44)
+    per = np.array([100.0, 60.0, 35.0])
+    pos = rng.random((6000, 3)) * per
+    face = rng.integers(0, 3, 2000)
+    pos[np.arange(2000), face] = per[face] * np.where(rng.random(2000) < 0.5, 0.01, 0.99)
+    mass = np.full(6000, 1.0 / 6000)
+    P = oracle.OracleTree(pos, None, mass, 16, 0, 0, 1000, list(per), backend="port")
+    R = oracle.OracleTree(pos, None, mass, 16, 0, 0, 1000, list(per), backend="ref")
+    for m in (0, 1):
+        pn, pd = P.knn(12, m)
+        rn, rd = R.knn(12, m)
+        assert_knn_equal(pn, pd, rn, rd, f"non-cubic method {m}", dropped_nearest=(m == 0))
+    ll = 0.2 * (np.prod(per) / 6000) ** (1.0 / 3.0)
+    gp, npg = P.fof(ll, 5)
+    gr, nr = R.fof(ll, 5)
+    assert npg == nr
+    assert_same_partition(gp, gr, "non-cubic FOF")
+
+
 def test_port_position_density_matches_reference(ref_built):
     pos, mass, vel = syn.clustered_box(4000, 30.0, seed=33, velocities=True)
     rng = np.random.default_rng(34)
