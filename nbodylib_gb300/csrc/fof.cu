@@ -448,12 +448,37 @@ __global__ void __launch_bounds__(128) k_crit_link(FofArgs a) {
   }
 }
 
-constexpr int kCritStack = 128;
+constexpr int kCritStack = 512;  // frontier stack of the phase-space link search (one warp)
+constexpr int kCritBatchLimit = kCritStack - 128;
 struct CritSmem {
   float4 sp[32], sv[32];
   int par[32];
   int stk[kCritStack];
 };
+
+// FP32 lower bound of sum_j w[j] * gap_j^2 between the box [qlo, qhi] around a warp's
+// query points and a node's FP32 box; every operation rounds down.
+__device__ __forceinline__ float boxbox_lb6f(const float qlo[6], const float qhi[6],
+                                             const float w[6], const NodeF6& b) {
+  float s = 0.f;
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    float g = fmaxf(0.f, fmaxf(__fsub_rd(b.lo[j], qhi[j]), __fsub_rd(qlo[j], b.hi[j])));
+    s = __fadd_rd(s, __fmul_rd(__fmul_rd(w[j], g), g));
+  }
+  return s;
+}
+
+// FOF6d weights 1/params[6] (positions) and 1/params[7] (velocities) rounded down / up.
+__device__ __forceinline__ void fof6d_weights(const double* p, float w_lo[6], float w_hi[6]) {
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    w_lo[j] = __double2float_rd(__ddiv_rd(1.0, p[6]));
+    w_hi[j] = __double2float_ru(__ddiv_ru(1.0, p[6]));
+    w_lo[3 + j] = __double2float_rd(__ddiv_rd(1.0, p[7]));
+    w_hi[3 + j] = __double2float_ru(__ddiv_ru(1.0, p[7]));
+  }
+}
 
 // FOFCriterion with FOF6d inside its search region on a physical tree: the accepted
 // pairs are those with sum dx^2 / params[6] + sum dv^2 / params[7] < 1, a unit ball of a
@@ -477,13 +502,7 @@ __global__ void __launch_bounds__(32 * kWpb) k_crit6_warp(FofArgs a) {
   const V4 mv = tv.vel[self];
   const double x0[3] = {me.x, me.y, me.z};
   float w_lo[6], w_hi[6];
-#pragma unroll
-  for (int j = 0; j < 3; j++) {
-    w_lo[j] = __double2float_rd(__ddiv_rd(1.0, a.params[6]));
-    w_hi[j] = __double2float_ru(__ddiv_ru(1.0, a.params[6]));
-    w_lo[3 + j] = __double2float_rd(__ddiv_rd(1.0, a.params[7]));
-    w_hi[3 + j] = __double2float_ru(__ddiv_ru(1.0, a.params[7]));
-  }
+  fof6d_weights(a.params, w_lo, w_hi);
   const float thr_hi = 1.0f + 1.0f / 1048576.0f, thr_lo = 1.0f - 1.0f / 1048576.0f;
   const NodeS* N = tv.nodes6 + tv.nbase;
   const NodeF6* F = tv.nodef6 + tv.nbase;
@@ -505,65 +524,111 @@ __global__ void __launch_bounds__(32 * kWpb) k_crit6_warp(FofArgs a) {
       q32[k] = __double2float_rn(xq[k]);
       e32[k] = fmaxf(tv.eps6[k], __fmul_ru(__double2float_ru(fabs(xq[k])), 1.2e-7f));
     }
+    // box around the active lanes' query intervals
+    float qlo[6], qhi[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      float lo = active ? __fsub_rd(q32[k], e32[k]) : FLT_MAX;
+      float hi = active ? __fadd_ru(q32[k], e32[k]) : -FLT_MAX;
+      for (int o = 16; o > 0; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(FULL, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(FULL, hi, o));
+      }
+      qlo[k] = lo;
+      qhi[k] = hi;
+    }
     if (lane == 0) w.stk[0] = 0;
     int sp = 1;
     __syncwarp();
-    while (sp > 0) {
-      const int h = w.stk[sp - 1];
-      sp--;
-      __syncwarp();
-      const NodeS nd = N[h];
-      // direct pass: nodes wholly before the warp's first particle hold only pairs tested
-      // from their lower index
-      const bool need = active && box_lb6f(q32, w_lo, e32, F[h]) < thr_hi &&
-                        (pass != 0 || nd.start + nd.count - 1 > first);
-      if (!__any_sync(FULL, need)) continue;
-      if (nd.split_dim >= 0) {
-        if (sp + 2 > kCritStack) {
-          if (lane == 0) atomicExch(a.err, kErrCapacity);
-          return;
-        }
-        if (lane == 0) {
-          w.stk[sp] = 2 * h + 2;
-          w.stk[sp + 1] = 2 * h + 1;
-        }
-        sp += 2;
-        __syncwarp();
-        continue;
+    // frontier-parallel: each step pops up to 32 nodes, lane i loads node i and drops it
+    // when the warp's query box cannot reach it, so the dependent node loads overlap; the
+    // surviving nodes are then tested against every lane's own query
+    for (int guard = 0; sp > 0 && guard < (1 << 26); guard++) {
+      // above kCritBatchLimit entries pop one node at a time: a depth-first descent from
+      // there adds at most the tree depth, so the stack never exceeds kCritStack
+      const int m = sp <= kCritBatchLimit ? min(32, sp) : 1;
+      int h = 0;
+      NodeS nd{};
+      NodeF6 f{};
+      bool keep = false;
+      if (lane < m) {
+        h = w.stk[sp - 1 - lane];
+        nd = N[h];
+        f = F[h];
+        // direct pass: nodes wholly before the warp's first particle hold only pairs
+        // tested from their lower index
+        keep = boxbox_lb6f(qlo, qhi, w_lo, f) < thr_hi &&
+               (pass != 0 || nd.start + nd.count - 1 > first);
       }
-      for (int c0 = 0; c0 < nd.count; c0 += 32) {
-        const int mm = min(32, nd.count - c0);
-        if (lane < mm) {
-          const int i = nd.start + c0 + lane;
-          w.sp[lane] = tv.posf[i];
-          w.sv[lane] = tv.velf[i];
-          w.par[lane] = ld_parent(a.parent, i);
+      __syncwarp();
+      sp -= m;
+      unsigned todo = __ballot_sync(FULL, keep);
+      unsigned expand = 0;
+      while (todo) {
+        const int jn = __ffs(todo) - 1;
+        todo &= todo - 1;
+        NodeF6 fj;
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+          fj.lo[k] = __shfl_sync(FULL, f.lo[k], jn);
+          fj.hi[k] = __shfl_sync(FULL, f.hi[k], jn);
         }
-        __syncwarp();
-        if (need) {
-          for (int jj = 0; jj < mm; jj++) {
-            const int ti = nd.start + c0 + jj;
-            if (ti == self || (pass == 0 && ti < self)) continue;  // direct pass: each pair once
-            const int pj = w.par[jj];
-            if (pj == myroot || ti == myroot) continue;
-            const float4 cp = w.sp[jj], cv = w.sv[jj];
-            const float c[6] = {cp.x, cp.y, cp.z, cv.x, cv.y, cv.z};
-            if (pair_lb6f(q32, c, w_lo, e32) >= thr_hi) continue;
-            bool in = pair_ub6f(q32, c, w_hi, e32) < thr_lo;
-            if (!in) in = crit_cmp(2, a.params, xq, mv, tv.pos[ti], tv.vel[ti]);
-            if (in) {
-              int rt = find_root(a.parent, pj, a.err);
-              if (rt != myroot) myroot = find_root(a.parent, myroot, a.err);
-              if (rt != myroot) {
-                unite(a.parent, self, ti, a.err);
-                myroot = find_root(a.parent, self, a.err);
+        const bool need = active && box_lb6f(q32, w_lo, e32, fj) < thr_hi;
+        if (!__any_sync(FULL, need)) continue;
+        if (__shfl_sync(FULL, nd.split_dim, jn) >= 0) {
+          expand |= 1u << jn;
+          continue;
+        }
+        const int nstart = __shfl_sync(FULL, nd.start, jn);
+        const int ncount = __shfl_sync(FULL, nd.count, jn);
+        for (int c0 = 0; c0 < ncount; c0 += 32) {
+          const int mm = min(32, ncount - c0);
+          if (lane < mm) {
+            const int i = nstart + c0 + lane;
+            w.sp[lane] = tv.posf[i];
+            w.sv[lane] = tv.velf[i];
+            w.par[lane] = ld_parent(a.parent, i);
+          }
+          __syncwarp();
+          if (need) {
+            for (int jj = 0; jj < mm; jj++) {
+              const int ti = nstart + c0 + jj;
+              if (ti == self || (pass == 0 && ti < self)) continue;  // direct pass: each pair once
+              const int pj = w.par[jj];
+              if (pj == myroot || ti == myroot) continue;
+              const float4 cp = w.sp[jj], cv = w.sv[jj];
+              const float c[6] = {cp.x, cp.y, cp.z, cv.x, cv.y, cv.z};
+              if (pair_lb6f(q32, c, w_lo, e32) >= thr_hi) continue;
+              bool in = pair_ub6f(q32, c, w_hi, e32) < thr_lo;
+              if (!in) in = crit_cmp(2, a.params, xq, mv, tv.pos[ti], tv.vel[ti]);
+              if (in) {
+                int rt = find_root(a.parent, pj, a.err);
+                if (rt != myroot) myroot = find_root(a.parent, myroot, a.err);
+                if (rt != myroot) {
+                  unite(a.parent, self, ti, a.err);
+                  myroot = find_root(a.parent, self, a.err);
+                }
               }
             }
           }
+          __syncwarp();
         }
-        __syncwarp();
       }
+      // children of the expanded nodes: lane i pushes those of its own node
+      const int ne = __popc(expand);
+      if (sp + 2 * ne > kCritStack) {
+        if (lane == 0) atomicExch(a.err, kErrCapacity);
+        return;
+      }
+      if ((expand >> lane) & 1u) {
+        const int slot = sp + 2 * __popc(expand & ((1u << lane) - 1u));
+        w.stk[slot] = 2 * h + 2;
+        w.stk[slot + 1] = 2 * h + 1;
+      }
+      sp += 2 * ne;
+      __syncwarp();
     }
+    if (sp > 0 && lane == 0) atomicExch(a.err, kErrIterCap);
   }
 }
 
