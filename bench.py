@@ -767,9 +767,9 @@ def run_reference(args, world, rank):
 
 def profile_case(args):
     """A small case of one kernel family, device-resident, for ncu captures: the FOF step
-    (build + FOF), the kNN-density step or the phase-space density step (build + CalcDensity
-    with the local metric) on args.n clustered particles, or the batched density on a
-    power-law group batch of about args.n particles."""
+    (build + FOF), the kNN-density step, the phase-space density step (build + CalcDensity
+    with the local metric) or the FOFCriterion FOF6d step on args.n clustered particles,
+    or the batched density on a power-law group batch of about args.n particles."""
     import torch
 
     from nbodylib_gb300 import BatchedDensity, KDTree, _build
@@ -802,6 +802,18 @@ def profile_case(args):
             t.close()
         torch.cuda.synchronize()
         return
+    if args.profile == "crit6":
+        pos, mass, vel = syn.clustered_box(n, box, seed=2, velocities=True)
+        dpos, dmass, dvel = (torch.from_numpy(a).cuda() for a in (pos, mass, vel))
+        ll = syn.linking_length(n, box)
+        crit = [0, ll * ll, 0, 0, 0, 0, ll * ll, 0.04]
+        for _ in range(args.steps):
+            t = KDTree(dpos, dvel, dmass, BUCKET, kerntype=0, period=[box] * 3, device=True)
+            t.FOFCriterion(2, crit, MINNUM)
+            t.sync()
+            t.close()
+        torch.cuda.synchronize()
+        return
     for _ in range(args.steps):
         per = [box] * 3 if args.profile == "fof" else None
         t = KDTree(dpos, None, dmass, BUCKET, kerntype=0, period=per, device=True)
@@ -824,7 +836,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--profile", choices=["fof", "knn", "build", "batch", "adjoint", "phase"],
+    ap.add_argument("--profile", choices=["fof", "knn", "build", "batch", "adjoint", "phase",
+                                          "crit6"],
                     help="run only `steps` steps of one small case (for ncu), print nothing")
     ap.add_argument("--n", type=int, default=1 << 18, help="particles for --profile")
     args = ap.parse_args()
