@@ -75,3 +75,45 @@ def test_batch_with_one_particle_groups(gpu, port_built):
             continue
         t = oracle.OracleTree(pos[s:e], None, mass[s:e], 16, 0, 0, 1000, None, backend="port")
         assert_density_close(rho[s:e], t.density(min(32, e - s - 1)), f"group {g}")
+
+
+def test_degenerate_parameters(gpu, port_built):
+    """ll = 0 links nothing (the test is strict), minnum above n leaves no group, a ball of
+    radius 0 is empty, and k = n - 1 (every other particle of a 100-particle tree) matches
+    the restatement."""
+    pos, mass = syn.uniform_box(600, 1.0, seed=12)
+    t = KDTree(pos, None, mass, 8, kerntype=KSPH)
+    o = oracle.OracleTree(pos, None, mass, 8, 0, 0, 1000, None, backend="port")
+    g, ng = t.FOF(0.0, 2)
+    assert ng == 0 and not np.any(np.asarray(g))
+    g, ng = t.FOF(0.3, 601)
+    assert ng == 0 and not np.any(np.asarray(g))
+    off, out = t.SearchBallPosTagged(np.arange(600, dtype=np.int32), 0.0)
+    assert int(np.asarray(off)[-1]) == 0
+    t.close()
+    small, ms = syn.uniform_box(100, 1.0, seed=14)
+    t = KDTree(small, None, ms, 8, kerntype=KSPH)
+    o = oracle.OracleTree(small, None, ms, 8, 0, 0, 1000, None, backend="port")
+    assert_density_close(t.CalcDensity(99), o.density(99), "k = n - 1")
+    t.close()
+
+
+def test_exact_duplicates(gpu, port_built):
+    """Coincident particles: the non-periodic target search skips zero distances (the
+    reference's FindNearest(tt), KDLeafNode.cxx:19-21), so a duplicate is never its twin's
+    neighbour; FOF links duplicates (distance 0 < ll)."""
+    base, _ = syn.uniform_box(500, 1.0, seed=13)
+    pos = np.concatenate([base, base[:100]])
+    mass = np.full(len(pos), 1.0 / len(pos))
+    t = KDTree(pos, None, mass, 16, kerntype=KSPH)
+    o = oracle.OracleTree(pos, None, mass, 16, 0, 0, 1000, None, backend="port")
+    nn, d2 = t.FindNearest(8)
+    perm = np.asarray(t.GetPerm())
+    want_nn, want_d2 = o.knn(8)
+    assert_knn_equal(rows_by_id(to_ids(np.asarray(nn), perm), perm), rows_by_id(np.asarray(d2), perm),
+                     want_nn, want_d2, "duplicates")
+    assert np.all(np.asarray(d2) > 0)
+    g, ng = t.FOF(1e-6, 2)
+    go, no = o.fof(1e-6, 2)
+    assert ng == no == 100
+    t.close()
