@@ -773,8 +773,10 @@ def run_reference(args, world, rank):
 def profile_case(args):
     """A small case of one kernel family, device-resident, for ncu captures: the FOF step
     (build + FOF), the kNN-density step, the phase-space density step (build + CalcDensity
-    with the local metric) or the FOFCriterion FOF6d step on args.n clustered particles,
-    or the batched density on a power-law group batch of about args.n particles."""
+    with the local metric), the FOFCriterion FOF6d step or CalcSmoothVel +
+    CalcSmoothVelDisp on args.n clustered particles, SearchBallPosTagged for every particle
+    of args.n uniform ones, or the batched density on a power-law group batch of about
+    args.n particles."""
     import torch
 
     from nbodylib_gb300 import BatchedDensity, KDTree, _build
@@ -805,6 +807,31 @@ def profile_case(args):
             t.CalcDensity(32)
             t.sync()
             t.close()
+        torch.cuda.synchronize()
+        return
+    if args.profile == "smooth":
+        pos, mass, vel = syn.clustered_box(n, box, seed=2, velocities=True)
+        dpos, dmass, dvel = (torch.from_numpy(a).cuda() for a in (pos, mass, vel))
+        t = KDTree(dpos, dvel, dmass, BUCKET, kerntype=0, device=True)
+        rho = t.CalcDensity(32)
+        for _ in range(args.steps):
+            sv = t.CalcSmoothVel(32, rho)
+            t.CalcSmoothVelDisp(sv, 32, rho)
+        t.sync()
+        t.close()
+        torch.cuda.synchronize()
+        return
+    if args.profile == "ball":
+        # uniform periodic unit box, 32 particles per ball on average
+        upos, umass = syn.uniform_box(n, 1.0, seed=7)
+        r2 = (3.0 * 32 / (4.0 * np.pi * n)) ** (2.0 / 3.0)
+        t = KDTree(torch.from_numpy(upos).cuda(), None, torch.from_numpy(umass).cuda(), BUCKET,
+                   kerntype=0, period=[1.0] * 3, device=True)
+        tgt = torch.arange(n, dtype=torch.int32, device="cuda")
+        for _ in range(args.steps):
+            t.SearchBallPosTagged(tgt, r2)
+        t.sync()
+        t.close()
         torch.cuda.synchronize()
         return
     if args.profile == "crit6":
@@ -842,7 +869,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--profile", choices=["fof", "knn", "build", "batch", "adjoint", "phase",
-                                          "crit6"],
+                                          "crit6", "smooth", "ball"],
                     help="run only `steps` steps of one small case (for ncu), print nothing")
     ap.add_argument("--n", type=int, default=1 << 18, help="particles for --profile")
     args = ap.parse_args()
