@@ -38,6 +38,7 @@ class KDTree:
                  period=None, device=False, stream=None):
         self._lib = _capi.load()
         self.device = device
+        self._ball_cap = 0  # largest ball-search output so far (sizes the next buffer)
         if device:
             import torch
             self._torch = torch
@@ -380,16 +381,26 @@ class KDTree:
         return self._ball(self._lib.nbk_ball_tagged_points, x, x.shape[0], fdist2)
 
     def _ball(self, fn, q, nq, fdist2):
+        """One call (count, scan, fill) when the output buffer sized by the largest result
+        of an earlier call on this tree is large enough; otherwise a counting call first
+        (the C ABI returns NBK_ERR_INVALID with *total set when out_capacity is short)."""
         offsets = self._empty(nq + 1, np.int64)
         total = ctypes.c_int64()
-        cap = 0
-        st = fn(self._h, _ptr(q), nq, float(fdist2), _ptr(offsets), None, 0, ctypes.byref(total))
+        cap = self._ball_cap
+        out = None
+        if cap > 0:
+            out = self._empty(cap, np.int32)
+        st = fn(self._h, _ptr(q), nq, float(fdist2), _ptr(offsets), _ptr(out), cap,
+                ctypes.byref(total))
+        if st == 0 and out is not None:
+            return offsets, out[: total.value]
         if st not in (0, 1):
             _capi.check(st)
         cap = max(total.value, 1)
         out = self._empty(cap, np.int32)
         _capi.check(fn(self._h, _ptr(q), nq, float(fdist2), _ptr(offsets), _ptr(out), cap,
                        ctypes.byref(total)))
+        self._ball_cap = max(self._ball_cap, cap)
         return offsets, out[: total.value]
 
     def SearchBallPos(self, target, fdist2, imark, nn, dist2):
