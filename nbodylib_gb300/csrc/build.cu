@@ -456,11 +456,10 @@ __device__ __forceinline__ unsigned block_excl_scan(unsigned v, unsigned* tot, u
 
 // Per chunk: how many keys are below / equal to the median key.
 template <int ND>
-__global__ void __launch_bounds__(kThreads) k_count(const Chunk* __restrict__ chunks,
-                                                    const GNodeT<ND>* __restrict__ g,
-                                                    const double* Cb, int64_t cs,
-                                                    unsigned* cnt_less, unsigned* cnt_eq) {
-  Chunk c = chunks[blockIdx.x];
+__device__ __forceinline__ void count_body(int vb, const Chunk* __restrict__ chunks,
+                                           const GNodeT<ND>* g, const double* Cb, int64_t cs,
+                                           unsigned* cnt_less, unsigned* cnt_eq) {
+  Chunk c = chunks[vb];
   const GNodeT<ND>& s = g[c.g];
   unsigned long long piv = s.prefix;
   unsigned a = 0, e = 0;
@@ -495,27 +494,27 @@ __global__ void __launch_bounds__(kThreads) k_count(const Chunk* __restrict__ ch
       ta += sa[i];
       te += se[i];
     }
-    cnt_less[blockIdx.x] = ta;
-    cnt_eq[blockIdx.x] = te;
+    cnt_less[vb] = ta;
+    cnt_eq[vb] = te;
   }
 }
 
-// One block per node: exclusive scan of the chunk counts (chunk order), the split value,
-// and the number of equal keys that go left.
+// For one node (one block): exclusive scan of the chunk counts (chunk order), the split
+// value, and the number of equal keys that go left.
 template <int ND>
-__global__ void __launch_bounds__(kThreads) k_chunk_scan(GNodeT<ND>* g, const unsigned* cnt_less,
-                                                         const unsigned* cnt_eq,
-                                                         unsigned* base_less, unsigned* base_eq,
-                                                         NodeOut<ND> out) {
+__device__ __forceinline__ void scan_body(int vn, GNodeT<ND>* g, const unsigned* cnt_less,
+                                          const unsigned* cnt_eq, unsigned* base_less,
+                                          unsigned* base_eq, NodeOut<ND> out) {
   __shared__ unsigned wsum[32];
   __shared__ unsigned tot;
-  const GNodeT<ND>& sg = g[blockIdx.x];
+  const GNodeT<ND>& sg = g[vn];
   const int nchunks = sg.nchunks, first_chunk = sg.first_chunk;
   unsigned run_l = 0, run_e = 0;
   for (int c0 = 0; c0 < nchunks; c0 += kThreads) {
     int c = c0 + threadIdx.x;
-    unsigned vl = c < nchunks ? cnt_less[first_chunk + c] : 0;
-    unsigned ve = c < nchunks ? cnt_eq[first_chunk + c] : 0;
+    // read through L2: in k_count_scan other blocks wrote these counts during the launch
+    unsigned vl = c < nchunks ? __ldcg(&cnt_less[first_chunk + c]) : 0;
+    unsigned ve = c < nchunks ? __ldcg(&cnt_eq[first_chunk + c]) : 0;
     unsigned el = block_excl_scan(vl, &tot, wsum);
     unsigned tl = tot;
     unsigned ee = block_excl_scan(ve, &tot, wsum);
@@ -531,11 +530,33 @@ __global__ void __launch_bounds__(kThreads) k_chunk_scan(GNodeT<ND>* g, const un
     // after selection n_less counts every key below the median key; rank k + 1 particles
     // go left: all of those plus (k_total + 1 - n_less) equal keys.
     int ktot = (sg.size - 1) / 2;
-    g[blockIdx.x].need_eq = ktot + 1 - (int)run_l;
-    g[blockIdx.x].total_eq = (int)run_e;
-    g[blockIdx.x].n_less = (int)run_l;
+    g[vn].need_eq = ktot + 1 - (int)run_l;
+    g[vn].total_eq = (int)run_e;
+    g[vn].n_less = (int)run_l;
     out.set_split(sg.node, okey_inv(sg.prefix));
   }
+}
+
+// k_count and k_chunk_scan in one launch: each block counts its chunk, and the node's
+// last-arriving block (arrival counter, no waiting) scans the node's chunk counts.
+template <int ND>
+__global__ void __launch_bounds__(kThreads) k_count_scan(const Chunk* __restrict__ chunks,
+                                                         GNodeT<ND>* g, const double* Cb,
+                                                         int64_t cs, unsigned* cnt_less,
+                                                         unsigned* cnt_eq, unsigned* base_less,
+                                                         unsigned* base_eq, NodeOut<ND> out) {
+  __shared__ int s_last;
+  count_body<ND>((int)blockIdx.x, chunks, g, Cb, cs, cnt_less, cnt_eq);
+  const int node = chunks[blockIdx.x].g;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0)
+    s_last = atomicAdd(&g[node].done, 1u) == (unsigned)g[node].nchunks - 1u;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  scan_body<ND>(node, g, cnt_less, cnt_eq, base_less, base_eq, out);
+  if (threadIdx.x == 0) g[node].done = 0u;
 }
 
 // Stable 3-way partition of every node of a level around its median key into the other
@@ -1178,7 +1199,7 @@ static int build_forest_t(const std::vector<TreeSpec>& trees, int b, const doubl
     GNode* d_gnext = li + 1 < levels.size() ? d_gall + levels[li + 1].g0 : nullptr;
     Chunk* d_c = d_call + L.c0;
     unsigned *cl = d_cl + L.c0, *ce = d_ce + L.c0, *bl = d_bl + L.c0, *be = d_be + L.c0;
-    int ng = L.ng, nc = L.nc;
+    int nc = L.nc;
     const double* C = L.buf ? Cb : Ca;
     const int* I = L.buf ? IDb : IDa;
     double* C2 = L.buf ? Ca : Cb;
@@ -1191,8 +1212,8 @@ static int build_forest_t(const std::vector<TreeSpec>& trees, int b, const doubl
       k_radix<ND><<<nc, kThreads, 0, st>>>(d_c, d_g, C, cs, d_hist, d_cand, pass, nout, (int)p0,
                                            d_err); note_launch();
     }
-    k_count<ND><<<nc, kThreads, 0, st>>>(d_c, d_g, C, cs, cl, ce); note_launch();
-    k_chunk_scan<ND><<<ng, kThreads, 0, st>>>(d_g, cl, ce, bl, be, nout); note_launch();
+    k_count_scan<ND><<<nc, kThreads, 0, st>>>(d_c, d_g, C, cs, cl, ce, bl, be, nout);
+    note_launch();
     k_scatter<ND><<<nc, kThreads, 0, st>>>(d_c, d_g, C, I, C2, I2, cs, bl, be, d_err, d_gnext);
     note_launch();
     NBK_CUDA_TRY(cudaGetLastError());
