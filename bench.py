@@ -3,9 +3,13 @@
 Default workload (the FOF configuration): 2^20 particles, 70% in 500 Plummer spheres
 + 30% uniform background, periodic box L=100, linking length 0.2 x mean spacing,
 minnum 20. One step = GPU tree build (bucket 16) + FOF, i.e. the reference's
-KDTree(...) + FOF(ll, ngroup, 20). The line also reports the kNN-density workloads
-(32768 uniform particles in the periodic unit box with k=32 FindNearest + CalcDensity,
-and 2^20 clustered particles with CalcDensity(32)) under "components".
+KDTree(...) + FOF(ll, ngroup, 20). The line also carries the other parts of the metric
+under "metric_parts": kNN-density rates (32768 uniform particles in the periodic unit box
+with k=32 FindNearest + CalcDensity, 2^20 clustered particles with CalcDensity(32), 256^3
+clustered particles with CalcDensity(64) + CalcVelDensity(64, 64)), the batched path on
+20,000 power-law groups against the per-tree loop, and the adjoint's cost. Every
+component's full record (phases, CPU figures) goes to the file named by
+"components_file" (NBKDT_BENCH_DETAIL, default bench_components.json in the temp dir).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -151,6 +155,81 @@ def fof_inputs():
     return pos, mass, syn.linking_length(N_FOF, BOX)
 
 
+def fof_config(ll, groups, world):
+    """The workload description both arms print (identical keys and values)."""
+    return {"workload": "FOF, 2^20 clustered particles, periodic L=100, ll=0.2 mean "
+                        "spacing, minnum 20; step = tree build (b=16) + FOF",
+            "n": N_FOF, "bucket": BUCKET, "minnum": MINNUM, "linking_length": ll,
+            "groups": int(groups), "l2": "flushed (512 MB write) before every timed step",
+            "parallelism": f"replicas x{world}"}
+
+
+def write_components(comps):
+    """Write the full per-workload record to a JSON file and return its path; the stdout
+    line keeps only the summary (metric_parts). NBKDT_BENCH_DETAIL names the file; the
+    default is bench_components.json in the system temp directory."""
+    path = os.environ.get("NBKDT_BENCH_DETAIL") or os.path.join(tempfile.gettempdir(),
+                                                                "bench_components.json")
+    try:
+        d = os.path.dirname(path)
+        if d:
+            os.makedirs(d, exist_ok=True)
+        with open(path, "w") as f:
+            json.dump(comps, f, indent=1)
+    except OSError as e:
+        log(f"bench: could not write {path}: {e}")
+        return None
+    return path
+
+
+def metric_parts(fof_value, comps):
+    """The three parts of the metric, short enough for one stdout line: FOF particles/s
+    (the headline value), kNN-density queries/s with the FP64 roofline fraction of the
+    density kernel, the batched path against the per-tree loop, and the adjoint cost."""
+    def g(d, *keys):
+        for k in keys:
+            if not isinstance(d, dict) or k not in d:
+                return None
+            d = d[k]
+        return d
+
+    def r(x, nd=4):
+        return None if x is None else float(f"{x:.{nd}g}")
+
+    knn = {}
+    for name in ("uniform_32768_periodic_k32", "clustered_2pow20_k32"):
+        c = comps.get(name, {})
+        knn[name] = {"density_kernel_queries_per_s": r(c.get("density_queries_per_s")),
+                     "step_queries_per_s": r(c.get("queries_per_s_step")),
+                     "fp64_frac": r(g(c, "roofline_fp64", "frac"), 3),
+                     "cpu_findnearest_queries_per_s": r(g(c, "cpu", "findnearest_queries_per_s"))}
+    c3 = comps.get("clustered_256cubed_k64_density_veldensity", {})
+    n3 = c3.get("n", 1 << 24)
+    knn["clustered_256cubed_k64"] = {
+        "density_kernel_queries_per_s": r(n3 / (c3["density_kernel_ms"] / 1e3))
+        if c3.get("density_kernel_ms") else None,
+        "veldensity_kernel_queries_per_s": r(n3 / (c3["veldensity_kernel_ms"] / 1e3))
+        if c3.get("veldensity_kernel_ms") else None,
+        "fp64_frac": r(g(c3, "roofline_fp64_density", "frac"), 3),
+        "cpu_density_queries_per_s": r(g(c3, "cpu", "density_queries_per_s"))}
+    b = comps.get("batched_20000_groups_k32", {})
+    at = b.get("autotuned", {})
+    batched = {"particles": b.get("particles"),
+               "build_plus_search_speedup": r(g(b, "build_plus_search", "speedup"), 4),
+               "search_only_speedup": r(g(b, "search_only", "speedup"), 4),
+               "batched_graph_ms": r(g(b, "search_only", "batched_graph_ms")),
+               "pertree_loop_ms": r(g(b, "build_plus_search", "pertree_loop_ms")),
+               "autotuned": {k: at.get(k) for k in ("bucket", "query_bucket",
+                                                   "warp_per_query", "batched_graph_ms")},
+               "queries_per_s": r(b.get("batched_queries_per_s"))}
+    a = comps.get("adjoint_clustered_2pow20_k32", {})
+    return {"fof_particles_per_s": r(fof_value),
+            "knn_density": knn,
+            "batched_vs_pertree": batched,
+            "adjoint_backward_over_forward": r(a.get("backward_over_forward"), 3),
+            "fp64_peak_gflops_measured": r(comps.get("fp64_peak_gflops_measured"))}
+
+
 def run_gpu(args, world, rank, local):
     import torch
 
@@ -231,16 +310,13 @@ def run_gpu(args, world, rank, local):
         achieved = 28.0 * N_FOF / per_launch_s / 1e9
     phases = {k: round(v["ms"] / max(v["count"], 1), 4) for k, v in trace.items()}
     comps = components(args, lib)
+    detail_path = write_components(comps)
     result = {
         "metric": METRIC, "value": value, "unit": "particles/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot_s * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded clustered Plummer spheres + background)",
-        "config": {"workload": "FOF, 2^20 clustered particles, periodic L=100, ll=0.2 mean "
-                               "spacing, minnum 20; step = GPU tree build (b=16) + FOF",
-                   "n": N_FOF, "bucket": BUCKET, "minnum": MINNUM, "linking_length": ll,
-                   "groups": ng, "l2": "flushed (512 MB write) before every timed step",
-                   "parallelism": f"replicas x{world}"},
+        "config": fof_config(ll, ng, world),
         "e2e": {"value": e2e, "unit": "particles/s", "steps": e2e_steps,
                 "h2d_bytes_per_step": int(pos.nbytes + mass.nbytes),
                 "d2h_bytes_per_step": int(g.nbytes + 4)},
@@ -255,7 +331,8 @@ def run_gpu(args, world, rank, local):
                      "algorithmic_bytes_per_launch": 28 * N_FOF},
         "phase_ms_per_step": phases,
         "clocks": clocks,
-        "components": comps,
+        "metric_parts": metric_parts(value, comps),
+        "components_file": detail_path,
     }
     if rank == 0 and not args.no_cpu:
         result["cpu_baseline"] = cpu_baseline_fof(pos, mass, ll)
@@ -742,27 +819,34 @@ def run_reference(args, world, rank):
     oracle.build(ref=False)
     pos, mass, ll = fof_inputs()
     threads = os.cpu_count() or 1
-    for _ in range(min(args.warmup, 1)):
+    # the host caches are flushed before every timed step, as the GPU arm flushes L2
+    flush = np.zeros(512 << 20, dtype=np.uint8)
+
+    def step():
         o = oracle.OracleTree(pos, None, mass, BUCKET, 0, 0, 1000, [BOX] * 3, backend="port",
                               nthreads=threads)
-        o.fof(ll, MINNUM)
+        _, ng = o.fof(ll, MINNUM)
         o.close()
-    steps = max(1, min(args.steps, 5))
-    t0 = time.perf_counter()
+        return ng
+
+    ng = 0
+    for _ in range(args.warmup):
+        ng = step()
+    steps = max(1, args.steps)
+    dt = 0.0
     for _ in range(steps):
-        o = oracle.OracleTree(pos, None, mass, BUCKET, 0, 0, 1000, [BOX] * 3, backend="port",
-                              nthreads=threads)
-        o.fof(ll, MINNUM)
-        o.close()
-    dt = (time.perf_counter() - t0) / steps
+        flush[::64] += 1
+        t0 = time.perf_counter()
+        ng = step()
+        dt += time.perf_counter() - t0
+    dt /= steps
     v = N_FOF / dt
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": "particles/s",
-            "n_gpus": world, "steps": steps, "warmup": min(args.warmup, 1),
+            "n_gpus": world, "steps": steps, "warmup": args.warmup,
             "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "FOF, 2^20 clustered particles, periodic L=100, ll=0.2 mean "
-                                   "spacing, minnum 20; step = tree build (b=16) + FOF",
-                       "n": N_FOF},
+            "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded clustered Plummer spheres + background)",
+            "config": fof_config(ll, ng, world),
             "cpu_baseline": {"value": v, "unit": "particles/s", "cores": threads, "kind": "port",
                              "sample": f"{steps} full steps on the host cores (build with "
                                        f"{threads} OpenMP threads, FOF serial as shipped)"},
