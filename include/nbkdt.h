@@ -106,6 +106,25 @@ int nbk_trace_enable(int on);
 int nbk_trace_reset(void);
 int64_t nbk_trace_json(char* buf, int64_t cap);
 
+/* The compute capability (major*10 + minor) of the SASS and PTX that the CUDA runtime
+   selected on the current device for one product kernel (the scatter to input order that
+   every density call launches): 103 and 103 for an sm_103a build. (No reference
+   counterpart.) */
+int nbk_kernel_binary_version(int* binary_version, int* ptx_version);
+
+/* ---- test hooks (no reference counterpart: the reference loops without bound and
+   exits on failure, KDCalcSmoothQuantities.cxx:273-276, PriorityQueue.h:49-53) ---- */
+/* Iteration cap of the union-find loops of FOF, FOFCriterion and FOFNNCriterion on the
+   current device (default 2^24; cap <= 0 restores it). A loop that reaches the cap stops,
+   sets the call's device error word, and the call returns NBK_ERR_DEVICE. */
+int nbk_debug_set_iteration_cap(int cap);
+/* Make the device allocation `countdown` allocations from now (0 = the next) fail with
+   NBK_ERR_NOMEM, once; a negative countdown disarms. */
+int nbk_debug_fail_allocation(long long countdown);
+/* Device allocations the library currently holds (trees, batches, per-call scratch not
+   yet freed); a failed call must leave it where it was. */
+long long nbk_debug_live_allocations(void);
+
 /*
  * Build a tree. Replaces KDTree::KDTree(Particle*, Int_t numparts, Int_t bucket_size,
  * int TreeType, int KernType, int KernRes, int SplittingCriterion, int Aniso,
@@ -202,14 +221,15 @@ int nbk_knn_phase_points(nbk_tree* tree, const double* x, int64_t nq, int k, int
 int nbk_density(nbk_tree* tree, int k, double* rho);
 
 /* nbk_density without any device allocation (no counterpart in the reference: it exists
-   for callers that cannot allocate device memory while they run, e.g. codes that own all
-   HBM through their own pool, or work inside a stream being captured into a CUDA graph).
-   The tree must already exist; rho_dev is a caller-owned DEVICE buffer of n doubles
-   (input order), whatever the tree's pointer mode. The scratch is a static device array
-   of 4,194,304 doubles (32 MiB, held per GPU until exit): larger trees return
-   NBK_ERR_INVALID. All calls share it, so calls that overlap on the GPU race and must be
-   serialised by the caller. The first call on each device sets the scratch up; make it
-   before any stream capture. */
+   for callers that cannot allocate device memory while they run, e.g. simulation codes
+   and in-situ halo finders that reserve the GPU's memory for their own pool at start-up
+   and allow no allocation afterwards). The tree must already exist; rho_dev is a
+   caller-owned DEVICE buffer of n doubles (input order), whatever the tree's pointer
+   mode. The scratch is a static device array of 4,194,304 doubles (32 MiB, held per GPU
+   until exit): larger trees return NBK_ERR_INVALID. All calls share it, so calls that
+   overlap on the GPU race and must be serialised by the caller. The call runs on the
+   tree's device and returns when its GPU work has finished; the first call on each
+   device looks the scratch's address up. */
 int nbk_density_noalloc(nbk_tree* tree, int k, double* rho_dev);
 
 /* Gather-only density of selected particles. Replaces KDTree::CalcDensityParticle

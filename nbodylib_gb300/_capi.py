@@ -29,6 +29,10 @@ SIGNATURES = {
     "nbk_trace_enable": (c_int, [c_int]),
     "nbk_trace_reset": (c_int, []),
     "nbk_trace_json": (c_i64, [ctypes.c_char_p, c_i64]),
+    "nbk_kernel_binary_version": (c_int, [ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
+    "nbk_debug_set_iteration_cap": (c_int, [c_int]),
+    "nbk_debug_fail_allocation": (c_int, [ctypes.c_longlong]),
+    "nbk_debug_live_allocations": (ctypes.c_longlong, []),
     "nbk_create": (c_int, [c_vp, c_vp, c_vp, c_i64, c_int, c_int, c_int, c_int, c_int, c_int,
                            c_int, c_vp, ctypes.c_uint, ctypes.POINTER(c_vp)]),
     "nbk_destroy": (c_int, [c_vp]),

@@ -102,6 +102,25 @@ void drop_graphs(nbk_batch* B) {
   B->graphs.clear();
 }
 
+// Everything a batch owns on the device (null entries skipped), its graphs and its
+// stream; used by nbk_batch_destroy and by a failed nbk_batch_create.
+void batch_release(nbk_batch* B) {
+  drop_graphs(B);
+  free_arrays(B);
+  if (B->own_inputs) {
+    dev_free(B->d_pos_in, B->st);
+    dev_free(B->d_mass_in, B->st);
+  }
+  void* owned[] = {B->d_kernel, B->d_counter, B->d_err, B->d_rho_tree, B->d_rho_out};
+  for (void* p : owned) dev_free(p, B->st);
+  B->d_pos_in = B->d_mass_in = B->d_kernel = B->d_rho_tree = B->d_rho_out = nullptr;
+  B->d_counter = B->d_err = nullptr;
+  if (B->st) cudaStreamSynchronize(B->st);
+  if (B->own_stream && B->st) cudaStreamDestroy(B->st);
+  B->st = nullptr;
+  B->own_stream = false;
+}
+
 // Work items: (tree, q0, count) buckets of qb queries, largest trees first.
 int make_items(nbk_batch* B, int qb) {
   std::vector<int> order(B->ngroups);
@@ -298,6 +317,13 @@ int nbk_batch_create(const double* pos, const double* mass, const int64_t* offse
     return NBK_ERR_UNSUPPORTED;
   }
   std::unique_ptr<nbk_batch> B(new nbk_batch);
+  // a failed creation frees whatever it had already allocated
+  struct ReleaseOnFailure {
+    nbk_batch* B;
+    ~ReleaseOnFailure() {
+      if (B) batch_release(B);
+    }
+  } guard{B.get()};
   B->ngroups = ngroups;
   B->flags = flags;
   B->kerntype = (kerntype >= NBK_KSPH && kerntype <= NBK_KTH) ? kerntype : NBK_KSPH;
@@ -330,6 +356,7 @@ int nbk_batch_create(const double* pos, const double* mass, const int64_t* offse
     B->d_pos_in = const_cast<double*>(pos);
     B->d_mass_in = const_cast<double*>(mass);
   } else {
+    B->own_inputs = true;  // before the allocations: a failed one frees the other
     NBK_TRY(dev_malloc((void**)&B->d_pos_in, sizeof(double) * 3 * n, st));
     NBK_CUDA_TRY(cudaMemcpyAsync(B->d_pos_in, pos, sizeof(double) * 3 * B->ntot,
                                  cudaMemcpyHostToDevice, st));
@@ -338,7 +365,6 @@ int nbk_batch_create(const double* pos, const double* mass, const int64_t* offse
       NBK_CUDA_TRY(cudaMemcpyAsync(B->d_mass_in, mass, sizeof(double) * B->ntot,
                                    cudaMemcpyHostToDevice, st));
     }
-    B->own_inputs = true;
   }
   kernel_table(B->kerntype, B->kernres, 3, B->h_kernel, B->kernnorm);
   kernel_device_image(B->h_kernel, B->h_kernel_img);
@@ -352,7 +378,9 @@ int nbk_batch_create(const double* pos, const double* mass, const int64_t* offse
   NBK_TRY(dev_malloc((void**)&B->d_rho_out, sizeof(double) * n, st));
   // FP32 rounding bound of every coordinate
   unsigned long long* d_m;
-  NBK_TRY(dev_malloc((void**)&d_m, sizeof(unsigned long long), st));
+  DevAlloc tmp;  // frees d_m on every path out
+  tmp.st = st;
+  NBK_TRY(tmp.get((void**)&d_m, sizeof(unsigned long long)));
   NBK_CUDA_TRY(cudaMemsetAsync(d_m, 0, sizeof(unsigned long long), st));
   if (B->ntot > 0) {
     k_maxabs<<<256, 256, 0, st>>>(B->d_pos_in, 3 * B->ntot, d_m);
@@ -361,7 +389,6 @@ int nbk_batch_create(const double* pos, const double* mass, const int64_t* offse
   unsigned long long hm = 0;
   NBK_CUDA_TRY(cudaMemcpyAsync(&hm, d_m, sizeof(hm), cudaMemcpyDeviceToHost, st));
   NBK_CUDA_TRY(cudaStreamSynchronize(st));
-  dev_free(d_m, st);
   double maxabs;
   memcpy(&maxabs, &hm, sizeof(double));
   if (!std::isfinite(maxabs)) {
@@ -371,6 +398,7 @@ int nbk_batch_create(const double* pos, const double* mass, const int64_t* offse
   B->eps = (float)std::ldexp(maxabs, -23) * 1.0001f + 1e-38f;
   if (bucket_size <= 0) NBK_TRY(autotune(B.get()));
   else NBK_TRY(batch_build(B.get(), bucket_size));
+  guard.B = nullptr;
   *out = B.release();
   return NBK_OK;
   BAPI_END
@@ -378,19 +406,7 @@ int nbk_batch_create(const double* pos, const double* mass, const int64_t* offse
 
 int nbk_batch_destroy(nbk_batch* B) {
   if (!B) return NBK_OK;
-  drop_graphs(B);
-  free_arrays(B);
-  if (B->own_inputs) {
-    dev_free(B->d_pos_in, B->st);
-    dev_free(B->d_mass_in, B->st);
-  }
-  dev_free(B->d_kernel, B->st);
-  dev_free(B->d_counter, B->st);
-  dev_free(B->d_err, B->st);
-  dev_free(B->d_rho_tree, B->st);
-  dev_free(B->d_rho_out, B->st);
-  cudaStreamSynchronize(B->st);
-  if (B->own_stream) cudaStreamDestroy(B->st);
+  batch_release(B);
   delete B;
   return NBK_OK;
 }

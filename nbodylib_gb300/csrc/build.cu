@@ -1220,12 +1220,7 @@ static int build_forest_t(const std::vector<TreeSpec>& trees, int b, const doubl
   }
   if (!lroots.empty()) {
     size_t sm = LocalLayout<ND>::total;
-    static bool attr_set = false;
-    if (!attr_set) {
-      NBK_CUDA_TRY(cudaFuncSetAttribute(k_local_build<ND>,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-      attr_set = true;
-    }
+    NBK_TRY(ensure_dyn_smem((const void*)k_local_build<ND>, (int)sm));
     k_local_build<ND><<<(unsigned)lroots.size(), kLocalThreads, sm, st>>>(
         d_r, Ca, IDa, Cb, IDb, cs, d_mass_in, d_vel_in, b, nout, pout, d_err, (int)p0);
     note_launch();

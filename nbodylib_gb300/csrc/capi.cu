@@ -191,8 +191,22 @@ Phase::~Phase() {
   g_pending.push_back({name, a, b});
 }
 
+// Live device allocations made through dev_malloc (freed through dev_free), and the
+// test hook that makes one chosen future allocation fail (-1: disarmed).
+static std::atomic<long long> g_live_allocs{0};
+static std::atomic<long long> g_fail_countdown{-1};
+
 int dev_malloc(void** p, size_t bytes, cudaStream_t st) {
   ensure_pool();
+  long long c = g_fail_countdown.load(std::memory_order_relaxed);
+  while (c >= 0 && !g_fail_countdown.compare_exchange_weak(c, c - 1)) {
+  }
+  if (c == 0) {
+    set_error(std::string("device allocation of ") + std::to_string(bytes) +
+              " bytes failed: injected failure (nbk_debug_fail_allocation)");
+    *p = nullptr;
+    return NBK_ERR_NOMEM;
+  }
   cudaError_t e = cudaMallocAsync(p, std::max<size_t>(bytes, 16), st);
   if (e != cudaSuccess) {
     set_error(std::string("device allocation of ") + std::to_string(bytes) +
@@ -200,10 +214,27 @@ int dev_malloc(void** p, size_t bytes, cudaStream_t st) {
     *p = nullptr;
     return NBK_ERR_NOMEM;
   }
+  g_live_allocs.fetch_add(1, std::memory_order_relaxed);
   return NBK_OK;
 }
 void dev_free(void* p, cudaStream_t st) {
-  if (p) cudaFreeAsync(p, st);
+  if (!p) return;
+  cudaFreeAsync(p, st);
+  g_live_allocs.fetch_sub(1, std::memory_order_relaxed);
+}
+
+int ensure_dyn_smem(const void* func, int bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, int> done;
+  int dev = 0;
+  NBK_CUDA_TRY(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  auto key = std::make_pair(dev, func);
+  auto it = done.find(key);
+  if (it != done.end() && it->second >= bytes) return NBK_OK;
+  NBK_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  done[key] = bytes;
+  return NBK_OK;
 }
 int DevAlloc::get(void** p, size_t bytes) {
   NBK_TRY(dev_malloc(p, bytes, st));
@@ -234,6 +265,7 @@ using namespace nbk;
 
 struct nbk_tree {
   int64_t n = 0;
+  int device = 0;  // the CUDA device the tree's arrays live on (current at nbk_create)
   int b = 16, treetype = 0, kerntype = 0, kernres = 1000;
   int aniso = 0;  // phase-space trees: -1 plain phase distance, 0 local metric
   bool periodic = false;
@@ -274,6 +306,19 @@ struct nbk_tree {
     return v;
   }
 };
+
+// Frees every device array a tree owns (null entries are skipped) and waits for the
+// stream; used by nbk_destroy and by a failed nbk_create.
+static void free_tree_arrays(nbk_tree* t) {
+  cudaStream_t st = t->st;
+  BuiltArrays& A = t->arr;
+  void* arrays[] = {A.pos, A.posf, A.vel, A.perm, A.node, A.nodex, A.nodes6, A.nodeb6,
+                    A.nodef6, A.velf, t->d_err};
+  for (void* p : arrays) dev_free(p, st);
+  A = BuiltArrays();
+  t->d_err = nullptr;  // t->d_kernel belongs to the process-wide kernel cache
+  cudaStreamSynchronize(st);
+}
 
 #define API_BEGIN try {
 #define API_END                                          \
@@ -416,6 +461,7 @@ int density_into_scratch(nbk_tree* t, int k, double* scratch, double* rho_dev) {
   return check_err(t, "nbk_density_noalloc");
 }
 int64_t tree_size(const nbk_tree* t) { return t ? t->n : 0; }
+int tree_device(const nbk_tree* t) { return t ? t->device : 0; }
 }  // namespace nbk
 
 extern "C" {
@@ -423,6 +469,26 @@ extern "C" {
 const char* nbk_last_error(void) { return get_error(); }
 
 long long nbk_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int nbk_kernel_binary_version(int* binary_version, int* ptx_version) {
+  cudaFuncAttributes fa{};
+  // k_scatter_d: the scatter back to input order that every density call launches
+  NBK_CUDA_TRY(cudaFuncGetAttributes(&fa, (const void*)k_scatter_d));
+  if (binary_version) *binary_version = fa.binaryVersion;
+  if (ptx_version) *ptx_version = fa.ptxVersion;
+  return NBK_OK;
+}
+
+int nbk_debug_set_iteration_cap(int cap) { return set_uf_iteration_cap(cap); }
+
+int nbk_debug_fail_allocation(long long countdown) {
+  g_fail_countdown.store(countdown < 0 ? -1 : countdown);
+  return NBK_OK;
+}
+
+long long nbk_debug_live_allocations(void) {
+  return g_live_allocs.load(std::memory_order_relaxed);
+}
 
 int nbk_trace_enable(int on) {
   g_trace_on.store(on != 0);
@@ -509,6 +575,14 @@ int nbk_create(const double* pos, const double* vel, const double* mass, int64_t
     return NBK_ERR_UNSUPPORTED;
   }
   std::unique_ptr<nbk_tree> t(new nbk_tree);
+  // a failed creation frees whatever device arrays it had already allocated
+  struct FreeOnFailure {
+    nbk_tree* t;
+    ~FreeOnFailure() {
+      if (t) free_tree_arrays(t);
+    }
+  } guard{t.get()};
+  NBK_CUDA_TRY(cudaGetDevice(&t->device));
   t->n = n;
   t->b = bucket_size;
   t->treetype = treetype;
@@ -622,6 +696,7 @@ int nbk_create(const double* pos, const double* vel, const double* mass, int64_t
   double maxper = std::max(t->period[0], std::max(t->period[1], t->period[2]));
   t->eps = (float)std::ldexp(maxabs + maxper, -23) * 1.0001f + 1e-38f;
   alloc.release_all_scratch(st);
+  guard.t = nullptr;
   *out = t.release();
   return NBK_OK;
   API_END
@@ -629,20 +704,7 @@ int nbk_create(const double* pos, const double* vel, const double* mass, int64_t
 
 int nbk_destroy(nbk_tree* t) {
   if (!t) return NBK_OK;
-  cudaStream_t st = t->st;
-  dev_free(t->arr.pos, st);
-  dev_free(t->arr.posf, st);
-  dev_free(t->arr.vel, st);
-  dev_free(t->arr.perm, st);
-  dev_free(t->arr.node, st);
-  dev_free(t->arr.nodex, st);
-  dev_free(t->arr.nodes6, st);
-  dev_free(t->arr.nodeb6, st);
-  dev_free(t->arr.nodef6, st);
-  dev_free(t->arr.velf, st);
-  // t->d_kernel belongs to the process-wide kernel cache
-  dev_free(t->d_err, st);
-  cudaStreamSynchronize(st);
+  free_tree_arrays(t);
   delete t;
   return NBK_OK;
 }

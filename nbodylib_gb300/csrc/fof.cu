@@ -29,14 +29,19 @@ namespace nbk {
 
 namespace {
 
-constexpr int kCap = 1 << 24;  // iteration cap for union-find loops
+// Iteration cap of every union-find loop (root finding, flattening, uniting). The
+// default is far above any chain the link phase leaves; a loop that reaches it sets
+// kErrIterCap and returns, and the host reports NBK_ERR_DEVICE. Adjustable per device
+// through nbk_debug_set_iteration_cap (a test hook that makes the limit run out).
+constexpr int kCapDefault = 1 << 24;
+__constant__ int c_uf_cap = kCapDefault;
 
 __device__ __forceinline__ int ld_parent(const int* p, int x) {
   return *((volatile const int*)p + x);
 }
 
 __device__ __forceinline__ int find_root(int* parent, int x, int* err) {
-  for (int it = 0; it < kCap; it++) {
+  for (int it = 0; it < c_uf_cap; it++) {
     int p = ld_parent(parent, x);
     if (p == x) return x;
     int gp = ld_parent(parent, p);
@@ -48,7 +53,8 @@ __device__ __forceinline__ int find_root(int* parent, int x, int* err) {
 }
 
 __device__ __forceinline__ void unite(int* parent, int a, int b, int* err) {
-  for (int it = 0; it < 1 << 20; it++) {
+  const int cap = min(c_uf_cap, 1 << 20);
+  for (int it = 0; it < cap; it++) {
     a = find_root(parent, a, err);
     b = find_root(parent, b, err);
     if (a == b) return;
@@ -639,7 +645,7 @@ __global__ void k_carry_roots(const int* parent6, const int* perm6, int* parent,
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= n) return;
   int r = j;
-  for (int it = 0; it < kCap; it++) {
+  for (int it = 0; it < c_uf_cap; it++) {
     int p = parent6[r];
     if (p == r) break;
     r = p;
@@ -782,7 +788,7 @@ __global__ void k_compress(int* parent, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int x = i;
-  for (int it = 0; it < kCap; it++) {
+  for (int it = 0; it < c_uf_cap; it++) {
     int p = ld_parent(parent, x);
     if (p == x) break;
     x = p;
@@ -796,12 +802,12 @@ __global__ void k_flatten_count(int* parent, int n, int* cnt, int* err) {
   int x = valid ? i : -1;
   if (valid) {
     int it = 0;
-    for (; it < kCap; it++) {
+    for (; it < c_uf_cap; it++) {
       int p = parent[x];
       if (p == x) break;
       x = p;
     }
-    if (it == kCap) atomicExch(err, kErrIterCap);
+    if (it == c_uf_cap) atomicExch(err, kErrIterCap);
     parent[i] = x;  // no concurrent writers remain; roots are untouched
   }
   // neighbouring particles mostly share a root: one atomic per distinct root in the warp
@@ -1056,6 +1062,13 @@ int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tr
     k_relabel<<<(n + 255) / 256, 256, 0, st>>>(d_group_tree, newlbl, n); note_launch();
     NBK_CUDA_TRY(cudaGetLastError());
   }
+  return NBK_OK;
+}
+
+// Union-find iteration cap on the current device; cap <= 0 restores the default.
+int set_uf_iteration_cap(int cap) {
+  int v = cap > 0 ? cap : kCapDefault;
+  NBK_CUDA_TRY(cudaMemcpyToSymbol(c_uf_cap, &v, sizeof(int)));
   return NBK_OK;
 }
 

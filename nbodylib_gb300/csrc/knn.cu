@@ -4,6 +4,8 @@
 // CalcDensityPosition / CalcVelDensityPosition (:1092-1207) as epilogues of the warp
 // search of knn_core.cuh.
 #include <algorithm>
+#include <map>
+#include <mutex>
 
 #include "knn_core.cuh"
 
@@ -187,12 +189,7 @@ template <int KMAX, int EPI>
 int launch_t(const KnnArgs& a, cudaStream_t st) {
   constexpr int WPB = warps_per_block<KMAX>();
   size_t sm = sizeof(WarpSmem<KMAX>) * WPB;
-  static bool set = false;
-  if (!set) {
-    NBK_CUDA_TRY(cudaFuncSetAttribute(k_knn<KMAX, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)sm));
-    set = true;
-  }
+  NBK_TRY(ensure_dyn_smem((const void*)k_knn<KMAX, EPI>, (int)sm));
   int warps = (a.nq + 31) / 32;
   int blocks = (warps + WPB - 1) / WPB;
   if (blocks == 0) return NBK_OK;
@@ -218,15 +215,24 @@ template <int KMAX>
 int launch_batch_t(const KnnArgs& a, const BatchArgs& b, cudaStream_t st) {
   constexpr int WPB = warps_per_block<KMAX>();
   size_t sm = sizeof(WarpSmem<KMAX>) * WPB;
-  static int grid = 0;
+  // persistent grid: every resident block of this device (cached per device)
+  static std::mutex mu;
+  static std::map<int, int> grids;
+  int dev = 0, grid = 0;
+  NBK_CUDA_TRY(cudaGetDevice(&dev));
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = grids.find(dev);
+    if (it != grids.end()) grid = it->second;
+  }
   if (grid == 0) {
-    NBK_CUDA_TRY(cudaFuncSetAttribute(k_knn_batch<KMAX>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    int dev = 0, nsm = 0, per = 0;
-    NBK_CUDA_TRY(cudaGetDevice(&dev));
+    NBK_TRY(ensure_dyn_smem((const void*)k_knn_batch<KMAX>, (int)sm));
+    int nsm = 0, per = 0;
     NBK_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     NBK_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_knn_batch<KMAX>, 32 * WPB, sm));
     grid = nsm * (per > 0 ? per : 1);
+    std::lock_guard<std::mutex> lk(mu);
+    grids[dev] = grid;
   }
   int blocks = std::min(grid, (b.nitems + WPB - 1) / WPB);
   if (blocks <= 0) return NBK_OK;

@@ -51,6 +51,11 @@ struct DevAlloc {
 };
 int dev_malloc(void** p, size_t bytes, cudaStream_t st);
 void dev_free(void* p, cudaStream_t st);
+// Raise a kernel's dynamic shared-memory limit to `bytes` on the current device (once per
+// device and kernel; the attribute is per device).
+int ensure_dyn_smem(const void* func, int bytes);
+// Test hook behind nbk_debug_set_iteration_cap (fof.cu).
+int set_uf_iteration_cap(int cap);
 
 int64_t heap_slots(int64_t n, int b);
 int64_t count_nodes(int64_t n, int b);

@@ -16,13 +16,20 @@
 // The local-metric search (the reference's default, Aniso = 0) scales the distance at the
 // leaves by a per-query metric but prunes with the unscaled incremental offset, so its
 // result is not the exact nearest-neighbour set and depends on the order in which the
-// tree is walked. Each query is therefore one thread that walks the tree in exactly the
-// reference's depth-first order (nearer child first; the farther child opened when the
-// FP64 offset sum, rounded as the reference rounds it, is below the heap top at that
-// moment) with the same bounded max-heap, which reproduces the reference's neighbour
-// sets. The walk is stackless over the heap-indexed nodes (the parent of h is (h-1)/2);
-// per depth it keeps the offset sum and the overwritten offset. The plain phase-space
-// search (Aniso = -1) is exact and runs through the same walk.
+// tree is walked. Two work mappings give the reference's answer:
+//  - warp-cooperative exact search: one warp walks the tree once for 32 consecutive
+//    queries (a node is opened when any lane still needs it) and every lane tests the
+//    opened leaves against its own query. This is the plain phase distance (Aniso = -1),
+//    which is exact, and every local-metric query whose metric weights are all at least
+//    1 + 1e-9: for those the reference's unscaled pruning never removes a particle of the
+//    final heap, so its result is the exact k nearest in the metric.
+//  - per-lane walk for the remaining local-metric queries: the lane walks the tree in
+//    exactly the reference's depth-first order (nearer child first; the farther child
+//    opened when the FP64 offset sum, rounded as the reference rounds it, is below the
+//    heap top at that moment) with the same bounded max-heap, which reproduces the
+//    reference's neighbour sets. The walk is stackless over the heap-indexed nodes (the
+//    parent of h is (h-1)/2); per depth it keeps the offset sum and the overwritten
+//    offset.
 //
 // The walk skips every subtree whose particles provably cannot enter the heap: when the
 // FP32 distance bound of its bounding box (box_lb6f, in the query's own metric, rounded
@@ -538,12 +545,7 @@ template <int KMAX>
 int launch_phase_t(const PhaseArgs& pa, cudaStream_t st) {
   constexpr int WPB = ph_warps_per_block<KMAX>();
   size_t sm = sizeof(PhWarp<KMAX>) * WPB;
-  static bool attr_set = false;
-  if (!attr_set) {
-    NBK_CUDA_TRY(cudaFuncSetAttribute(k_phase<KMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)sm));
-    attr_set = true;
-  }
+  NBK_TRY(ensure_dyn_smem((const void*)k_phase<KMAX>, (int)sm));
   unsigned warps = (unsigned)((pa.k.nq + 31) / 32);
   k_phase<KMAX><<<(warps + WPB - 1) / WPB, 32 * WPB, sm, st>>>(pa);
   note_launch();

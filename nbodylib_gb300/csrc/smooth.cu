@@ -219,12 +219,7 @@ template <int KMAX, int SM>
 int launch_st(const SmoothArgs& s, cudaStream_t st) {
   constexpr int WPB = warps_per_block<KMAX>();
   size_t sm = sizeof(WarpSmem<KMAX>) * WPB;
-  static bool set = false;
-  if (!set) {
-    NBK_CUDA_TRY(cudaFuncSetAttribute(k_smooth<KMAX, SM>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    set = true;
-  }
+  NBK_TRY(ensure_dyn_smem((const void*)k_smooth<KMAX, SM>, (int)sm));
   int blocks = ((s.k.nq + 31) / 32 + WPB - 1) / WPB;
   if (blocks == 0) return NBK_OK;
   Phase ph("smooth", st);

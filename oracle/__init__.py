@@ -21,7 +21,21 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libnbport.so")
 REF_SO = os.path.join(HERE, "_ref", "libnbref.so")
-DEFAULT_REF_SRC = "/root/reference"
+
+
+def ref_src() -> str:
+    """The reference checkout the "ref" backend compiles from: NBKDT_REF_SRC if set, else
+    the REF default of oracle/Makefile (the build recipe is the one place that names it)."""
+    env = os.environ.get("NBKDT_REF_SRC")
+    if env:
+        return env
+    r = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True)
+    return r.stdout.strip()
+
+
+def ref_present(src: str | None = None) -> bool:
+    src = src or ref_src()
+    return bool(src) and os.path.isdir(os.path.join(src, "src", "KDTree"))
 
 _c_int_p = ctypes.POINTER(ctypes.c_int)
 _c_dbl_p = ctypes.POINTER(ctypes.c_double)
@@ -30,8 +44,8 @@ _c_dbl_p = ctypes.POINTER(ctypes.c_double)
 def build(ref: bool = False, ref_src: str | None = None) -> None:
     """Compile the restatement (always) and the reference (if its sources exist)."""
     subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
-    src = ref_src or os.environ.get("NBKDT_REF_SRC", DEFAULT_REF_SRC)
-    if ref and os.path.isdir(os.path.join(src, "src", "KDTree")):
+    src = ref_src or globals()["ref_src"]()
+    if ref and ref_present(src):
         subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", f"REF={src}"], check=True)
 
 

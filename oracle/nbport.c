@@ -8,7 +8,7 @@
  * Makefile compiles with -ffp-contract=off, so distances, box offsets and kernel weights
  * round exactly as the reference's do. The quickselect median partition is restated
  * swap for swap, so the particle permutation (tree order) equals the reference's, which
- * tests/test_oracle_port.py checks against the compiled reference.
+ * tests/test_oracle.py checks against the compiled reference.
  *
  * Paths are relative to the reference checkout (pelahi/NBodylib).
  */

@@ -2,7 +2,7 @@
  * Test infrastructure only. C restatement of the reference NBodylib KDTree hot path
  * (src/KDTree/), used as the CPU checker by tests/ and as the CPU baseline by bench.py.
  * It is never linked into the product library. Parity of this restatement is pinned
- * against the reference itself (oracle/_ref/libnbref.so) by tests/test_oracle_port.py
+ * against the reference itself (oracle/_ref/libnbref.so) by tests/test_oracle.py
  * and against the committed golden fixtures in tests/golden/.
  *
  * Indices: every neighbour list and every per-particle output is in input order ("ID"

@@ -23,8 +23,8 @@ def port_built():
 def ref_built():
     """The reference compiled from its own sources; only where its checkout exists."""
     import oracle
-    src = os.environ.get("NBKDT_REF_SRC", oracle.DEFAULT_REF_SRC)
-    if not os.path.isdir(os.path.join(src, "src", "KDTree")):
+    src = oracle.ref_src()
+    if not oracle.ref_present(src):
         pytest.skip("reference checkout not present on this machine")
     oracle.build(ref=True, ref_src=src)
     return True

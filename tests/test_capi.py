@@ -1,8 +1,11 @@
-"""CPU tests of the boundary: libnbkdt.so builds for sm_103a, loads, and exports every
-entry point include/nbkdt.h declares (no compute calls: there may be no GPU)."""
+"""Tests of the boundary: libnbkdt.so builds for sm_103a, loads, and exports every entry
+point include/nbkdt.h declares (CPU, no compute calls); on a GPU, the runtime runs its
+kernels from sm_103a code."""
 import ctypes
 import os
 import re
+
+import pytest
 
 from nbodylib_gb300 import _build, _capi
 
@@ -30,6 +33,11 @@ def test_library_builds_loads_and_exports_every_symbol(lib_built):
     assert set(declared_functions()) <= set(_capi.SIGNATURES)
 
 
-def test_library_is_sm103a():
-    # the build passes exactly one target, compute_103a -> sm_103a
-    assert _build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+@pytest.mark.gpu
+def test_library_kernels_run_as_sm103a(gpu):
+    # what the CUDA runtime selected for a product kernel on this GPU: SASS for sm_103a
+    # and PTX of the same target (cudaFuncGetAttributes through the library itself)
+    lib = _capi.load()
+    b, p = ctypes.c_int(), ctypes.c_int()
+    _capi.check(lib.nbk_kernel_binary_version(ctypes.byref(b), ctypes.byref(p)))
+    assert (b.value, p.value) == (103, 103)

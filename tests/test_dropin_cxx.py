@@ -27,7 +27,7 @@ def compile_demo(out, include_nbody, link=True):
 
 
 def test_compiles_against_the_reference_headers(lib_built, tmp_path):
-    ref = os.environ.get("NBKDT_REF_SRC", oracle.DEFAULT_REF_SRC)
+    ref = oracle.ref_src()
     if not os.path.isdir(os.path.join(ref, "src", "NBody")):
         pytest.skip("reference checkout not present on this machine")
     inc = [os.path.join(ROOT, "oracle", "gslshim"), os.path.join(ref, "src", "NBody"),
@@ -40,7 +40,7 @@ def test_reference_density_smooth_compiles_unmodified(lib_built, tmp_path):
     """The reference's own in-repo caller, src/Analysis/Density.cxx (DensitySmooth:
     KDTree(S, b) + CalcDensity), compiles unmodified against the drop-in through
     include/compat/KDTree.h placed ahead of the reference's KDTree headers."""
-    ref = os.environ.get("NBKDT_REF_SRC", oracle.DEFAULT_REF_SRC)
+    ref = oracle.ref_src()
     src = os.path.join(ref, "src", "Analysis", "Density.cxx")
     if not os.path.exists(src):
         pytest.skip("reference checkout not present on this machine")
