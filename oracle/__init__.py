@@ -106,6 +106,9 @@ def _lib(backend: str) -> ctypes.CDLL:
         sig["knn_pos"] = (ctypes.c_int, [vp, _c_dbl_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          _c_int_p, _c_dbl_p])
         sig["density"] = (ctypes.c_int, [vp, ctypes.c_int, _c_dbl_p, _c_int_p])
+        sig["density_parallel"] = (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, _c_dbl_p])
+        sig["veldensity_parallel"] = (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int,
+                                                     ctypes.c_int, _c_dbl_p])
         sig["kernel_table"] = (None, [vp, _c_dbl_p])
         sig["density_adjoint"] = (ctypes.c_int, [vp, ctypes.c_int, _c_int_p, _c_dbl_p, _c_dbl_p,
                                                  _c_dbl_p, _c_dbl_p, _c_dbl_p, _c_dbl_p])
@@ -292,6 +295,23 @@ class OracleTree:
     def veldensity(self, nsmooth, nsearch):
         out = np.empty(self.n, np.float64)
         self._f("veldensity")(self._h, nsmooth, nsearch, _dp(out))
+        return out
+
+    def density_parallel(self, k, nthreads=0):
+        """CalcDensity(k) with the searches over OpenMP threads (port only): each
+        density differs from density()'s by the summation order of its terms."""
+        rho = np.empty(self.n, np.float64)
+        st = self._f("density_parallel")(self._h, k, nthreads, _dp(rho))
+        if st:
+            raise RuntimeError(f"CalcDensity (parallel): status {st}")
+        return rho
+
+    def veldensity_parallel(self, nsmooth, nsearch, nthreads=0):
+        """CalcVelDensity over OpenMP threads (port only): bit-identical to veldensity()."""
+        out = np.empty(self.n, np.float64)
+        st = self._f("veldensity_parallel")(self._h, nsmooth, nsearch, nthreads, _dp(out))
+        if st:
+            raise RuntimeError(f"CalcVelDensity (parallel): status {st}")
         return out
 
     def density_particle(self, pid, k):

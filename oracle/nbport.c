@@ -887,6 +887,94 @@ int pt_veldensity(PTree* t, int nsmooth, int nsearch, double* out) {
     return status;
 }
 
+/* pt_density with the per-particle searches spread over OpenMP threads, for checking
+   large particle sets in reasonable time (the reference's CalcDensity is a serial loop).
+   Each particle's search, smoothing length and weights are exactly those of pt_density;
+   the symmetric scatter goes to one accumulator per thread (static schedule), summed at
+   the end, so a density differs from pt_density's only by the order in which its
+   non-negative terms are added (a few ulps). Physical and velocity trees only. */
+int pt_density_parallel(PTree* t, int k, int nthreads, double* rho) {
+    int n = t->n;
+    if (t->treetype == TPHS) return 7;
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+    int nt = omp_get_max_threads();
+    double* acc = (double*)calloc((size_t)nt * n, sizeof(double));
+    if (!acc) return 8;
+    int nd = t->nd;
+    double delta = 2.0 / (double)(t->kernres - 1);
+    int status = 0;
+#pragma omp parallel
+    {
+        PQ pq;
+        pq_init(&pq, k);
+        double* my = acc + (size_t)omp_get_thread_num() * n;
+#pragma omp for schedule(static, 256)
+        for (int i = 0; i < n; i++) {
+            pq.n = 0;
+            for (int j = 0; j < k; j++) pq_push(&pq, -1, MAXVALUE);
+            double scale;
+            density_search(t, &pq, i, &scale);
+            double hi = 0.5 * sqrt(pq_top(&pq));
+            double norm = 1.0 / pow(hi, (double)(nd * 1.));
+            for (int j = 0; j < k; j++) {
+                if (pq_topq(&pq) == -1) {
+#pragma omp atomic write
+                    status = 6;
+                    break;
+                }
+                double rij = sqrt(pq_top(&pq));
+                double wij = 0.5 *
+                             wsm(rij / hi, (int)(rij / hi * 0.5 * (t->kernres - 1)), t->kernres,
+                                 delta, t->kernel) *
+                             norm;
+                int id = pq_topq(&pq);
+                my[i] += wij * t->p[id].mass;
+                my[id] += wij * t->p[i].mass;
+                pq_pop(&pq);
+            }
+        }
+        pq_free(&pq);
+#pragma omp for schedule(static)
+        for (int i = 0; i < n; i++) {
+            double s = 0;
+            for (int th = 0; th < nt; th++) s += acc[(size_t)th * n + i];
+            rho[t->p[i].id] = s;
+        }
+    }
+    free(acc);
+    return status;
+}
+
+/* pt_veldensity with the particles spread over OpenMP threads: every value is a gather
+   over the particle's own neighbours, so the results are bit-identical to pt_veldensity. */
+int pt_veldensity_parallel(PTree* t, int nsmooth, int nsearch, int nthreads, double* out) {
+    if (nsmooth > nsearch) nsmooth = nsearch;
+    int n = t->n;
+    int status = 0;
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel
+    {
+        PQ pq, pq2;
+        pq_init(&pq, nsearch);
+        pq_init(&pq2, nsmooth);
+        int* nnids = (int*)malloc(sizeof(int) * nsearch);
+        double* vdist = (double*)malloc(sizeof(double) * nsearch);
+        int st = 0;
+#pragma omp for schedule(dynamic, 256)
+        for (int i = 0; i < n; i++)
+            out[t->p[i].id] = veldensity_one(t, i, nsmooth, nsearch, &pq, &pq2, nnids, vdist, &st);
+        if (st) {
+#pragma omp atomic write
+            status = st;
+        }
+        free(nnids);
+        free(vdist);
+        pq_free(&pq);
+        pq_free(&pq2);
+    }
+    return status;
+}
+
 /* KDTree::CalcDensityParticle (KDCalcSmoothQuantities.cxx:768-843): gather only,
    no 0.5 factor, no scatter. */
 double pt_density_particle(PTree* t, int id, int k) {

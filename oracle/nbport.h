@@ -45,6 +45,11 @@ int pt_knn_coord(PTree* t, const double* x, int nq, int k, int nthreads, int* nn
    pops them) so that tests can freeze them for the adjoint. */
 int pt_density(PTree* t, int k, double* rho, int* nn_ids);
 int pt_veldensity(PTree* t, int nsmooth, int nsearch, double* out);
+/* The same two over OpenMP threads (physical and velocity trees): the parallel density
+   sums each particle's terms in another order (within a few ulps of pt_density); the
+   velocity density is bit-identical to pt_veldensity. Status 7 for phase-space trees. */
+int pt_density_parallel(PTree* t, int k, int nthreads, double* rho);
+int pt_veldensity_parallel(PTree* t, int nsmooth, int nsearch, int nthreads, double* out);
 double pt_density_particle(PTree* t, int id, int k);
 double pt_veldensity_particle(PTree* t, int id, int nsmooth, int nsearch);
 double pt_density_position(PTree* t, const double* x, int k);

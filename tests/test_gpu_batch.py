@@ -1,6 +1,9 @@
 """GPU batched path: many per-group trees, one persistent density launch (optionally a
 replayed CUDA graph), autotuned leaf / query-bucket sizes; checked per group against the
 oracle's KDTree(group) + CalcDensity(min(k, n-1)) and against the per-tree loop."""
+import concurrent.futures as cf
+import os
+
 import numpy as np
 import pytest
 
@@ -12,12 +15,27 @@ from tests.helpers import assert_density_close
 pytestmark = pytest.mark.gpu
 
 
-def reference_batch(pos, mass, off, k, b):
+def reference_batch(pos, mass, off, k, b, threads=1):
+    """The reference's per-group pattern on the restatement: KDTree(group) +
+    CalcDensity(min(k, n - 1)) for every group (groups spread over host threads)."""
     rho = np.empty(len(mass))
-    for g in range(len(off) - 1):
-        s, e = off[g], off[g + 1]
-        t = oracle.OracleTree(pos[s:e], None, mass[s:e], b, 0, 0, 1000, None, backend="port")
+
+    def one(g):
+        s, e = int(off[g]), int(off[g + 1])
+        if e - s < 2:
+            rho[s:e] = 0.0
+            return
+        t = oracle.OracleTree(pos[s:e], None, mass[s:e], b, 0, 0, 1000, None, backend="port",
+                              nthreads=1)
         rho[s:e] = t.density(min(k, e - s - 1))
+        t.close()
+
+    if threads <= 1:
+        for g in range(len(off) - 1):
+            one(g)
+    else:
+        with cf.ThreadPoolExecutor(threads) as ex:
+            list(ex.map(one, range(len(off) - 1)))
     return rho
 
 
@@ -65,3 +83,23 @@ def test_batched_large_groups(gpu, port_built):
     want = reference_batch(pos, mass, off, 32, 16)
     B = BatchedDensity(pos, mass, off, bucket_size=16)
     assert_density_close(B.density(32), want, "large groups")
+
+
+def test_batched_density_full_powerlaw_batch(gpu, port_built):
+    """The benchmarked batch itself: 20,000 Plummer groups with sizes n^-2 on
+    [20, 200000] (3,657,291 particles), k = min(32, n - 1), every density against the
+    restatement's per-group KDTree + CalcDensity, through the replayed graph with the
+    plain leaf size and with the autotuned one, and through the per-tree loop."""
+    sizes = syn.group_sizes(20000, 20, 200000, seed=4)
+    pos, vel, mass, off = syn.plummer_groups(sizes, seed=4)
+    assert len(mass) == 3657291
+    want = reference_batch(pos, mass, off, 32, 16, threads=os.cpu_count() or 1)
+    for bucket in (16, 0):
+        B = BatchedDensity(pos, mass, off, bucket_size=bucket)
+        b, qb, _ = B.params()
+        for _ in range(2):
+            assert_density_close(B.density(32, use_graph=True), want,
+                                 f"full batch, b={b} qb={qb}, graph")
+        if bucket == 16:
+            assert_density_close(B.density_pertree_search(32), want, "full batch, per-tree")
+        B.close()

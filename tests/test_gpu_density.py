@@ -1,5 +1,7 @@
 """GPU parity: SPH density (CalcDensity), velocity density (CalcVelDensity) and the
 single-particle variants, within the stated 1e-12 relative tolerance."""
+import os
+
 import numpy as np
 import pytest
 
@@ -89,11 +91,13 @@ def test_density_full_size_sampled(gpu, port_built):
     assert np.all(rho > 0) and np.all(np.isfinite(rho))
 
 
-def test_256cubed_sampled(gpu, port_built):
+def test_256cubed_full_arrays(gpu, port_built):
     """The largest configuration, 256^3 = 16,777,216 clustered particles in L = 250 with
-    velocities, k = 64: FindNearest(x) at 1000 sampled particles' positions,
-    CalcDensityParticle(64) and CalcVelDensityParticle(64, 64) at the same particles
-    against the restatement, and a checksum of the full scatter density: with equal
+    velocities, k = 64, every particle: CalcDensity(64) and CalcVelDensity(64, 64) (the
+    separate calls the bench times, and the fused one-traversal form) element by element
+    against the restatement run over all host threads, <= 1e-12; FindNearest(x) at 1000
+    sampled particles' positions, CalcDensityParticle(64) and CalcVelDensityParticle(64,
+    64) at the same particles; and a checksum of the full scatter density: with equal
     masses, every pair's half-weight is added once at each end, so sum_i CalcDensity_i
     equals sum_i CalcDensityParticle_i."""
     from tests.helpers import assert_knn_equal, to_ids
@@ -115,8 +119,18 @@ def test_256cubed_sampled(gpu, port_built):
     got = t.CalcVelDensityParticle(inv[ids], 64, 64)
     want = np.array([o.veldensity_particle(int(i), 64, 64) for i in ids])
     assert_density_close(got, want, "CalcVelDensityParticle 256^3")
-    o.close()
     rho = np.asarray(t.CalcDensity(64))
+    vden = np.asarray(t.CalcVelDensity(64, 64))
+    threads = os.cpu_count() or 1
+    want_rho = o.density_parallel(64, nthreads=threads)
+    assert_density_close(rho, want_rho, "CalcDensity(64), all 256^3 particles")
+    want_v = o.veldensity_parallel(64, 64, nthreads=threads)
+    assert_density_close(vden, want_v, "CalcVelDensity(64, 64), all 256^3 particles")
+    rho2, vden2 = t.CalcDensityAndVelDensity(64, 64)
+    assert_density_close(np.asarray(rho2), want_rho, "fused CalcDensity(64), 256^3")
+    assert_density_close(np.asarray(vden2), want_v, "fused CalcVelDensity(64, 64), 256^3")
+    o.close()
+    del want_rho, want_v, rho2, vden2
     gather = np.asarray(t.CalcDensityParticle(np.arange(n, dtype=np.int32), 64))
     assert np.all(rho > 0) and np.all(np.isfinite(rho))
     assert abs(rho.sum() - gather.sum()) <= 1e-10 * gather.sum()

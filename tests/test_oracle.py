@@ -120,6 +120,21 @@ def test_port_matches_reference(ref_built, periodic):
         np.testing.assert_array_equal(ga, gb)
 
 
+def test_port_parallel_density_matches_serial(port_built):
+    # the threaded CalcDensity / CalcVelDensity used to check the 256^3 arrays: the
+    # density within a few ulps of the serial restatement (summation order only), the
+    # velocity density bit-identical
+    pos, mass, vel = syn.clustered_box(30000, 30.0, seed=9, velocities=True)
+    o = oracle.OracleTree(pos, vel, mass, 16, 0, 0, 1000, None, backend="port", nthreads=4)
+    rho = o.density(32)
+    rp = o.density_parallel(32, nthreads=4)
+    assert np.max(np.abs(rp - rho) / rho) <= 1e-14
+    v = o.veldensity(32, 64)
+    vp = o.veldensity_parallel(32, 64, nthreads=4)
+    assert np.array_equal(v, vp)
+    o.close()
+
+
 def test_adjoint_restatement_finite_differences(port_built):
     """The CPU adjoint (frozen neighbour lists and table cells) against central finite
     differences of the same frozen model."""
