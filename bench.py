@@ -504,8 +504,9 @@ def components(args, lib):
     loop_search_ms = _timed(lambda: B.density_pertree_search(32, out=rho), 2, flush, st)
     pertree_ms = _timed(lambda: B.density_pertree(32, out=rho), 1, flush, st)
     B.close()
-    Bt = BatchedDensity(dgp, dgm, doff, bucket_size=0, device=True)  # autotuned b, qb
-    bt, qbt, _ = Bt.params()
+    Bt = BatchedDensity(dgp, dgm, doff, bucket_size=0, device=True)  # autotuned b, qb, mapping
+    bt, qbt, tune = Bt.params()
+    wpqt = Bt.query_mapping()
     Bt.set_stream(st)
     Bt.density(32, use_graph=True, out=rho)
     graph_tuned_ms = _timed(lambda: Bt.density(32, use_graph=True, out=rho), reps, flush, st)
@@ -516,7 +517,9 @@ def components(args, lib):
                               "speedup": pertree_ms / bbs_ms},
         "search_only": {"batched_graph_ms": graph_ms, "pertree_loop_ms": loop_search_ms,
                         "speedup": loop_search_ms / graph_ms},
-        "autotuned": {"bucket": bt, "query_bucket": qbt, "batched_graph_ms": graph_tuned_ms},
+        "autotuned": {"bucket": bt, "query_bucket": qbt, "warp_per_query": wpqt,
+                      "batched_graph_ms": graph_tuned_ms,
+                      "table": json.loads(tune) if tune else None},
         "batched_queries_per_s": len(gm) / (graph_ms / 1e3),
         "target": "batched >= 5x the per-tree loop",
     }

@@ -423,10 +423,17 @@ int nbk_batch_density_pertree(nbk_batch* batch, int k, double* rho);
 /* The search half of the plain comparator: one kNN-density launch per group over the
    forest the batch already built, looping over groups on the host (no builds). */
 int nbk_batch_density_pertree_search(nbk_batch* batch, int k, double* rho);
-/* The leaf size and query-bucket size in use, and (when autotuned) the tuner's timings
-   as JSON in tune_json (NUL-terminated, up to cap bytes). (No reference counterpart.) */
+/* The leaf size and query-bucket size in use, and (when autotuned) the tuner's median
+   timings of every (leaf size, query bucket, query mapping) candidate as JSON in
+   tune_json (NUL-terminated, up to cap bytes). (No reference counterpart.) */
 int nbk_batch_get_params(const nbk_batch* batch, int32_t* bucket_size, int32_t* query_bucket,
                          char* tune_json, int64_t cap);
+/* How the batched search maps queries to warps: 1 (the default) a warp serves one query
+   at a time (its k-list spread over the lanes' registers), 0 a lane serves one query and
+   a warp 32 queries of a bucket. The autotuner chooses it with the leaf and bucket sizes.
+   (No reference counterpart.) */
+int nbk_batch_set_query_mapping(nbk_batch* batch, int warp_per_query);
+int nbk_batch_get_query_mapping(const nbk_batch* batch, int32_t* warp_per_query);
 
 #ifdef __cplusplus
 }

@@ -86,6 +86,8 @@ SIGNATURES = {
     "nbk_batch_density": (c_int, [c_vp, c_int, c_vp, c_int]),
     "nbk_batch_density_pertree": (c_int, [c_vp, c_int, c_vp]),
     "nbk_batch_density_pertree_search": (c_int, [c_vp, c_int, c_vp]),
+    "nbk_batch_set_query_mapping": (c_int, [c_vp, c_int]),
+    "nbk_batch_get_query_mapping": (c_int, [c_vp, c_i32p]),
     "nbk_batch_get_params": (c_int, [c_vp, c_i32p, c_i32p, ctypes.c_char_p, c_i64]),
 }
 

@@ -27,6 +27,7 @@ using namespace nbk;
 struct nbk_batch {
   int64_t ntot = 0, ngroups = 0;
   int b = 16, qb = 32;
+  int wpq = 1;  // query mapping: 1 a warp per query, 0 a lane per query (32 per warp)
   int kerntype = 0, kernres = 1000;
   unsigned flags = 0;
   cudaStream_t st = nullptr;
@@ -195,7 +196,7 @@ int density_sequence(nbk_batch* B, int k, double* out) {
   NBK_CUDA_TRY(cudaMemsetAsync(B->d_rho_tree, 0, sizeof(double) * B->ntot, B->st));
   NBK_CUDA_TRY(cudaMemsetAsync(B->d_counter, 0, sizeof(int), B->st));
   KnnArgs a = batch_args(B, k);
-  BatchArgs ba{B->d_items, B->d_trees, B->nitems, B->d_counter};
+  BatchArgs ba{B->d_items, B->d_trees, B->nitems, B->d_counter, B->wpq};
   NBK_TRY(launch_knn_batch(a, ba, B->st));
   NBK_TRY(scatter_to_input_order(B->d_rho_tree, B->arr.perm, out, B->ntot, 1, B->st));
   return NBK_OK;
@@ -203,7 +204,7 @@ int density_sequence(nbk_batch* B, int k, double* out) {
 
 int run_density(nbk_batch* B, int k, double* out, int use_graph) {
   if (!use_graph) return density_sequence(B, k, out);
-  auto key = std::make_pair(k, out);
+  auto key = std::make_pair(k * 2 + B->wpq, out);
   auto it = B->graphs.find(key);
   if (it == B->graphs.end()) {
     // first use outside capture sets kernel attributes and sizes the persistent grid
@@ -243,51 +244,78 @@ float elapsed_ms(cudaEvent_t a, cudaEvent_t b) {
   return ms;
 }
 
-// Autotuner: leaf size b and query-bucket size qb minimising build + batched search for
-// the caller's groups with k = 32 (the density workload's k).
+struct EventPair {
+  cudaEvent_t a = nullptr, b = nullptr;
+  EventPair() {
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+  }
+  ~EventPair() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+};
+
+float median3(float x, float y, float z) {
+  return std::max(std::min(x, y), std::min(std::max(x, y), z));
+}
+
+// Autotuner: leaf size b, query-bucket size qb and the query mapping (a warp per query,
+// or a lane per query with 32 queries per warp) minimising build + batched search for the
+// caller's groups with k = 32 (the density workload's k). Every candidate is timed three
+// times after a warm-up run and scored by the medians.
 int autotune(nbk_batch* B) {
   const int bs[] = {8, 12, 16, 24, 32};
   const int qbs[] = {16, 32};
-  cudaEvent_t e0, e1, e2;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  cudaEventCreate(&e2);
+  const int wpqs[] = {1, 0};
+  EventPair ev;
   double best = 1e30;
-  int bb = 16, bq = 32;
+  int bb = 16, bq = 32, bw = 1;
   std::string rep = "{";
   for (int b : bs) {
     B->qb = 32;
-    cudaEventRecord(e0, B->st);
-    NBK_TRY(batch_build(B, b));
-    cudaEventRecord(e1, B->st);
-    float build_ms = elapsed_ms(e0, e1);
+    float tb[3];
+    for (int r = 0; r < 3; r++) {
+      cudaEventRecord(ev.a, B->st);
+      NBK_TRY(batch_build(B, b));
+      cudaEventRecord(ev.b, B->st);
+      tb[r] = elapsed_ms(ev.a, ev.b);
+    }
+    float build_ms = median3(tb[0], tb[1], tb[2]);
     for (int qb : qbs) {
       NBK_TRY(make_items(B, qb));
-      NBK_TRY(density_sequence(B, 32, B->d_rho_out));  // warm
-      cudaEventRecord(e1, B->st);
-      NBK_TRY(density_sequence(B, 32, B->d_rho_out));
-      cudaEventRecord(e2, B->st);
-      float dens_ms = elapsed_ms(e1, e2);
-      double score = build_ms + dens_ms;
-      char tmp[160];
-      snprintf(tmp, sizeof(tmp), "%s\"b%d_qb%d\": [%.4f, %.4f]", rep.size() > 1 ? ", " : "", b, qb,
-               build_ms, dens_ms);
-      rep += tmp;
-      if (score < best) {
-        best = score;
-        bb = b;
-        bq = qb;
+      for (int wpq : wpqs) {
+        B->wpq = wpq;
+        NBK_TRY(density_sequence(B, 32, B->d_rho_out));  // warm
+        float td[3];
+        for (int r = 0; r < 3; r++) {
+          cudaEventRecord(ev.a, B->st);
+          NBK_TRY(density_sequence(B, 32, B->d_rho_out));
+          cudaEventRecord(ev.b, B->st);
+          td[r] = elapsed_ms(ev.a, ev.b);
+        }
+        float dens_ms = median3(td[0], td[1], td[2]);
+        double score = build_ms + dens_ms;
+        char tmp[160];
+        snprintf(tmp, sizeof(tmp), "%s\"b%d_qb%d_wpq%d\": [%.4f, %.4f]",
+                 rep.size() > 1 ? ", " : "", b, qb, wpq, build_ms, dens_ms);
+        rep += tmp;
+        if (score < best) {
+          best = score;
+          bb = b;
+          bq = qb;
+          bw = wpq;
+        }
       }
     }
   }
   rep += "}";
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  cudaEventDestroy(e2);
   NBK_TRY(check_batch_err(B));
   B->tune = "{\"chosen\": {\"b\": " + std::to_string(bb) + ", \"qb\": " + std::to_string(bq) +
-            "}, \"ms_build_search\": " + rep + "}";
+            ", \"warp_per_query\": " + std::to_string(bw) +
+            "}, \"runs_per_candidate\": 3, \"median_ms_build_search\": " + rep + "}";
   B->qb = bq;
+  B->wpq = bw;
   return batch_build(B, bb);
 }
 
@@ -436,6 +464,24 @@ int nbk_batch_get_params(const nbk_batch* B, int32_t* bucket_size, int32_t* quer
     memcpy(tune_json, B->tune.data(), m);
     tune_json[m] = 0;
   }
+  return NBK_OK;
+}
+
+int nbk_batch_set_query_mapping(nbk_batch* B, int warp_per_query) {
+  if (!B || (warp_per_query != 0 && warp_per_query != 1)) {
+    set_error("nbk_batch_set_query_mapping: null batch or mapping other than 0 / 1");
+    return NBK_ERR_INVALID;
+  }
+  B->wpq = warp_per_query;
+  return NBK_OK;
+}
+
+int nbk_batch_get_query_mapping(const nbk_batch* B, int32_t* warp_per_query) {
+  if (!B || !warp_per_query) {
+    set_error("nbk_batch_get_query_mapping: null argument");
+    return NBK_ERR_INVALID;
+  }
+  *warp_per_query = B->wpq;
   return NBK_OK;
 }
 

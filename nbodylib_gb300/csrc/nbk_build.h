@@ -158,7 +158,8 @@ struct BatchArgs {
   const WorkItem* items;
   const TreeInfo* trees;
   int nitems;
-  int* counter;  // zeroed before each launch
+  int* counter;         // zeroed before each launch
+  int warp_per_query;   // 1: a warp serves one query at a time; 0: a lane per query
 };
 // Density of every particle of every tree (a.kheap = k, clamped per tree to n-1).
 int launch_knn_batch(const KnnArgs& a, const BatchArgs& b, cudaStream_t st);

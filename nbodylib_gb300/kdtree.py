@@ -522,6 +522,15 @@ class BatchedDensity:
                                                    buf, len(buf)))
         return b.value, q.value, buf.value.decode()
 
+    def query_mapping(self):
+        """1: a warp serves one query at a time; 0: a lane per query (32 per warp)."""
+        w = ctypes.c_int32()
+        _capi.check(self._lib.nbk_batch_get_query_mapping(self._h, ctypes.byref(w)))
+        return w.value
+
+    def set_query_mapping(self, warp_per_query):
+        _capi.check(self._lib.nbk_batch_set_query_mapping(self._h, int(warp_per_query)))
+
     def _out(self):
         if self.device:
             return self._torch.empty(self.n, dtype=self._torch.float64, device="cuda")

@@ -2,6 +2,7 @@
 replayed CUDA graph), autotuned leaf / query-bucket sizes; checked per group against the
 oracle's KDTree(group) + CalcDensity(min(k, n-1)) and against the per-tree loop."""
 import concurrent.futures as cf
+import json
 import os
 
 import numpy as np
@@ -49,8 +50,15 @@ def test_batched_density_vs_oracle(gpu, port_built, bucket):
     b, qb, tune = B.params()
     if bucket == 0:
         assert b in (8, 12, 16, 24, 32) and qb in (16, 32) and "chosen" in tune
-    for use_graph in (False, True, True):
-        assert_density_close(B.density(32, use_graph=use_graph), want, f"batched graph={use_graph}")
+        tune = json.loads(tune)
+        # every (leaf size, query bucket, query mapping) candidate was timed
+        assert len(tune["median_ms_build_search"]) == 5 * 2 * 2
+        assert tune["chosen"]["warp_per_query"] == B.query_mapping()
+    for wpq in (1, 0):
+        B.set_query_mapping(wpq)
+        for use_graph in (False, True, True):
+            assert_density_close(B.density(32, use_graph=use_graph), want,
+                                 f"batched graph={use_graph} warp_per_query={wpq}")
     assert_density_close(B.density_pertree(32), want, "per-tree loop")
     assert_density_close(B.density_pertree_search(32), want, "per-tree search loop")
     B.close()
