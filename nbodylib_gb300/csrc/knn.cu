@@ -305,8 +305,10 @@ __device__ void wq_run(const KnnArgs& a, const TreeView& tv, WqSmem& w, int lane
   }
 }
 
+// 64 registers per thread (4 blocks of 8 warps per SM): the occupancy outweighs the few
+// spills of the two- and four-slot lists (measured at 2^20 and 2^22 clustered particles)
 template <int S, int EPI>
-__global__ void k_knn_wq(KnnArgs a) {
+__global__ void __launch_bounds__(32 * kWqWpb, 4) k_knn_wq(KnnArgs a) {
   __shared__ WqSmem ws[kWqWpb];
   int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   int qi = blockIdx.x * kWqWpb + warp;
@@ -325,7 +327,7 @@ __global__ void k_knn_wq(KnnArgs a) {
 // Batched density, warp per query: the persistent grid's warps pull (tree, query bucket)
 // work items and serve the bucket's queries one after another.
 template <int S>
-__global__ void k_knn_batch_wq(KnnArgs a, BatchArgs b) {
+__global__ void __launch_bounds__(32 * kWqWpb, 4) k_knn_batch_wq(KnnArgs a, BatchArgs b) {
   __shared__ WqSmem ws[kWqWpb];
   int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int guard = 0; guard < b.nitems + 1; guard++) {
