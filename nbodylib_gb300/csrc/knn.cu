@@ -192,12 +192,12 @@ constexpr int kWqWpb = 8;  // warps (queries) per block
 
 // One query's search and epilogue on one warp; `qi` indexes the per-query outputs and
 // `self` is the query's tree index. All lanes of the warp call this together.
-template <int S, int EPI>
+template <int S, int EPI, bool F32FIRST = false>
 __device__ void wq_run(const KnnArgs& a, const TreeView& tv, WqSmem& w, int lane, int qi,
                        int self, const double x0[3], int K) {
   const unsigned FULL = 0xffffffffu;
   WqQuery<S> Q;
-  wq_search<S>(Q, w, a, tv, lane, self, x0, K, a.exclude_self != 0);
+  wq_search<S, F32FIRST>(Q, w, a, tv, lane, self, x0, K, a.exclude_self != 0);
   const int kr = a.kernres;
   const double inv_delta = 0.5 * (double)(kr - 1);  // 1 / table step, exact
   if (EPI == kEpiNN) {
@@ -327,7 +327,8 @@ __global__ void __launch_bounds__(32 * kWqWpb, 4) k_knn_wq(KnnArgs a) {
 // Batched density, warp per query: the persistent grid's warps pull (tree, query bucket)
 // work items and serve the bucket's queries one after another.
 // 6 blocks per SM (42 registers): for the many small trees of a batch the occupancy pays
-// more than for one large tree (20,000 power-law groups: 17.98 ms against 20.59 ms at 4)
+// more than for one large tree (20,000 power-law groups: 17.98 ms against 20.59 ms at 4).
+// The batch's one-slot searches run FP32 first (knn_wq.cuh wq_search_f32: 16.2 ms)
 template <int S>
 __global__ void __launch_bounds__(32 * kWqWpb, 6) k_knn_batch_wq(KnnArgs a, BatchArgs b) {
   __shared__ WqSmem ws[kWqWpb];
@@ -349,7 +350,7 @@ __global__ void __launch_bounds__(32 * kWqWpb, 6) k_knn_batch_wq(KnnArgs a, Batc
       int self = ti.pstart + it.q0 + q;
       P4 p = tv.pos[self];
       double x0[3] = {p.x, p.y, p.z};
-      wq_run<S, kEpiDensity>(a, tv, ws[warp], lane, self, self, x0, K);
+      wq_run<S, kEpiDensity, true>(a, tv, ws[warp], lane, self, self, x0, K);
       __syncwarp();
     }
   }

@@ -28,7 +28,10 @@
 // with every lane busy. A candidate enters when d2 < the k-th distance (strict, as the
 // reference's `dist2 < pq->TopPriority()`); the FP32 screen uses a bound at or above the
 // k-th distance, the exact test the current k-th distance, so the result is the exact k
-// nearest.
+// nearest. The batched kernel's one-slot searches first run the whole search on FP32
+// bounds alone (wq_search_f32), then compute FP64 distances only for the particles within
+// the final FP32 bound of the k-th distance; for one large tree that extra FP32 work
+// costs more than the FP64 it saves, so the direct form above serves it.
 #pragma once
 #include "nbk_build.h"
 
@@ -39,9 +42,13 @@ constexpr int kWqStack = 192;      // frontier stack (node indices) per warp
 constexpr int kWqBatchLimit = 64;  // above this many entries the stack pops one at a time
 constexpr long long kWqSent = 0x7fffffffffffffffll;  // key beyond position k - 1
 
+constexpr int kWqBuf = 256;  // candidates kept per query by the FP32 search
+
 struct WqSmem {
   int stk[kWqStack];
-  int queue[64];  // candidates (tree indices) that passed the FP32 screen
+  int queue[64];        // candidates (tree indices) that passed the FP32 screen
+  int buf[kWqBuf];      // FP32 search: candidates whose lower bound was within the bound
+  unsigned blo[kWqBuf];  // and those lower bounds (FP32 bit patterns)
 };
 
 // The sorted k-list of one query: keys are the bit patterns of the non-negative squared
@@ -267,14 +274,111 @@ __device__ __forceinline__ void wq_range(WqQuery<S>& Q, WqSmem& w, const TreeVie
     wq_consider<S>(Q, w, tv, lane, c0 + lane < count, start + c0 + lane);
 }
 
+// ---- FP32 search (target queries, one-slot lists): the whole search runs on FP32
+// bounds only. An FP32 k-list keeps the K smallest upper bounds of the squared distance
+// (particles other than the query and provably at a non-zero distance), so its last
+// entry T bounds the k-th distance from above; every particle whose lower bound is at or
+// below the T of the moment is kept in a buffer. Afterwards only the kept particles with
+// a lower bound at or below the final T -- the k nearest and the few within the FP32
+// rounding of them -- get exact FP64 distances. Bit patterns of non-negative floats order
+// as their values; 0xffffffff marks an empty list position (above +inf).
+struct WqF32 {
+  unsigned fk;   // this lane's position of the FP32 k-list (one slot)
+  unsigned tb;   // bits of T, the list's entry K - 1
+  int bn;        // particles in the buffer
+  bool over;     // the buffer overflowed: the query takes the exact search instead
+};
+
+__device__ __forceinline__ void warp_sort_asc_u32(unsigned& k, int lane) {
+#pragma unroll
+  for (int size = 2; size <= 32; size <<= 1) {
+#pragma unroll
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      unsigned ok = __shfl_xor_sync(0xffffffffu, k, stride);
+      bool up = (lane & size) == 0;
+      bool lower = (lane & stride) == 0;
+      bool take = (lower == up) ? (ok < k) : (ok > k);
+      if (take) k = ok;
+    }
+  }
+}
+
+// FP32 screen of one candidate per lane (valid lanes only): keep it when its lower
+// bound is within T, and let its upper bound into the FP32 k-list.
+template <int S>
+__device__ __forceinline__ void wq32_consider(const WqQuery<S>& Q, WqF32& F, WqSmem& w,
+                                              const TreeView& tv, int lane, bool valid, int ti,
+                                              int self, int K) {
+  const unsigned FULL = 0xffffffffu;
+  unsigned lob = 0xffffffffu, hib = 0xffffffffu;
+  if (valid) {
+    float4 cf = tv.posf[ti];
+    float lo = pair_d2_lo(Q.qx, Q.qy, Q.qz, cf.x, cf.y, cf.z, Q.two_eps);
+    lob = __float_as_uint(lo);
+    if (lob <= F.tb && ti != self && lo > 0.f)
+      hib = __float_as_uint(pair_d2_hi(Q.qx, Q.qy, Q.qz, cf.x, cf.y, cf.z, Q.two_eps));
+  }
+  bool keep = valid && lob <= F.tb;
+  unsigned km = __ballot_sync(FULL, keep);
+  if (!km) return;
+  int nk = __popc(km);
+  if (F.bn + nk > kWqBuf) {
+    // drop kept particles that the bound has since excluded
+    int nb = 0;
+    for (int c0 = 0; c0 < F.bn; c0 += 32) {
+      int i = c0 + lane;
+      bool stay = i < F.bn && w.blo[i] <= F.tb;
+      int bi = stay ? w.buf[i] : 0;
+      unsigned bl = stay ? w.blo[i] : 0u;
+      unsigned sm = __ballot_sync(FULL, stay);
+      __syncwarp();
+      if (stay) {
+        int d = nb + __popc(sm & ((1u << lane) - 1u));
+        w.buf[d] = bi;
+        w.blo[d] = bl;
+      }
+      nb += __popc(sm);
+      __syncwarp();
+    }
+    F.bn = nb;
+    if (F.bn + nk > kWqBuf) {
+      F.over = true;
+      return;
+    }
+  }
+  if (keep) {
+    int d = F.bn + __popc(km & ((1u << lane) - 1u));
+    w.buf[d] = ti;
+    w.blo[d] = lob;
+  }
+  F.bn += nk;
+  __syncwarp();
+  // the list takes the batch's upper bounds below T (sorted, then merged)
+  if (__ballot_sync(FULL, hib < F.tb)) {
+    unsigned k = hib < F.tb ? hib : 0xffffffffu;
+    warp_sort_asc_u32(k, lane);
+    unsigned rk = __shfl_sync(FULL, k, 31 - lane);
+    unsigned m = rk < F.fk ? rk : F.fk;
+#pragma unroll
+    for (int stride = 16; stride > 0; stride >>= 1) {
+      unsigned o = __shfl_xor_sync(FULL, m, stride);
+      bool lower = (lane & stride) == 0;
+      if (lower ? (o < m) : (o > m)) m = o;
+    }
+    F.fk = lane < K ? m : 0xffffffffu;
+    F.tb = __shfl_sync(FULL, F.fk, K - 1);
+  }
+}
+
 // Frontier-parallel traversal of every node whose FP32 box bound is below the k-th
 // distance: the whole tree when `home` is -1, else the whole tree but the subtree at heap
 // index `home` (already searched), which is the union of the subtrees of the siblings of
 // home and of each of its ancestors: those are pushed at once, so the first step tests
 // them all together instead of descending from the root one level per step. Returns
 // false when the stack would overflow (the caller sets the error word).
-template <int S>
-__device__ bool wq_traverse(WqQuery<S>& Q, WqSmem& w, const TreeView& tv, int lane, int home) {
+template <int S, bool F32 = false>
+__device__ bool wq_traverse(WqQuery<S>& Q, WqSmem& w, const TreeView& tv, int lane, int home,
+                            WqF32* F = nullptr, int self = -1, int K = 0) {
   const unsigned FULL = 0xffffffffu;
   int sp = 0;
   if (home < 0) {
@@ -296,7 +400,8 @@ __device__ bool wq_traverse(WqQuery<S>& Q, WqSmem& w, const TreeView& tv, int la
     if (lane < m) {
       h = w.stk[sp - 1 - lane];
       r = tv.node[tv.nbase + h];
-      need = box_d2_lo(Q.qx, Q.qy, Q.qz, Q.eps, r) < Q.thr;
+      float blo = box_d2_lo(Q.qx, Q.qy, Q.qz, Q.eps, r);
+      need = F32 ? __float_as_uint(blo) <= F->tb : blo < Q.thr;
     }
     __syncwarp();
     sp -= m;
@@ -317,19 +422,27 @@ __device__ bool wq_traverse(WqQuery<S>& Q, WqSmem& w, const TreeView& tv, int la
       int l = __ffs(lm) - 1;
       int st = __shfl_sync(FULL, r.start, l), ct = __shfl_sync(FULL, r.count, l);
       if (fill > 0 && fill + ct > 32) {
-        wq_consider<S>(Q, w, tv, lane, lane < fill, my);
+        if (F32) wq32_consider<S>(Q, *F, w, tv, lane, lane < fill, my, self, K);
+        else wq_consider<S>(Q, w, tv, lane, lane < fill, my);
         fill = 0;
       }
       lm &= lm - 1;
       if (ct > 32) {
-        wq_range<S>(Q, w, tv, lane, st, ct);
+        for (int c0 = 0; c0 < ct; c0 += 32) {
+          if (F32) wq32_consider<S>(Q, *F, w, tv, lane, c0 + lane < ct, st + c0 + lane, self, K);
+          else wq_consider<S>(Q, w, tv, lane, c0 + lane < ct, st + c0 + lane);
+        }
         continue;
       }
       if (lane >= fill && lane < fill + ct) my = st + lane - fill;
       fill += ct;
     }
-    if (fill > 0) wq_consider<S>(Q, w, tv, lane, lane < fill, my);
+    if (fill > 0) {
+      if (F32) wq32_consider<S>(Q, *F, w, tv, lane, lane < fill, my, self, K);
+      else wq_consider<S>(Q, w, tv, lane, lane < fill, my);
+    }
     __syncwarp();
+    if (F32 && F->over) return true;  // the caller redoes the query exactly
   }
   return sp == 0;
 }
@@ -407,13 +520,69 @@ __device__ __forceinline__ float wq_home_bound(const WqQuery<S>& Q, const TreeVi
   return __uint_as_float(hi + 1u);  // strictly above: candidates test lo < thr
 }
 
+// Target search of a one-slot list (K <= 32) without periodic images: the FP32 search
+// of the whole tree (own subtree, then the siblings of it and of its ancestors), then
+// exact FP64 distances for the kept particles within the final bound. Returns false when
+// the buffer overflowed (the caller runs wq_search instead) or the stack would.
+template <int S>
+__device__ bool wq_search_f32(WqQuery<S>& Q, WqSmem& w, const TreeView& tv, int lane, int self,
+                              const double x0[3], int K) {
+  WqF32 F;
+  F.fk = 0xffffffffu;
+  F.tb = 0xffffffffu;
+  F.bn = 0;
+  F.over = false;
+  wq_set_point<S>(Q, tv, x0);
+  int hh, hs, hn;
+  wq_home(tv, self, K + 1, hh, hs, hn);
+  for (int c0 = 0; c0 < hn && !F.over; c0 += 32)
+    wq32_consider<S>(Q, F, w, tv, lane, c0 + lane < hn, hs + c0 + lane, self, K);
+  bool ok = F.over || hh == 0 || wq_traverse<S, true>(Q, w, tv, lane, hh, &F, self, K);
+  if (!ok || F.over) return false;
+  // exact phase
+  wq_init<S>(Q.L, lane, K);
+  Q.K = K;
+  Q.topk = __double_as_longlong(kMaxValue);
+  Q.thr = __uint_as_float(0x7f800000u);
+  Q.qn = 0;
+  Q.self = self;
+  const unsigned FULL = 0xffffffffu;
+  for (int c0 = 0; c0 < F.bn; c0 += 32) {
+    int i = c0 + lane;
+    bool sel = i < F.bn && w.blo[i] <= F.tb;
+    int ti = sel ? w.buf[i] : 0;
+    unsigned pm = __ballot_sync(FULL, sel);
+    if (!pm) continue;
+    if (sel) w.queue[Q.qn + __popc(pm & ((1u << lane) - 1u))] = ti;
+    Q.qn += __popc(pm);
+    __syncwarp();
+    if (Q.qn >= 32) {
+      wq_flush<S>(Q, w, tv, lane, 32);
+      __syncwarp();
+      int rest = Q.qn - 32;
+      int moved = lane < rest ? w.queue[32 + lane] : 0;
+      __syncwarp();
+      if (lane < rest) w.queue[lane] = moved;
+      Q.qn = rest;
+      __syncwarp();
+    }
+  }
+  wq_drain<S>(Q, w, tv, lane);
+  return true;
+}
+
 // The search of one target query (tree index `self`, position x0): the direct pass
 // (seeded with the query's own subtree) and, on a periodic tree, the image passes with
 // the reference's gates. exclude_self: the target search of the direct pass skips the
 // query and zero distances (KDLeafNode.cxx:19-21). On return Q.L holds the K nearest.
-template <int S>
+// F32FIRST: one-slot target searches without images take wq_search_f32 first (faster
+// for the many small trees of a batch; for one large tree the direct form is faster).
+template <int S, bool F32FIRST = false>
 __device__ void wq_search(WqQuery<S>& Q, WqSmem& w, const KnnArgs& a, const TreeView& tv,
                           int lane, int self, const double x0[3], int K, bool exclude_self) {
+  if (F32FIRST && S == 1 && exclude_self && !a.periodic &&
+      wq_search_f32<S>(Q, w, tv, lane, self, x0, K))
+    return;
   wq_init<S>(Q.L, lane, K);
   Q.K = K;
   Q.topk = __double_as_longlong(kMaxValue);
