@@ -307,9 +307,9 @@ struct nbk_tree {
   }
 };
 
-// Frees every device array a tree owns (null entries are skipped) and waits for the
-// stream; used by nbk_destroy and by a failed nbk_create.
-static void free_tree_arrays(nbk_tree* t) {
+// Frees every device array a tree owns (null entries are skipped; the frees are ordered on
+// the tree's stream); a failed nbk_create also waits for the stream.
+static void free_tree_arrays(nbk_tree* t, bool wait) {
   cudaStream_t st = t->st;
   BuiltArrays& A = t->arr;
   void* arrays[] = {A.pos, A.posf, A.vel, A.perm, A.node, A.nodex, A.nodes6, A.nodeb6,
@@ -317,7 +317,7 @@ static void free_tree_arrays(nbk_tree* t) {
   for (void* p : arrays) dev_free(p, st);
   A = BuiltArrays();
   t->d_err = nullptr;  // t->d_kernel belongs to the process-wide kernel cache
-  cudaStreamSynchronize(st);
+  if (wait) cudaStreamSynchronize(st);
 }
 
 #define API_BEGIN try {
@@ -372,10 +372,8 @@ struct Stage {
   }
 };
 
-int check_err(nbk_tree* t, const char* what) {
-  int h = 0;
-  NBK_CUDA_TRY(cudaMemcpyAsync(&h, t->d_err, sizeof(int), cudaMemcpyDeviceToHost, t->st));
-  NBK_CUDA_TRY(cudaStreamSynchronize(t->st));
+// Status for a device error word already read back.
+int err_status(int h, const char* what) {
   if (h == kErrTooFew) {
     set_error(std::string(what) + ": fewer than k neighbours were found for some particle");
     return NBK_ERR_TOO_FEW;
@@ -389,6 +387,31 @@ int check_err(nbk_tree* t, const char* what) {
     return NBK_ERR_DEVICE;
   }
   return NBK_OK;
+}
+
+int check_err(nbk_tree* t, const char* what) {
+  int h = 0;
+  NBK_CUDA_TRY(cudaMemcpyAsync(&h, t->d_err, sizeof(int), cudaMemcpyDeviceToHost, t->st));
+  NBK_CUDA_TRY(cudaStreamSynchronize(t->st));
+  return err_status(h, what);
+}
+
+// A few page-locked scalars per host thread, so that small device-to-host reads can be
+// queued without blocking and collected by one later synchronisation (null if the
+// page-locked allocation failed: callers then read synchronously).
+struct PinnedScalars {
+  int i[8];
+  double d[8];
+};
+PinnedScalars* pinned_scalars() {
+  static thread_local PinnedScalars* p = nullptr;
+  static thread_local bool tried = false;
+  if (!p && !tried) {
+    tried = true;
+    void* q = nullptr;
+    if (cudaMallocHost(&q, sizeof(PinnedScalars)) == cudaSuccess) p = (PinnedScalars*)q;
+  }
+  return p;
 }
 
 int clear_err(nbk_tree* t) {
@@ -579,7 +602,7 @@ int nbk_create(const double* pos, const double* vel, const double* mass, int64_t
   struct FreeOnFailure {
     nbk_tree* t;
     ~FreeOnFailure() {
-      if (t) free_tree_arrays(t);
+      if (t) free_tree_arrays(t, true);
     }
   } guard{t.get()};
   NBK_CUDA_TRY(cudaGetDevice(&t->device));
@@ -590,13 +613,10 @@ int nbk_create(const double* pos, const double* vel, const double* mass, int64_t
   t->kerntype = (kerntype >= NBK_KSPH && kerntype <= NBK_KTH) ? kerntype : NBK_KSPH;
   t->kernres = kernres < 100 ? 100 : kernres;  // KDTree.cxx:1145-1148
   t->flags = flags;
-  if (period) {
-    double per[3];
-    if (flags & NBK_DEVICE_PTRS) {
-      NBK_CUDA_TRY(cudaMemcpy(per, period, sizeof(per), cudaMemcpyDeviceToHost));
-    } else {
-      memcpy(per, period, sizeof(per));
-    }
+  // a device-resident period is read back with the build's own final synchronisation
+  // (queued into page-locked memory) and checked after it; a host one is checked now
+  PinnedScalars* ps = (period && (flags & NBK_DEVICE_PTRS)) ? pinned_scalars() : nullptr;
+  auto take_period = [&](const double* per) -> int {
     for (int d = 0; d < 3; d++) {
       if (!(per[d] > 0)) {
         set_error("nbk_create: period entries must be positive");
@@ -605,6 +625,21 @@ int nbk_create(const double* pos, const double* vel, const double* mass, int64_t
       t->period[d] = per[d];
     }
     t->periodic = true;
+    return NBK_OK;
+  };
+  if (period) {
+    if (flags & NBK_DEVICE_PTRS) {
+      if (ps) {
+        NBK_CUDA_TRY(cudaMemcpyAsync(ps->d, period, sizeof(double) * 3, cudaMemcpyDeviceToHost,
+                                     t->st));
+      } else {
+        double per[3];
+        NBK_CUDA_TRY(cudaMemcpy(per, period, sizeof(per), cudaMemcpyDeviceToHost));
+        NBK_TRY(take_period(per));
+      }
+    } else {
+      NBK_TRY(take_period(period));
+    }
   }
   t->has_vel = vel != nullptr;
   cudaStream_t st = t->st;
@@ -689,6 +724,7 @@ int nbk_create(const double* pos, const double* vel, const double* mass, int64_t
       rhi[d] = root.hi[d];
     }
   }
+  if (ps) NBK_TRY(take_period(ps->d));  // the build has synchronised the stream
   // FP32 rounding bound for coordinates and image coordinates
   double maxabs = 0;
   for (int d = 0; d < 3; d++)
@@ -704,7 +740,7 @@ int nbk_create(const double* pos, const double* vel, const double* mass, int64_t
 
 int nbk_destroy(nbk_tree* t) {
   if (!t) return NBK_OK;
-  free_tree_arrays(t);
+  free_tree_arrays(t, false);
   delete t;
   return NBK_OK;
 }
@@ -1557,13 +1593,23 @@ int nbk_fof(nbk_tree* t, double fdist, int32_t minnum, int order, int32_t* group
   a.parent = parent;
   a.err = t->d_err;
   int ng = 0;
-  NBK_TRY(run_fof(a, (int)t->nslots, minnum, order, gtree, &ng, S.alloc, t->st));
+  // the group count and the error word come back together, in one synchronisation
+  PinnedScalars* ps = order == 0 ? pinned_scalars() : nullptr;
+  NBK_TRY(run_fof(a, (int)t->nslots, minnum, order, gtree, ps ? &ps->i[0] : &ng, S.alloc, t->st,
+                  ps != nullptr));
   if (t->n > 0) {
     k_scatter_i<<<(unsigned)((t->n + 255) / 256), 256, 0, t->st>>>(gtree, t->arr.perm, dg, t->n); note_launch();
     NBK_CUDA_TRY(cudaGetLastError());
   }
   NBK_TRY(S.finish());
-  NBK_TRY(check_err(t, "nbk_fof"));
+  if (ps) {
+    NBK_CUDA_TRY(cudaMemcpyAsync(&ps->i[1], t->d_err, sizeof(int), cudaMemcpyDeviceToHost, t->st));
+    NBK_CUDA_TRY(cudaStreamSynchronize(t->st));
+    NBK_TRY(err_status(ps->i[1], "nbk_fof"));
+    ng = ps->i[0];
+  } else {
+    NBK_TRY(check_err(t, "nbk_fof"));
+  }
   *ngroup = ng;
   return NBK_OK;
   API_END

@@ -983,7 +983,7 @@ static int link_fof6d_phase_tree(const FofArgs& a, DevAlloc& alloc, cudaStream_t
 }
 
 int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tree,
-            int* h_ngroup, DevAlloc& alloc, cudaStream_t st) {
+            int* h_ngroup, DevAlloc& alloc, cudaStream_t st, bool defer_count) {
   (void)nnodes;
   int n = a.tv.n;
   if (n == 0) {
@@ -1042,6 +1042,11 @@ int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tr
   k_scan_add<<<nb, 1024, 0, st>>>(lbl, bsum, n); note_launch();
   k_label<<<(n + 255) / 256, 256, 0, st>>>(a.parent, flag, lbl, n, d_group_tree); note_launch();
   NBK_CUDA_TRY(cudaGetLastError());
+  if (defer_count && !order) {
+    // the caller's page-locked h_ngroup is read after the caller's own synchronisation
+    NBK_CUDA_TRY(cudaMemcpyAsync(h_ngroup, d_total, sizeof(int), cudaMemcpyDeviceToHost, st));
+    return NBK_OK;
+  }
   int total = 0;
   NBK_CUDA_TRY(cudaMemcpyAsync(&total, d_total, sizeof(int), cudaMemcpyDeviceToHost, st));
   NBK_CUDA_TRY(cudaStreamSynchronize(st));

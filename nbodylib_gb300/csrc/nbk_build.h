@@ -183,7 +183,8 @@ struct FofArgs {
                        //   distance^2), so reachability follows from the comparator
 };
 int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tree,
-            int* h_ngroup, DevAlloc& alloc, cudaStream_t st);
+            int* h_ngroup, DevAlloc& alloc, cudaStream_t st,
+            bool defer_count = false);
 
 int run_ball(const TreeView& tv, int qmode, const int* qidx, const double* qx, int nq,
              double fdist2, int exclude_self, int64_t* d_offsets, int* d_out,
