@@ -22,6 +22,24 @@ FOF3D, FOFVEL, FOF6D = 0, 1, 2
 DEVICE_PTRS = 1
 
 
+# device copies of periods, by (values, device): a tree built from device arrays passes its
+# period as a device pointer, and a new 24-byte host-to-device copy per tree (blocking the
+# host) would cost more than the call's own set-up
+_DEVICE_PERIODS: dict = {}
+
+
+def _device_period(torch, period, device):
+    vals = tuple(float(x) for x in np.broadcast_to(np.asarray(period, np.float64), (3,)))
+    key = (vals, str(device))
+    t = _DEVICE_PERIODS.get(key)
+    if t is None:
+        if len(_DEVICE_PERIODS) > 64:
+            _DEVICE_PERIODS.clear()
+        t = torch.tensor(vals, dtype=torch.float64, device=device)
+        _DEVICE_PERIODS[key] = t
+    return t
+
+
 def _ptr(a):
     if a is None:
         return None
@@ -44,8 +62,7 @@ class KDTree:
             self._torch = torch
             pos = pos.contiguous()
             self.n = pos.shape[0]
-            per = None if period is None else torch.as_tensor(
-                np.broadcast_to(np.asarray(period, np.float64), (3,)).copy(), device=pos.device)
+            per = None if period is None else _device_period(torch, period, pos.device)
             args = [pos, None if vel is None else vel.contiguous(),
                     None if mass is None else mass.contiguous()]
         else:
