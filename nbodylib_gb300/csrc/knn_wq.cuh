@@ -9,7 +9,7 @@
 // Work mapping: one warp serves one query. The query's k-list is distributed over the
 // warp's registers, sorted: position p = s * 32 + lane holds the p-th smallest (d2, index)
 // in slot s of that lane (S slots, k <= 32 S). A batch of candidates enters by a bitonic
-// sort over the lanes and a merge with the list (one slot), or one candidate at a time
+// sort over the lanes and a merge with the list (one or two slots), or one candidate at a time
 // by a ballot (its position) and a shuffle of the tail one place up; the k-th distance
 // (the heap top of the reference) is one shuffle away.
 //
@@ -166,6 +166,59 @@ __device__ __forceinline__ void wq_merge1(WqList<1>& L, int lane, int K, long lo
   L.idx[0] = mj;
 }
 
+// The same for a two-slot list of K <= 64 entries (positions 0-31 in slot 0, 32-63 in
+// slot 1): against the 128-sequence list ascending ++ (batch padded to 64 with +inf)
+// reversed, the lower half keeps slot 0 and takes min(slot 1, batch reversed); that
+// bitonic 64-sequence is sorted by an in-lane compare-exchange (stride 32) and five
+// shuffle half-cleaners per slot.
+__device__ __forceinline__ void wq_merge2(WqList<2>& L, int lane, int K, long long k, int j) {
+  const unsigned FULL = 0xffffffffu;
+  long long rk = __shfl_sync(FULL, k, 31 - lane);
+  int rj = __shfl_sync(FULL, j, 31 - lane);
+  long long a0 = L.key[0], a1 = L.key[1];
+  int i0 = L.idx[0], i1 = L.idx[1];
+  if (rk < a1) {
+    a1 = rk;
+    i1 = rj;
+  }
+  if (a1 < a0) {
+    long long tk = a0;
+    a0 = a1;
+    a1 = tk;
+    int ti = i0;
+    i0 = i1;
+    i1 = ti;
+  }
+#pragma unroll
+  for (int stride = 16; stride > 0; stride >>= 1) {
+    bool lower = (lane & stride) == 0;
+    long long o0 = __shfl_xor_sync(FULL, a0, stride);
+    int p0 = __shfl_xor_sync(FULL, i0, stride);
+    long long o1 = __shfl_xor_sync(FULL, a1, stride);
+    int p1 = __shfl_xor_sync(FULL, i1, stride);
+    if (lower ? (o0 < a0) : (o0 > a0)) {
+      a0 = o0;
+      i0 = p0;
+    }
+    if (lower ? (o1 < a1) : (o1 > a1)) {
+      a1 = o1;
+      i1 = p1;
+    }
+  }
+  if (lane >= K) {
+    a0 = kWqSent;
+    i0 = -1;
+  }
+  if (32 + lane >= K) {
+    a1 = kWqSent;
+    i1 = -1;
+  }
+  L.key[0] = a0;
+  L.idx[0] = i0;
+  L.key[1] = a1;
+  L.idx[1] = i1;
+}
+
 // Per-warp search state of one query.
 template <int S>
 struct WqQuery {
@@ -206,13 +259,14 @@ __device__ void wq_flush(WqQuery<S>& Q, WqSmem& w, const TreeView& tv, int lane,
     if (Q.self >= 0 && (ti == Q.self || dk == 0)) dk = kWqSent;  // KDLeafNode.cxx:19-21
   }
   unsigned acc = __ballot_sync(FULL, dk < Q.topk);
-  if (S == 1 && __popc(acc) > 2) {
+  if (S <= 2 && __popc(acc) > 2) {
     // many at once: sort the batch and merge it (the k smallest of list and batch: the
     // same entries the one-by-one strict insertions keep, up to exact ties)
     long long k = dk < Q.topk ? dk : kWqSent;
     int j = ti;
     warp_sort_asc(k, j, lane);
-    wq_merge1(*reinterpret_cast<WqList<1>*>(&Q.L), lane, Q.K, k, j);
+    if (S == 1) wq_merge1(*reinterpret_cast<WqList<1>*>(&Q.L), lane, Q.K, k, j);
+    else wq_merge2(*reinterpret_cast<WqList<2>*>(&Q.L), lane, Q.K, k, j);
     Q.topk = wq_key_at<S>(Q.L, Q.K - 1);
     acc = 0;
   }
