@@ -150,6 +150,7 @@ namespace {
 struct PendingPhase {
   std::string name;
   cudaEvent_t a, b;
+  int dev;
 };
 struct TraceAcc {
   long long count = 0;
@@ -159,6 +160,24 @@ std::mutex g_trace_mu;
 std::atomic<bool> g_trace_on{false};
 std::vector<PendingPhase> g_pending;
 std::map<std::string, TraceAcc> g_trace;
+// resolved events are kept for reuse (creating events costs host time inside the very
+// call sequence being traced); keyed by device, as events belong to one
+std::map<int, std::vector<cudaEvent_t>> g_event_pool;
+
+cudaEvent_t pooled_event(int dev) {
+  {
+    std::lock_guard<std::mutex> lk(g_trace_mu);
+    auto& v = g_event_pool[dev];
+    if (!v.empty()) {
+      cudaEvent_t e = v.back();
+      v.pop_back();
+      return e;
+    }
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
 
 void resolve_pending() {
   std::lock_guard<std::mutex> lk(g_trace_mu);
@@ -169,8 +188,8 @@ void resolve_pending() {
     auto& acc = g_trace[p.name];
     acc.count++;
     acc.ms += ms;
-    cudaEventDestroy(p.a);
-    cudaEventDestroy(p.b);
+    g_event_pool[p.dev].push_back(p.a);
+    g_event_pool[p.dev].push_back(p.b);
   }
   g_pending.clear();
 }
@@ -180,15 +199,16 @@ Phase::Phase(const char* n, cudaStream_t s) : name(n), st(s) {
   if (!g_trace_on.load(std::memory_order_relaxed)) return;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
-  cudaEventCreate(&a);
-  cudaEventCreate(&b);
+  cudaGetDevice(&dev);
+  a = pooled_event(dev);
+  b = pooled_event(dev);
   cudaEventRecord(a, st);
 }
 Phase::~Phase() {
   if (!a) return;
   cudaEventRecord(b, st);
   std::lock_guard<std::mutex> lk(g_trace_mu);
-  g_pending.push_back({name, a, b});
+  g_pending.push_back({name, a, b, dev});
 }
 
 // Live device allocations made through dev_malloc (freed through dev_free), and the

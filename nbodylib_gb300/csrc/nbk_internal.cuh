@@ -401,6 +401,7 @@ struct Phase {
   const char* name;
   cudaStream_t st;
   cudaEvent_t a = nullptr, b = nullptr;
+  int dev = 0;
   Phase(const char* n, cudaStream_t s);
   ~Phase();
 };
