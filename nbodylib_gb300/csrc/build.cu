@@ -1054,9 +1054,29 @@ int64_t heap_slots(int64_t n, int b) {
 }
 
 int64_t count_nodes(int64_t n, int b) {
-  if (n <= b) return 1;
-  int64_t l = (n - 1) / 2 + 1;
-  return 1 + count_nodes(l, b) + count_nodes(n - l, b);
+  // level by level: the split rule gives the nodes of one level at most a few distinct
+  // sizes, so counting (size, multiplicity) pairs replaces a walk over every node
+  std::vector<std::pair<int64_t, int64_t>> cur{{n, 1}}, nxt;
+  int64_t total = 0;
+  while (!cur.empty()) {
+    nxt.clear();
+    for (auto& sm : cur) {
+      total += sm.second;
+      if (sm.first <= b) continue;
+      int64_t l = (sm.first - 1) / 2 + 1;
+      for (int64_t c : {l, sm.first - l}) {
+        bool found = false;
+        for (auto& q : nxt)
+          if (q.first == c) {
+            q.second += sm.second;
+            found = true;
+          }
+        if (!found) nxt.push_back({c, sm.second});
+      }
+    }
+    cur.swap(nxt);
+  }
+  return total;
 }
 
 // Build every tree of the forest. All arrays live on `st`. Returns NBK status.
@@ -1077,12 +1097,6 @@ static int build_forest_t(const std::vector<TreeSpec>& trees, int b, const doubl
   if (ntot == 0) return NBK_OK;
   double *Ca, *Cb;
   int *IDa, *IDb, *d_err;
-  NBK_TRY(alloc.get((void**)&Ca, sizeof(double) * ND * ntot));
-  NBK_TRY(alloc.get((void**)&Cb, sizeof(double) * ND * ntot));
-  NBK_TRY(alloc.get((void**)&IDa, sizeof(int) * ntot));
-  NBK_TRY(alloc.get((void**)&IDb, sizeof(int) * ntot));
-  NBK_TRY(alloc.get((void**)&d_err, sizeof(int)));
-  NBK_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
   const int64_t cs = ntot;  // coordinate stride of the ping-pong buffers
 
   // The whole plan (every global level's nodes and chunks, every subtree handed to the
@@ -1166,8 +1180,29 @@ static int build_forest_t(const std::vector<TreeSpec>& trees, int b, const doubl
   memcpy(plan.data(), gn.data(), bg);
   memcpy(plan.data() + bg, ch.data(), bc);
   memcpy(plan.data() + bg + bc, lroots.data(), br);
+  // every scratch array of the build in one allocation; the error word and the radix
+  // histograms, which start zeroed, come first
   unsigned char* d_plan;
-  NBK_TRY(alloc.get((void**)&d_plan, plan.size()));
+  unsigned long long* d_cand = nullptr;
+  unsigned *d_hist = nullptr, *d_cl = nullptr, *d_ce = nullptr, *d_bl = nullptr, *d_be = nullptr;
+  const size_t ncall = std::max<size_t>(ch.size(), 1);
+  const size_t hist_bytes = levels.empty() ? 0 : sizeof(unsigned) * kBins * max_ng;
+  std::vector<DevPart> parts{{(void**)&d_err, sizeof(int)}, {(void**)&d_hist, hist_bytes}};
+  const size_t zeroed = block_bytes(parts);
+  parts.insert(parts.end(), {{(void**)&Ca, sizeof(double) * ND * ntot},
+                             {(void**)&Cb, sizeof(double) * ND * ntot},
+                             {(void**)&IDa, sizeof(int) * ntot},
+                             {(void**)&IDb, sizeof(int) * ntot},
+                             {(void**)&d_plan, plan.size()}});
+  if (!levels.empty()) {
+    parts.insert(parts.end(), {{(void**)&d_cand, sizeof(unsigned long long) * ntot},
+                               {(void**)&d_cl, sizeof(unsigned) * ncall},
+                               {(void**)&d_ce, sizeof(unsigned) * ncall},
+                               {(void**)&d_bl, sizeof(unsigned) * ncall},
+                               {(void**)&d_be, sizeof(unsigned) * ncall}});
+  }
+  NBK_TRY(alloc.get_block(parts));
+  NBK_CUDA_TRY(cudaMemsetAsync(d_err, 0, zeroed, st));
   NBK_CUDA_TRY(cudaMemcpyAsync(d_plan, plan.data(), plan.size(), cudaMemcpyHostToDevice, st));
   // every way out of here waits for the stream, so the staging buffer is free again
   struct WaitOnExit {
@@ -1177,18 +1212,6 @@ static int build_forest_t(const std::vector<TreeSpec>& trees, int b, const doubl
   GNode* d_gall = (GNode*)d_plan;
   Chunk* d_call = (Chunk*)(d_plan + bg);
   LRoot* d_r = (LRoot*)(d_plan + bg + bc);
-  unsigned long long* d_cand = nullptr;
-  unsigned *d_hist = nullptr, *d_cl = nullptr, *d_ce = nullptr, *d_bl = nullptr, *d_be = nullptr;
-  if (!levels.empty()) {
-    size_t ncall = std::max<size_t>(ch.size(), 1);
-    NBK_TRY(alloc.get((void**)&d_cand, sizeof(unsigned long long) * ntot));
-    NBK_TRY(alloc.get((void**)&d_hist, sizeof(unsigned) * kBins * max_ng));
-    NBK_CUDA_TRY(cudaMemsetAsync(d_hist, 0, sizeof(unsigned) * kBins * max_ng, st));
-    NBK_TRY(alloc.get((void**)&d_cl, sizeof(unsigned) * ncall));
-    NBK_TRY(alloc.get((void**)&d_ce, sizeof(unsigned) * ncall));
-    NBK_TRY(alloc.get((void**)&d_bl, sizeof(unsigned) * ncall));
-    NBK_TRY(alloc.get((void**)&d_be, sizeof(unsigned) * ncall));
-  }
   k_init_soa<ND><<<(unsigned)((ntot + 255) / 256), 256, 0, st>>>(
       d_pos_in + 3 * p0, d_vel_in ? d_vel_in + 3 * p0 : nullptr, Ca, cs, IDa, ntot, d_err);
   note_launch();

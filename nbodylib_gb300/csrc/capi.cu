@@ -256,6 +256,24 @@ int ensure_dyn_smem(const void* func, int bytes) {
   done[key] = bytes;
   return NBK_OK;
 }
+size_t block_bytes(const std::vector<DevPart>& parts) {
+  size_t total = 0;
+  for (auto& q : parts) total += (std::max<size_t>(q.bytes, 16) + 255) & ~size_t(255);
+  return total;
+}
+void carve_block(void* base, const std::vector<DevPart>& parts) {
+  size_t off = 0;
+  for (auto& q : parts) {
+    *q.p = static_cast<char*>(base) + off;
+    off += (std::max<size_t>(q.bytes, 16) + 255) & ~size_t(255);
+  }
+}
+int DevAlloc::get_block(const std::vector<DevPart>& parts) {
+  void* base = nullptr;
+  NBK_TRY(get(&base, block_bytes(parts)));
+  carve_block(base, parts);
+  return NBK_OK;
+}
 int DevAlloc::get(void** p, size_t bytes) {
   NBK_TRY(dev_malloc(p, bytes, st));
   scratch.push_back(*p);
@@ -301,6 +319,7 @@ struct nbk_tree {
   float eps = 0;
   float eps6[6] = {0, 0, 0, 0, 0, 0};
   int* d_err = nullptr;
+  void* block = nullptr;  // the one device allocation holding every array above
   bool dev() const { return flags & NBK_DEVICE_PTRS; }
   TreeView view() const {
     TreeView v{};
@@ -331,11 +350,9 @@ struct nbk_tree {
 // the tree's stream); a failed nbk_create also waits for the stream.
 static void free_tree_arrays(nbk_tree* t, bool wait) {
   cudaStream_t st = t->st;
-  BuiltArrays& A = t->arr;
-  void* arrays[] = {A.pos, A.posf, A.vel, A.perm, A.node, A.nodex, A.nodes6, A.nodeb6,
-                    A.nodef6, A.velf, t->d_err};
-  for (void* p : arrays) dev_free(p, st);
-  A = BuiltArrays();
+  dev_free(t->block, st);  // every array of the tree lives in this one allocation
+  t->block = nullptr;
+  t->arr = BuiltArrays();
   t->d_err = nullptr;  // t->d_kernel belongs to the process-wide kernel cache
   if (wait) cudaStreamSynchronize(st);
 }
@@ -670,8 +687,6 @@ int nbk_create(const double* pos, const double* vel, const double* mass, int64_t
     t->kernnorm = ke->norm;
     t->d_kernel = ke->d_img;  // shared, not owned by the tree
   }
-  NBK_TRY(dev_malloc((void**)&t->d_err, sizeof(int), st));
-  NBK_CUDA_TRY(cudaMemsetAsync(t->d_err, 0, sizeof(int), st));
   t->nslots = heap_slots(n, bucket_size);
   t->numnodes = count_nodes(n, bucket_size);
   {
@@ -681,38 +696,45 @@ int nbk_create(const double* pos, const double* vel, const double* mass, int64_t
     t->numleaves = nl;
   }
   BuiltArrays& A = t->arr;
-  NBK_TRY(dev_malloc((void**)&A.pos, sizeof(P4) * n, st));
-  NBK_TRY(dev_malloc((void**)&A.posf, sizeof(float4) * n, st));
-  NBK_TRY(dev_malloc((void**)&A.perm, sizeof(int) * n, st));
-  if (vel) NBK_TRY(dev_malloc((void**)&A.vel, sizeof(V4) * n, st));
-  if (treetype == NBK_TPHS) {
-    NBK_TRY(dev_malloc((void**)&A.nodes6, sizeof(NodeS) * t->nslots, st));
-    NBK_TRY(dev_malloc((void**)&A.nodeb6, sizeof(NodeB6) * t->nslots, st));
-    NBK_TRY(dev_malloc((void**)&A.nodef6, sizeof(NodeF6) * t->nslots, st));
-    NBK_TRY(dev_malloc((void**)&A.velf, sizeof(float4) * n, st));
-    NBK_CUDA_TRY(cudaMemsetAsync(A.nodes6, 0, sizeof(NodeS) * t->nslots, st));
-    NBK_CUDA_TRY(cudaMemsetAsync(A.nodeb6, 0, sizeof(NodeB6) * t->nslots, st));
-  } else {
-    NBK_TRY(dev_malloc((void**)&A.node, sizeof(NodeRec) * t->nslots, st));
-    NBK_TRY(dev_malloc((void**)&A.nodex, sizeof(NodeX) * t->nslots, st));
-    NBK_CUDA_TRY(cudaMemsetAsync(A.node, 0, sizeof(NodeRec) * t->nslots, st));
-    NBK_CUDA_TRY(cudaMemsetAsync(A.nodex, 0, sizeof(NodeX) * t->nslots, st));
+  {
+    // every array of the tree in one allocation; the error word and the node arrays that
+    // start zeroed come first, so one memset clears them
+    const bool phs = treetype == NBK_TPHS;
+    std::vector<DevPart> parts{{(void**)&t->d_err, sizeof(int)}};
+    if (phs) {
+      parts.push_back({(void**)&A.nodes6, sizeof(NodeS) * t->nslots});
+      parts.push_back({(void**)&A.nodeb6, sizeof(NodeB6) * t->nslots});
+    } else {
+      parts.push_back({(void**)&A.node, sizeof(NodeRec) * t->nslots});
+      parts.push_back({(void**)&A.nodex, sizeof(NodeX) * t->nslots});
+    }
+    size_t zeroed = block_bytes(parts);
+    parts.push_back({(void**)&A.pos, sizeof(P4) * n});
+    parts.push_back({(void**)&A.posf, sizeof(float4) * n});
+    parts.push_back({(void**)&A.perm, sizeof(int) * n});
+    if (vel) parts.push_back({(void**)&A.vel, sizeof(V4) * n});
+    if (phs) {
+      parts.push_back({(void**)&A.nodef6, sizeof(NodeF6) * t->nslots});
+      parts.push_back({(void**)&A.velf, sizeof(float4) * n});
+    }
+    NBK_TRY(dev_malloc(&t->block, block_bytes(parts), st));
+    carve_block(t->block, parts);
+    NBK_CUDA_TRY(cudaMemsetAsync(t->block, 0, zeroed, st));
   }
   DevAlloc alloc;
   alloc.st = st;
   const double *d_pos = pos, *d_vel = vel, *d_mass = mass;
   if (!(flags & NBK_DEVICE_PTRS)) {
     double *a, *v = nullptr, *m = nullptr;
-    NBK_TRY(alloc.get((void**)&a, sizeof(double) * 3 * n));
+    std::vector<DevPart> parts{{(void**)&a, sizeof(double) * 3 * n}};
+    if (vel) parts.push_back({(void**)&v, sizeof(double) * 3 * n});
+    if (mass) parts.push_back({(void**)&m, sizeof(double) * n});
+    NBK_TRY(alloc.get_block(parts));
     NBK_CUDA_TRY(cudaMemcpyAsync(a, pos, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
-    if (vel) {
-      NBK_TRY(alloc.get((void**)&v, sizeof(double) * 3 * n));
+    if (vel)
       NBK_CUDA_TRY(cudaMemcpyAsync(v, vel, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st));
-    }
-    if (mass) {
-      NBK_TRY(alloc.get((void**)&m, sizeof(double) * n));
+    if (mass)
       NBK_CUDA_TRY(cudaMemcpyAsync(m, mass, sizeof(double) * n, cudaMemcpyHostToDevice, st));
-    }
     d_pos = a;
     d_vel = v;
     d_mass = m;
@@ -1604,8 +1626,8 @@ int nbk_fof(nbk_tree* t, double fdist, int32_t minnum, int order, int32_t* group
   int* dg;
   NBK_TRY(S.out(group, t->n, &dg));
   int *parent, *gtree;
-  NBK_TRY(S.alloc.get((void**)&parent, sizeof(int) * t->n));
-  NBK_TRY(S.alloc.get((void**)&gtree, sizeof(int) * t->n));
+  NBK_TRY(S.alloc.get_block({{(void**)&parent, sizeof(int) * t->n},
+                             {(void**)&gtree, sizeof(int) * t->n}}));
   NBK_TRY(clear_err(t));
   FofArgs a{};
   a.tv = t->view();

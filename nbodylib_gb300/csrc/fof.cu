@@ -993,11 +993,11 @@ int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tr
   int* cnt;
   int *flag, *lbl, *bsum, *d_total;
   int nb = (n + 1023) / 1024;
-  NBK_TRY(alloc.get((void**)&cnt, sizeof(int) * n));
-  NBK_TRY(alloc.get((void**)&flag, sizeof(int) * n));
-  NBK_TRY(alloc.get((void**)&lbl, sizeof(int) * n));
-  NBK_TRY(alloc.get((void**)&bsum, sizeof(int) * (nb + 1)));
-  NBK_TRY(alloc.get((void**)&d_total, sizeof(int)));
+  NBK_TRY(alloc.get_block({{(void**)&cnt, sizeof(int) * n},
+                           {(void**)&flag, sizeof(int) * n},
+                           {(void**)&lbl, sizeof(int) * n},
+                           {(void**)&bsum, sizeof(int) * (nb + 1)},
+                           {(void**)&d_total, sizeof(int)}}));
   k_iota<<<(n + 255) / 256, 256, 0, st>>>(a.parent, n); note_launch();
   // FOFCriterion with FOF3d inside its search region links exactly the pairs with
   // sum dx^2 / params[6] < 1: the FOF kernels with ll^2 = params[6]

@@ -41,10 +41,20 @@ struct BuiltArrays {
 // Stream-ordered device allocations. Scratch allocations made through get() are freed
 // together by release_all_scratch(); the device's default memory pool keeps the memory
 // cached, so repeated builds do not return to the driver.
+// One device allocation carved into several arrays, each starting on a 256-byte boundary
+// (one call to the allocator instead of one per array).
+struct DevPart {
+  void** p;
+  size_t bytes;
+};
+size_t block_bytes(const std::vector<DevPart>& parts);
+void carve_block(void* base, const std::vector<DevPart>& parts);
+
 struct DevAlloc {
   std::vector<void*> scratch;
   cudaStream_t st = nullptr;
   int get(void** p, size_t bytes);
+  int get_block(const std::vector<DevPart>& parts);
   int upload(void* dst, const void* src, size_t bytes, cudaStream_t s);
   void release_all_scratch(cudaStream_t s);
   ~DevAlloc();
