@@ -13,8 +13,14 @@
 // The backward kernel recomputes every weight from the saved neighbour lists (4 B per
 // neighbour) instead of storing weights; one thread per particle, FP64 atomics for the
 // contributions that land on other particles. The quotients that do not depend on the
-// pair (g_i = w_i / rho_i, the table slopes (T[c+1]-T[c])/delta, -0.5 h^-3 / h) are
-// formed once, so a pair costs two FP64 divisions and one square root.
+// pair (g_i = w_i / rho_i, the table slopes (T[c+1]-T[c])/delta, 1/h, h^-3) are formed
+// once; a pair takes 1/r from an FP32 reciprocal square root and two FP64 Newton steps
+// (no division, no FP64 square root). Each pair's table cell is the forward pass's
+// (int)(r / h * 0.5 * (kernres - 1)): from the fast r / h, and from the correctly rounded
+// square root and division whenever the fast value lies within 1e-10 of a cell edge (its
+// own error is below 1e-12 there), so the frozen cells are exactly the forward's.
+// The forward (the warp-per-query kNN) writes each neighbour row ascending in distance,
+// so the row's last entry is the farthest neighbour, the one that set h_i.
 #include <algorithm>
 
 #include "nbk_build.h"
@@ -22,6 +28,18 @@
 namespace nbk {
 
 namespace {
+
+// 1 / sqrt(x) to about 2e-16 relative: the FP32 reciprocal square root and two Newton
+// steps y (3/2 - x/2 y^2) in FP64; outside the FP32 normal range the FP64 path.
+__device__ __forceinline__ double rsqrt_newton(double x) {
+  const float xf = __double2float_rn(x);
+  if (!(xf > 1e-30f && xf < 1e30f)) return 1.0 / __dsqrt_rn(x);
+  double y = (double)rsqrtf(xf);
+  const double hx = 0.5 * x;
+  y = y * __fma_rn(-hx, y * y, 1.5);
+  y = y * __fma_rn(-hx, y * y, 1.5);
+  return y;
+}
 
 // g_i = w_i / rho_i in place of w_i (tree order), and the slope of every table cell
 // (0 for the last entry, whose cell the forward pass never interpolates).
@@ -46,32 +64,31 @@ __global__ void __launch_bounds__(128) k_adjoint(TreeView tv, int K, const int* 
   const int* row = nn + (size_t)i * K;
   P4 xi = tv.pos[ti];
   double gi = g[ti];
-  // farthest neighbour: the one that set h_i in the forward pass
-  double best = -1.0;
-  int kf = row[0];
-  for (int s = 0; s < K; s++) {
-    P4 xj = tv.pos[row[s]];
-    double d2 = dist2_exact(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z);
-    if (d2 > best) {
-      best = d2;
-      kf = row[s];
-    }
-  }
-  double rk = __dsqrt_rn(best);
-  double hh = 0.5 * rk;
-  double norm = 1.0 / pow(hh, 3.0);
-  double delta = 2.0 / (double)(kr - 1);
-  double nh = -0.5 * norm / hh;  // dw/dh = nh (3 T + q T'), dw/dr = -nh T'
+  // farthest neighbour: the one that set h_i in the forward pass (the row's last entry)
+  const int kf = row[K - 1];
+  P4 xk = tv.pos[kf];
+  const double best = dist2_exact(xi.x, xi.y, xi.z, xk.x, xk.y, xk.z);
+  const double hh = 0.5 * __dsqrt_rn(best);  // the forward's h_i, for the cell edge cases
+  const double irk = rsqrt_newton(best);      // 1 / r_iK
+  const double ih = 2.0 * irk;                // 1 / h_i
+  const double norm = ih * ih * ih;
+  const double delta = 2.0 / (double)(kr - 1);
+  const double hk = 0.5 * (double)(kr - 1);
+  const double nh = -0.5 * norm * ih;  // dw/dh = nh (3 T + q T'), dw/dr = -nh T'
   double A = 0.0, gmi = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
   for (int s = 0; s < K; s++) {
     int j = row[s];
     P4 xj = tv.pos[j];
     double dx = xi.x - xj.x, dy = xi.y - xj.y, dz = xi.z - xj.z;
-    double rij = __dsqrt_rn(dist2_exact(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z));
-    double q = rij / hh;
-    int c = (int)(q * 0.5 * (double)(kr - 1));
-    double Tq = wsm(q, c, kr, delta, T);
+    double d2 = dist2_exact(xi.x, xi.y, xi.z, xj.x, xj.y, xj.z);
+    double ir = rsqrt_newton(d2);  // 1 / r_ij (the target search excluded r = 0)
+    double q = d2 * ir * ih;
+    double u = q * hk;
+    int c = (int)u;
+    double fr = u - (double)c;
+    if (fr < 1e-10 || fr > 1.0 - 1e-10) c = (int)(__dsqrt_rn(d2) / hh * 0.5 * (double)(kr - 1));
     double Tp = slope[c < kr - 1 ? c : kr - 1];
+    double Tq = c < kr - 1 ? __fma_rn(Tp, q - delta * (double)c, T[c]) : T[kr - 1];
     double w = 0.5 * Tq * norm;
     double gj = g[j];
     double cij = gi * xj.m + gj * xi.m;
@@ -80,7 +97,7 @@ __global__ void __launch_bounds__(128) k_adjoint(TreeView tv, int K, const int* 
     double dwdr = -nh * Tp;
     double dwdh = nh * (3.0 * Tq + q * Tp);
     A += cij * dwdh;
-    double coef = cij * dwdr / rij;
+    double coef = cij * dwdr * ir;
     gx += coef * dx;
     gy += coef * dy;
     gz += coef * dz;
@@ -88,8 +105,7 @@ __global__ void __launch_bounds__(128) k_adjoint(TreeView tv, int K, const int* 
     atomicAdd(&gpos[3 * (size_t)j + 1], -coef * dy);
     atomicAdd(&gpos[3 * (size_t)j + 2], -coef * dz);
   }
-  P4 xk = tv.pos[kf];
-  double ch = A * 0.5 / rk;
+  double ch = A * 0.5 * irk;
   double kx = ch * (xi.x - xk.x), ky = ch * (xi.y - xk.y), kz = ch * (xi.z - xk.z);
   atomicAdd(&gpos[3 * (size_t)kf + 0], -kx);
   atomicAdd(&gpos[3 * (size_t)kf + 1], -ky);
