@@ -122,7 +122,9 @@ int nbk_debug_set_iteration_cap(int cap);
    NBK_ERR_NOMEM, once; a negative countdown disarms. */
 int nbk_debug_fail_allocation(long long countdown);
 /* Device allocations the library currently holds (trees, batches, per-call scratch not
-   yet freed); a failed call must leave it where it was. */
+   yet freed, and the scratch blocks a host thread keeps for its next tree build and FOF
+   call, at most 256 MB each, held until the thread exits); a failed call must leave it
+   where it was. */
 long long nbk_debug_live_allocations(void);
 
 /*

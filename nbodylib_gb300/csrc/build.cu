@@ -1265,7 +1265,8 @@ static int build_forest_t(const std::vector<TreeSpec>& trees, int b, const doubl
                                {(void**)&d_bl, sizeof(unsigned) * ncall},
                                {(void**)&d_be, sizeof(unsigned) * ncall}});
   }
-  NBK_TRY(alloc.get_block(parts));
+  // every way out of this build waits for the stream, so this thread's kept block is free
+  NBK_TRY(thread_scratch_block(0, parts, st, alloc));
   NBK_CUDA_TRY(cudaMemsetAsync(d_err, 0, zeroed, st));
   NBK_CUDA_TRY(cudaMemcpyAsync(d_plan, plan.data(), plan.size(), cudaMemcpyHostToDevice, st));
   // every way out of here waits for the stream, so the staging buffer is free again

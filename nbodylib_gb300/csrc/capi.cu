@@ -87,8 +87,15 @@ static int cached_kernel(int kerntype, int kernres, int nd, const KernelEntry** 
   static std::map<std::tuple<int, int, int, int>, KernelEntry> cache;
   int dev = 0;
   NBK_CUDA_TRY(cudaGetDevice(&dev));
-  std::lock_guard<std::mutex> lock(mu);
   auto key = std::make_tuple(dev, kerntype, kernres, nd);
+  // the entries never move or go away, so a thread can keep its last one
+  static thread_local std::tuple<int, int, int, int> last_key{-1, -1, -1, -1};
+  static thread_local const KernelEntry* last = nullptr;
+  if (last && last_key == key) {
+    *out = last;
+    return NBK_OK;
+  }
+  std::lock_guard<std::mutex> lock(mu);
   auto it = cache.find(key);
   if (it == cache.end()) {
     KernelEntry e;
@@ -101,6 +108,8 @@ static int cached_kernel(int kerntype, int kernres, int nd, const KernelEntry** 
     it = cache.emplace(key, std::move(e)).first;
   }
   *out = &it->second;
+  last_key = key;
+  last = &it->second;
   return NBK_OK;
 }
 
@@ -268,6 +277,47 @@ void carve_block(void* base, const std::vector<DevPart>& parts) {
     off += (std::max<size_t>(q.bytes, 16) + 255) & ~size_t(255);
   }
 }
+// Per-thread scratch blocks for calls that end with a synchronisation of their stream
+// (the tree build; FOF), so the block is idle again when the call returns and the next
+// call on this thread can reuse it instead of going to the allocator. Blocks above
+// kThreadScratchMax are not kept. A kept block stays allocated until the thread exits.
+constexpr size_t kThreadScratchMax = size_t(256) << 20;
+struct ThreadScratch {
+  void* p = nullptr;
+  size_t cap = 0;
+  int dev = -1;
+  ~ThreadScratch() {
+    if (p) {
+      cudaFree(p);
+      g_live_allocs.fetch_sub(1, std::memory_order_relaxed);
+    }
+  }
+};
+int thread_scratch_block(int slot, const std::vector<DevPart>& parts, cudaStream_t st,
+                         DevAlloc& fallback) {
+  static thread_local ThreadScratch keep[3];
+  size_t bytes = block_bytes(parts);
+  int dev = 0;
+  NBK_CUDA_TRY(cudaGetDevice(&dev));
+  if (slot < 0 || slot > 2 || bytes > kThreadScratchMax) return fallback.get_block(parts);
+  ThreadScratch& k = keep[slot];
+  if (!k.p || k.cap < bytes || k.dev != dev) {
+    if (k.p && k.dev == dev) {
+      dev_free(k.p, st);
+    } else if (k.p) {  // another device's block: cudaFree finds its device itself
+      cudaFree(k.p);
+      g_live_allocs.fetch_sub(1, std::memory_order_relaxed);
+    }
+    k.p = nullptr;
+    k.cap = 0;
+    NBK_TRY(dev_malloc(&k.p, bytes, st));
+    k.cap = bytes;
+    k.dev = dev;
+  }
+  carve_block(k.p, parts);
+  return NBK_OK;
+}
+
 int DevAlloc::get_block(const std::vector<DevPart>& parts) {
   void* base = nullptr;
   NBK_TRY(get(&base, block_bytes(parts)));
@@ -1626,8 +1676,12 @@ int nbk_fof(nbk_tree* t, double fdist, int32_t minnum, int order, int32_t* group
   int* dg;
   NBK_TRY(S.out(group, t->n, &dg));
   int *parent, *gtree;
-  NBK_TRY(S.alloc.get_block({{(void**)&parent, sizeof(int) * t->n},
-                             {(void**)&gtree, sizeof(int) * t->n}}));
+  // the call ends with a synchronisation (an early return waits too), so this thread's
+  // kept block is free again then
+  SyncUnlessOk sync_guard{t->st};
+  NBK_TRY(thread_scratch_block(2, {{(void**)&parent, sizeof(int) * t->n},
+                                   {(void**)&gtree, sizeof(int) * t->n}},
+                               t->st, S.alloc));
   NBK_TRY(clear_err(t));
   FofArgs a{};
   a.tv = t->view();
@@ -1647,9 +1701,11 @@ int nbk_fof(nbk_tree* t, double fdist, int32_t minnum, int order, int32_t* group
   if (ps) {
     NBK_CUDA_TRY(cudaMemcpyAsync(&ps->i[1], t->d_err, sizeof(int), cudaMemcpyDeviceToHost, t->st));
     NBK_CUDA_TRY(cudaStreamSynchronize(t->st));
+    sync_guard.ok = true;  // synchronised above
     NBK_TRY(err_status(ps->i[1], "nbk_fof"));
     ng = ps->i[0];
   } else {
+    sync_guard.ok = true;  // check_err synchronises
     NBK_TRY(check_err(t, "nbk_fof"));
   }
   *ngroup = ng;

@@ -993,11 +993,15 @@ int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tr
   int* cnt;
   int *flag, *lbl, *bsum, *d_total;
   int nb = (n + 1023) / 1024;
-  NBK_TRY(alloc.get_block({{(void**)&cnt, sizeof(int) * n},
-                           {(void**)&flag, sizeof(int) * n},
-                           {(void**)&lbl, sizeof(int) * n},
-                           {(void**)&bsum, sizeof(int) * (nb + 1)},
-                           {(void**)&d_total, sizeof(int)}}));
+  // every caller synchronises its stream before it returns (the group count, or the
+  // error word; an early return here waits), so this thread's kept block is free again
+  SyncUnlessOk sync_guard{st};
+  NBK_TRY(thread_scratch_block(1, {{(void**)&cnt, sizeof(int) * n},
+                                   {(void**)&flag, sizeof(int) * n},
+                                   {(void**)&lbl, sizeof(int) * n},
+                                   {(void**)&bsum, sizeof(int) * (nb + 1)},
+                                   {(void**)&d_total, sizeof(int)}},
+                               st, alloc));
   k_iota<<<(n + 255) / 256, 256, 0, st>>>(a.parent, n); note_launch();
   // FOFCriterion with FOF3d inside its search region links exactly the pairs with
   // sum dx^2 / params[6] < 1: the FOF kernels with ll^2 = params[6]
@@ -1045,6 +1049,7 @@ int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tr
   if (defer_count && !order) {
     // the caller's page-locked h_ngroup is read after the caller's own synchronisation
     NBK_CUDA_TRY(cudaMemcpyAsync(h_ngroup, d_total, sizeof(int), cudaMemcpyDeviceToHost, st));
+    sync_guard.ok = true;
     return NBK_OK;
   }
   int total = 0;
@@ -1067,6 +1072,7 @@ int run_fof(const FofArgs& a, int nnodes, int minnum, int order, int* d_group_tr
     k_relabel<<<(n + 255) / 256, 256, 0, st>>>(d_group_tree, newlbl, n); note_launch();
     NBK_CUDA_TRY(cudaGetLastError());
   }
+  sync_guard.ok = true;  // the count was read above (a synchronisation); callers wait again
   return NBK_OK;
 }
 

@@ -49,6 +49,21 @@ struct DevPart {
 };
 size_t block_bytes(const std::vector<DevPart>& parts);
 void carve_block(void* base, const std::vector<DevPart>& parts);
+struct DevAlloc;
+// A scratch block kept per host thread and slot (0: tree build, 1: FOF labels, 2: FOF
+// union-find arrays) for calls that synchronise their stream before they return; blocks
+// above 256 MB, or any request when the slot is unusable, come from `fallback` instead.
+int thread_scratch_block(int slot, const std::vector<DevPart>& parts, cudaStream_t st,
+                         DevAlloc& fallback);
+// Waits for the stream when a call leaves early (ok not set): its kernels may still use a
+// kept scratch block that the thread's next call would reuse.
+struct SyncUnlessOk {
+  cudaStream_t st;
+  bool ok = false;
+  ~SyncUnlessOk() {
+    if (!ok) cudaStreamSynchronize(st);
+  }
+};
 
 struct DevAlloc {
   std::vector<void*> scratch;

@@ -91,7 +91,7 @@ def test_allocation_failure_at_every_point_is_clean(gpu, port_built):
         break
     else:
         raise AssertionError("the sequence never completed")
-    assert failures >= 5  # creation, FOF and density each allocate
+    assert failures >= 4  # creation, FOF and density allocate (kept scratch blocks do not)
     assert lib.nbk_debug_live_allocations() == base
 
 
@@ -127,10 +127,12 @@ def test_batch_allocation_failure_is_clean(gpu, port_built):
 
 
 def test_tree_gives_back_every_allocation(gpu):
-    # a tree holds its arrays while it lives and gives every one back when destroyed
+    # a tree holds its arrays while it lives and gives every one back when destroyed (a
+    # first build keeps this thread's build scratch block, so the count is taken after it)
     lib = _capi.load()
-    base = lib.nbk_debug_live_allocations()
     pos, mass = syn.uniform_box(4096, 1.0, seed=83)
+    KDTree(pos, None, mass, 16, kerntype=0).close()
+    base = lib.nbk_debug_live_allocations()
     t = KDTree(pos, None, mass, 16, kerntype=0)
     assert lib.nbk_debug_live_allocations() > base
     t.close()
