@@ -254,7 +254,7 @@ __device__ bool ph_spacing_from_heap(const TreeView& tv, const PhHeap<KMAX, NT>&
       id[b] = id[b - 1];
       id[b - 1] = ti;
     }
-  if (id[0] < 0) return false;
+  if (id[7] < 0) return false;
   double sr0[6] = {0, 0, 0, 0, 0, 0};
   double kvol = 0.0;
   for (int ivol = 1; kvol == 0.0 && ivol < 8; ivol++) {
