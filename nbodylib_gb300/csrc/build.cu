@@ -694,6 +694,322 @@ __global__ void __launch_bounds__(kThreads) k_scatter(const Chunk* __restrict__ 
   }
 }
 
+// ---- phase 1b: one CTA per subtree of at most kMidMax (and more than kLocalMax) particles.
+// The CTA splits the subtree's nodes level by level, one node at a time, down to the
+// subtrees of at most kLocalMax particles that phase 2 finishes. Each split makes the
+// same decisions as a global level -- split dimension from the node box, the median key
+// by radix passes over the order keys (kept in shared memory; the median's class is
+// ranked directly once it holds at most kMidCollect keys), the stable 3-way partition
+// into the other buffer, the children's boxes -- with block barriers where a global level
+// needs arrival counters and launches.
+constexpr int kMidMax = 8192;
+constexpr int kMidThreads = 1024;
+constexpr int kMidCollect = 256;  // a class this small is ranked directly (O(n^2) compares)
+constexpr int kMidNodes = kMidMax / kLocalMax;  // nodes above kLocalMax on one level
+
+struct MRoot {
+  int start, size;  // absolute range in the ping-pong buffers
+  int nbase, h;     // node index of the tree's root, heap index of this subtree root
+  int buf;          // which ping-pong buffer holds its particles
+  int pad;
+};
+
+template <int ND>
+struct MNode {
+  int start, size, h, pad;
+  unsigned long long kmin[ND], kmax[ND];  // box as order keys
+};
+
+template <int ND>
+struct MidLayout {
+  static constexpr size_t key = 0;                                              // u64[kMidMax]
+  static constexpr size_t dst = key + sizeof(unsigned long long) * kMidMax;     // int[kMidMax]
+  static constexpr size_t bins = dst + sizeof(int) * kMidMax;  // u32[kBins], or u64[kMidCollect] keys
+  static constexpr size_t nodes = bins + sizeof(unsigned) * kBins;              // MNode[2][kMidNodes]
+  static constexpr size_t total = nodes + sizeof(MNode<ND>) * 2 * kMidNodes;
+  static_assert(sizeof(unsigned) * kBins >= sizeof(unsigned long long) * kMidCollect,
+                "the gathered keys share the bins' shared memory");
+  static_assert(nodes % 16 == 0, "MNode alignment");
+};
+
+template <int ND>
+__global__ void __launch_bounds__(kMidThreads) k_mid_build(
+    const MRoot* __restrict__ roots, double* Ca, int* IDa, double* Cb, int* IDb, int64_t cs,
+    NodeOut<ND> out, int* err, int p0) {
+  using L = MidLayout<ND>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  unsigned long long* key = (unsigned long long*)(smem + L::key);
+  int* dsti = (int*)(smem + L::dst);
+  unsigned* bin = (unsigned*)(smem + L::bins);
+  unsigned long long* cand = (unsigned long long*)(smem + L::bins);
+  MNode<ND>* cur = (MNode<ND>*)(smem + L::nodes);
+  MNode<ND>* nxt = cur + kMidNodes;
+  __shared__ unsigned wsum[32], tot;
+  __shared__ int n_cur, n_next, s_k, s_ncand;
+  __shared__ unsigned s_fill;
+  __shared__ unsigned long long s_prefix;
+  __shared__ unsigned long long box[4 * ND];  // left min, left max, right min, right max
+  const int tid = threadIdx.x, lane = tid & 31;
+  const MRoot R = roots[blockIdx.x];
+  int buf = R.buf;
+
+  // the subtree root's box
+  if (tid < 2 * ND) box[tid] = tid < ND ? ~0ull : 0ull;
+  __syncthreads();
+  {
+    const double* C = buf ? Cb : Ca;
+#pragma unroll
+    for (int d = 0; d < ND; d++) {
+      unsigned long long mn = ~0ull, mx = 0ull;
+      for (int i = tid; i < R.size; i += kMidThreads) {
+        unsigned long long k = okey(C[d * cs + R.start + i]);
+        mn = min(mn, k);
+        mx = max(mx, k);
+      }
+      mn = warp_min_u64(mn);
+      mx = warp_max_u64(mx);
+      if (lane == 0) {
+        atomicMin(&box[d], mn);
+        atomicMax(&box[ND + d], mx);
+      }
+    }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    MNode<ND> r;
+    r.start = R.start;
+    r.size = R.size;
+    r.h = R.h;
+    r.pad = 0;
+    for (int d = 0; d < ND; d++) {
+      r.kmin[d] = box[d];
+      r.kmax[d] = box[ND + d];
+    }
+    cur[0] = r;
+    n_cur = 1;
+  }
+  __syncthreads();
+  for (int depth = 0; depth < 32 && n_cur > 0; depth++) {
+    const double* C = buf ? Cb : Ca;
+    const int* I = buf ? IDb : IDa;
+    double* C2 = buf ? Ca : Cb;
+    int* I2 = buf ? IDa : IDb;
+    const int ncur = n_cur;  // read by every thread before thread 0 rewrites it
+    if (tid == 0) n_next = 0;
+    for (int j = 0; j < ncur; j++) {
+      const MNode<ND> nd = cur[j];
+      const int S = nd.size, s0 = nd.start;
+      // DetermineSplitDim: the first strictly larger FP64 spread wins
+      double lo[ND], hi[ND];
+#pragma unroll
+      for (int d = 0; d < ND; d++) {
+        lo[d] = okey_inv(nd.kmin[d]);
+        hi[d] = okey_inv(nd.kmax[d]);
+      }
+      int dim = 0;
+      double spread = dsub(hi[0], lo[0]);
+#pragma unroll
+      for (int d = 1; d < ND; d++) {
+        double sp = dsub(hi[d], lo[d]);
+        if (sp > spread) {
+          dim = d;
+          spread = sp;
+        }
+      }
+      const double* Cd = C + (int64_t)dim * cs + s0;
+      for (int i = tid; i < S; i += kMidThreads) key[i] = okey(Cd[i]);
+      // the median key: rank kr = (S - 1) / 2 along dim
+      const int kr = (S - 1) / 2;
+      const unsigned long long kmin_dim = sel<ND>(nd.kmin, dim), kmax_dim = sel<ND>(nd.kmax, dim);
+      const unsigned long long x = kmin_dim ^ kmax_dim;
+      const int first_diff = x ? 63 - __clzll((long long)x) : -1;
+      unsigned long long mask = first_diff < 0 ? ~0ull
+                                               : (first_diff >= 63 ? 0ull : (~0ull << (first_diff + 1)));
+      unsigned long long prefix = first_diff < 0 ? kmin_dim : (kmin_dim & mask);
+      int k = kr, ncand = S;
+      __syncthreads();  // keys stored
+      for (int pass = 0; mask != ~0ull && pass < kPasses; pass++) {
+        if (ncand <= kMidCollect) {
+          // the class is small: gather its keys; the k-th smallest of them is the median key
+          if (tid == 0) s_fill = 0u;
+          __syncthreads();
+          for (int i = tid; i < S; i += kMidThreads) {
+            const unsigned long long kk = key[i];
+            if ((kk & mask) == prefix) {
+              unsigned slot = atomicAdd(&s_fill, 1u);
+              if (slot < (unsigned)kMidCollect) cand[slot] = kk;
+            }
+          }
+          __syncthreads();
+          const int n = min(ncand, kMidCollect);
+          if (tid == 0 && s_fill != (unsigned)ncand) atomicExch(err, 5);
+          if (tid < n) {
+            const unsigned long long mine = cand[tid];
+            int below = 0, equal = 0;
+            for (int i = 0; i < n; i++) {
+              const unsigned long long o = cand[i];
+              below += o < mine;
+              equal += o == mine;
+            }
+            const int kk = min(max(k, 0), n - 1);
+            if (below <= kk && kk < below + equal) s_prefix = mine;  // every holder: same value
+          }
+          __syncthreads();
+          prefix = s_prefix;
+          mask = ~0ull;
+          __syncthreads();  // s_prefix and the gathered keys are read before any reuse
+          break;
+        }
+        const int hi_bit = first_diff - 11 * pass;
+        const int width = min(11, hi_bit + 1), shift = hi_bit - width + 1;
+        const unsigned long long dmask = ((1ull << width) - 1ull) << shift;
+        for (int i = tid; i < kBins; i += kMidThreads) bin[i] = 0u;
+        __syncthreads();
+        // whole warps per round (match_any needs every lane): lanes with the same digit
+        // add once
+        for (int i0 = 0; i0 < S; i0 += kMidThreads) {
+          const int i = i0 + tid;
+          int digit = -1;
+          if (i < S) {
+            const unsigned long long kk = key[i];
+            if ((kk & mask) == prefix) digit = (int)((kk & dmask) >> shift);
+          }
+          const unsigned peers = __match_any_sync(0xffffffffu, digit);
+          if (digit >= 0 && lane == __ffs(peers) - 1) atomicAdd(&bin[digit], __popc(peers));
+        }
+        __syncthreads();
+        // the digit whose bin holds rank k: each thread owns kPer consecutive bins
+        constexpr int kPer = kBins / kMidThreads;
+        unsigned cnt[kPer], sum = 0;
+#pragma unroll
+        for (int q = 0; q < kPer; q++) {
+          cnt[q] = bin[tid * kPer + q];
+          sum += cnt[q];
+        }
+        unsigned before = block_excl_scan_t<kMidThreads>(sum, &tot, wsum);
+        if (before <= (unsigned)k && (unsigned)k < before + sum) {
+          int digit = -1;
+#pragma unroll
+          for (int q = 0; q < kPer; q++) {
+            if (digit < 0) {
+              if ((unsigned)k < before + cnt[q]) {
+                digit = tid * kPer + q;
+                s_ncand = (int)cnt[q];
+              } else {
+                before += cnt[q];
+              }
+            }
+          }
+          s_k = k - (int)before;
+          s_prefix = prefix | ((unsigned long long)digit << shift);
+        }
+        __syncthreads();
+        k = s_k;
+        ncand = s_ncand;
+        prefix = s_prefix;
+        mask |= dmask;
+        __syncthreads();  // the shared values are read before the next pass writes them
+      }
+      if (mask != ~0ull && tid == 0) atomicExch(err, 5);  // selection unfinished: report
+      const unsigned long long piv = prefix;
+      // counts below / equal to the median key over contiguous runs, one per thread
+      const int E = (S + kMidThreads - 1) / kMidThreads;
+      const int r0 = min(tid * E, S), r1 = min(r0 + E, S);
+      unsigned a = 0, e = 0;
+      for (int i = r0; i < r1; i++) {
+        a += key[i] < piv;
+        e += key[i] == piv;
+      }
+      // (less, equal) packed in one word: both counts stay below 2^16
+      const unsigned pre = block_excl_scan_t<kMidThreads>((a << 16) | e, &tot, wsum);
+      const int n_less = (int)(tot >> 16), total_eq = (int)(tot & 0xffffu);
+      const int kleft = kr + 1, right0 = s0 + kleft;
+      const int need_eq = kleft - n_less, excess = total_eq - need_eq;
+      if (tid == 0) out.write(R.nbase + nd.h, lo, hi, p0 + s0, S, dim, okey_inv(piv));
+      // destinations: less, then the first need_eq equal keys on the left; the other equal
+      // keys, then greater, on the right; each class in its current order
+      unsigned rl = pre >> 16, re = pre & 0xffffu;
+      unsigned rg = (unsigned)r0 - rl - re;
+      for (int i = r0; i < r1; i++) {
+        const unsigned long long kk = key[i];
+        int dst;
+        if (kk < piv) {
+          dst = s0 + (int)(rl++);
+        } else if (kk == piv) {
+          const int q = (int)(re++);
+          dst = q < need_eq ? s0 + n_less + q : right0 + (q - need_eq);
+        } else {
+          dst = right0 + excess + (int)(rg++);
+        }
+        if (dst < s0 || dst >= s0 + S) {  // selection inconsistent: report, keep in bounds
+          atomicExch(err, 2);
+          dst = s0 + i;
+        }
+        dsti[i] = dst;
+      }
+      if (tid < 4 * ND) box[tid] = (tid % (2 * ND)) < ND ? ~0ull : 0ull;
+      __syncthreads();
+      // move every coordinate and id; the children's boxes on the way
+#pragma unroll
+      for (int d = 0; d < ND; d++) {
+        unsigned long long mnl = ~0ull, mxl = 0ull, mnr = ~0ull, mxr = 0ull;
+        for (int i = tid; i < S; i += kMidThreads) {
+          const double v = C[d * cs + s0 + i];
+          const int t = dsti[i];
+          C2[d * cs + t] = v;
+          const unsigned long long kk = okey(v);
+          if (t < right0) {
+            mnl = min(mnl, kk);
+            mxl = max(mxl, kk);
+          } else {
+            mnr = min(mnr, kk);
+            mxr = max(mxr, kk);
+          }
+        }
+        mnl = warp_min_u64(mnl);
+        mxl = warp_max_u64(mxl);
+        mnr = warp_min_u64(mnr);
+        mxr = warp_max_u64(mxr);
+        if (lane == 0) {
+          atomicMin(&box[d], mnl);
+          atomicMax(&box[ND + d], mxl);
+          atomicMin(&box[2 * ND + d], mnr);
+          atomicMax(&box[3 * ND + d], mxr);
+        }
+      }
+      for (int i = tid; i < S; i += kMidThreads) I2[dsti[i]] = I[s0 + i];
+      __syncthreads();
+      if (tid == 0) {
+        for (int side = 0; side < 2; side++) {
+          const int cst = side ? right0 : s0, csz = side ? S - kleft : kleft;
+          if (csz <= kLocalMax) continue;  // phase 2 finishes it
+          if (n_next >= kMidNodes) {
+            atomicExch(err, 3);
+            continue;
+          }
+          MNode<ND> c;
+          c.start = cst;
+          c.size = csz;
+          c.h = 2 * nd.h + 1 + side;
+          c.pad = 0;
+          for (int d = 0; d < ND; d++) {
+            c.kmin[d] = box[2 * ND * side + d];
+            c.kmax[d] = box[2 * ND * side + ND + d];
+          }
+          nxt[n_next++] = c;
+        }
+      }
+      __syncthreads();  // the next node reuses the keys, destinations and boxes
+    }
+    if (tid == 0) n_cur = n_next;
+    MNode<ND>* t = cur;
+    cur = nxt;
+    nxt = t;
+    buf ^= 1;
+    __syncthreads();
+  }
+}
+
 // ---- phase 2: one CTA per subtree of at most kLocalMax particles.
 // The subtree is sorted once along every coordinate (key, then local index). No level
 // sorts again: a node's bounding box is the first and last entry of its segment in each
@@ -1041,7 +1357,7 @@ struct PlanCache {
   std::vector<TreeSpec> trees;
   std::vector<PlanLevel> levels;
   int max_ng = 0;
-  size_t nch = 0, nroots = 0, bg = 0, bc = 0, br = 0;
+  size_t nch = 0, nroots = 0, nmroots = 0, bg = 0, bc = 0, br = 0, bm = 0;
 };
 bool same_trees(const std::vector<TreeSpec>& a, const std::vector<TreeSpec>& b) {
   if (a.size() != b.size()) return false;
@@ -1146,15 +1462,38 @@ static int build_forest_t(const std::vector<TreeSpec>& trees, int b, const doubl
   if (!hit) {
     cache.valid = false;
     std::vector<LRoot> lroots;
+    std::vector<MRoot> mroots;
     struct HN {
       int64_t start, size;
       int h, nbase;
     };
+    // a subtree of kLocalMax < size <= kMidMax particles at ping-pong side `side`: one
+    // CTA of phase 1b splits it level by level (each level flips the side); its
+    // descendants of at most kLocalMax particles go to phase 2 on the side they land on
+    auto add_mid = [&](const HN& r, int side) {
+      mroots.push_back({(int)r.start, (int)r.size, r.nbase, r.h, side, 0});
+      std::vector<HN> lev{r}, down;
+      while (!lev.empty()) {
+        side ^= 1;
+        down.clear();
+        for (const HN& x : lev) {
+          int64_t l = (x.size - 1) / 2 + 1;
+          for (HN c : {HN{x.start, l, 2 * x.h + 1, x.nbase},
+                       HN{x.start + l, x.size - l, 2 * x.h + 2, x.nbase}}) {
+            if (c.size <= kLocalMax) lroots.push_back({(int)c.start, (int)c.size, c.nbase, c.h, side, 0});
+            else down.push_back(c);
+          }
+        }
+        lev.swap(down);
+      }
+    };
     std::vector<HN> cur, nxt;
     for (auto& t : trees) {
       if (t.n <= 0) continue;
+      HN r{t.pstart - p0, t.n, 0, t.nbase};
       if (t.n <= kLocalMax) lroots.push_back({(int)(t.pstart - p0), (int)t.n, t.nbase, 0, 0, 0});
-      else cur.push_back({t.pstart - p0, t.n, 0, t.nbase});
+      else if (t.n <= kMidMax) add_mid(r, 0);
+      else cur.push_back(r);
     }
     std::vector<GNode> gn;
     std::vector<Chunk> ch;
@@ -1198,6 +1537,8 @@ static int build_forest_t(const std::vector<TreeSpec>& trees, int b, const doubl
         for (HN x : {Lh, Rh}) {
           if (x.size <= kLocalMax) {
             lroots.push_back({(int)x.start, (int)x.size, x.nbase, x.h, buf, 0});
+          } else if (x.size <= kMidMax) {
+            add_mid(x, buf);
           } else {
             gn[L.g0 + i].child[side] = (int)nxt.size();
             nxt.push_back(x);
@@ -1207,12 +1548,12 @@ static int build_forest_t(const std::vector<TreeSpec>& trees, int b, const doubl
       }
       cur.swap(nxt);
     }
-    // one upload: [GNode...][Chunk...][LRoot...]
+    // one upload: [GNode...][Chunk...][LRoot...][MRoot...]
     size_t bg = sizeof(GNode) * gn.size(), bc = sizeof(Chunk) * ch.size(),
-           br = sizeof(LRoot) * lroots.size();
+           br = sizeof(LRoot) * lroots.size(), bm = sizeof(MRoot) * mroots.size();
     // staged in page-locked memory so the upload is a plain asynchronous copy (the build's
     // final synchronisation orders it before the buffer is reused by this thread)
-    PinnedStage& plan = pinned_stage(bg + bc + br + 16);
+    PinnedStage& plan = pinned_stage(bg + bc + br + bm + 16);
     if (!plan.data()) {
       set_error("tree build: page-locked staging allocation failed");
       return NBK_ERR_NOMEM;
@@ -1220,6 +1561,7 @@ static int build_forest_t(const std::vector<TreeSpec>& trees, int b, const doubl
     memcpy(plan.data(), gn.data(), bg);
     memcpy(plan.data() + bg, ch.data(), bc);
     memcpy(plan.data() + bg + bc, lroots.data(), br);
+    memcpy(plan.data() + bg + bc + br, mroots.data(), bm);
     plan.gen++;
     cache.stage = plan.p;
     cache.gen = plan.gen;
@@ -1231,14 +1573,17 @@ static int build_forest_t(const std::vector<TreeSpec>& trees, int b, const doubl
     cache.max_ng = max_ng;
     cache.nch = ch.size();
     cache.nroots = lroots.size();
+    cache.nmroots = mroots.size();
     cache.bg = bg;
     cache.bc = bc;
     cache.br = br;
+    cache.bm = bm;
   }
   const std::vector<PlanLevel>& levels = cache.levels;
   const int max_ng = cache.max_ng;
-  const size_t nch = cache.nch, nroots = cache.nroots, bg = cache.bg, bc = cache.bc;
-  PinnedStage& plan = pinned_stage(cache.bg + cache.bc + cache.br + 16);
+  const size_t nch = cache.nch, nroots = cache.nroots, nmroots = cache.nmroots, bg = cache.bg,
+               bc = cache.bc, br = cache.br;
+  PinnedStage& plan = pinned_stage(cache.bg + cache.bc + cache.br + cache.bm + 16);
   if (!plan.data()) {
     cache.valid = false;
     set_error("tree build: page-locked staging allocation failed");
@@ -1277,6 +1622,7 @@ static int build_forest_t(const std::vector<TreeSpec>& trees, int b, const doubl
   GNode* d_gall = (GNode*)d_plan;
   Chunk* d_call = (Chunk*)(d_plan + bg);
   LRoot* d_r = (LRoot*)(d_plan + bg + bc);
+  MRoot* d_m = (MRoot*)(d_plan + bg + bc + br);
   k_init_soa<ND><<<(unsigned)((ntot + 255) / 256), 256, 0, st>>>(
       d_pos_in + 3 * p0, d_vel_in ? d_vel_in + 3 * p0 : nullptr, Ca, cs, IDa, ntot, d_err);
   note_launch();
@@ -1303,6 +1649,14 @@ static int build_forest_t(const std::vector<TreeSpec>& trees, int b, const doubl
     k_count_scan<ND><<<nc, kThreads, 0, st>>>(d_c, d_g, C, cs, cl, ce, bl, be, nout);
     note_launch();
     k_scatter<ND><<<nc, kThreads, 0, st>>>(d_c, d_g, C, I, C2, I2, cs, bl, be, d_err, d_gnext);
+    note_launch();
+    NBK_CUDA_TRY(cudaGetLastError());
+  }
+  if (nmroots > 0) {
+    size_t sm = MidLayout<ND>::total;
+    NBK_TRY(ensure_dyn_smem((const void*)k_mid_build<ND>, (int)sm));
+    k_mid_build<ND><<<(unsigned)nmroots, kMidThreads, sm, st>>>(d_m, Ca, IDa, Cb, IDb, cs, nout,
+                                                                d_err, (int)p0);
     note_launch();
     NBK_CUDA_TRY(cudaGetLastError());
   }
