@@ -695,17 +695,23 @@ __global__ void __launch_bounds__(kThreads) k_scatter(const Chunk* __restrict__ 
 }
 
 // ---- phase 1b: one CTA per subtree of at most kMidMax (and more than kLocalMax) particles.
-// The CTA splits the subtree's nodes level by level, one node at a time, down to the
-// subtrees of at most kLocalMax particles that phase 2 finishes. Each split makes the
-// same decisions as a global level -- split dimension from the node box, the median key
-// by radix passes over the order keys (kept in shared memory; the median's class is
-// ranked directly once it holds at most kMidCollect keys), the stable 3-way partition
-// into the other buffer, the children's boxes -- with block barriers where a global level
-// needs arrival counters and launches.
+// The CTA splits the subtree's nodes level by level down to the subtrees of at most
+// kLocalMax particles that phase 2 finishes; the nodes of one level (at most kMidGroups)
+// are split at the same time, each by its own group of warps synchronised by a named
+// barrier. Each split makes the same decisions as a global level -- split dimension from
+// the node box, the median key by radix passes over the order keys (kept in shared
+// memory; the median's class is ranked directly once it holds at most kMidCollect keys),
+// the stable 3-way partition into the other buffer, the children's boxes -- with group
+// barriers where a global level needs arrival counters and launches.
 constexpr int kMidMax = 8192;
 constexpr int kMidThreads = 1024;
-constexpr int kMidCollect = 256;  // a class this small is ranked directly (O(n^2) compares)
-constexpr int kMidNodes = kMidMax / kLocalMax;  // nodes above kLocalMax on one level
+constexpr int kMidGroups = 4;     // a level of a subtree of <= 8192 holds <= 4 nodes above 1024
+constexpr int kMidCollect = 32;   // a class this small is ranked directly by one warp
+constexpr int kMidNodes = 2 * kMidGroups;
+constexpr int kMidRounds = 8;     // keys per group thread on a level: at most 8192 / 1024
+static_assert(kMidMax <= kMidGroups * 2 * kLocalMax, "a subtree level fits in the groups");
+static_assert(kMidCollect <= kMidThreads / kMidGroups, "one candidate per group thread");
+static_assert(kMidMax <= kMidRounds * kMidThreads, "a level's keys fit the group's rounds");
 
 struct MRoot {
   int start, size;  // absolute range in the ping-pong buffers
@@ -724,13 +730,47 @@ template <int ND>
 struct MidLayout {
   static constexpr size_t key = 0;                                              // u64[kMidMax]
   static constexpr size_t dst = key + sizeof(unsigned long long) * kMidMax;     // int[kMidMax]
-  static constexpr size_t bins = dst + sizeof(int) * kMidMax;  // u32[kBins], or u64[kMidCollect] keys
-  static constexpr size_t nodes = bins + sizeof(unsigned) * kBins;              // MNode[2][kMidNodes]
+  // per group: u32[kBins] bins, or u64[kMidCollect] gathered keys
+  static constexpr size_t bins = dst + sizeof(int) * kMidMax;
+  static constexpr size_t nodes = bins + sizeof(unsigned) * kBins * kMidGroups;  // MNode[2][kMidNodes]
   static constexpr size_t total = nodes + sizeof(MNode<ND>) * 2 * kMidNodes;
   static_assert(sizeof(unsigned) * kBins >= sizeof(unsigned long long) * kMidCollect,
                 "the gathered keys share the bins' shared memory");
   static_assert(nodes % 16 == 0, "MNode alignment");
 };
+
+// Barrier of the nt threads of group g (named barrier g + 1; nt a multiple of 32).
+__device__ __forceinline__ void group_sync(int g, int nt) {
+  asm volatile("bar.sync %0, %1;" ::"r"(g + 1), "r"(nt) : "memory");
+}
+
+// Exclusive scan over the nt threads of group g (r: the thread's rank in the group); the
+// group's total goes to *tot.
+__device__ __forceinline__ unsigned group_excl_scan(unsigned v, int r, int nt, int g,
+                                                    unsigned* tot, unsigned* wsum) {
+  const int lane = r & 31, w = r >> 5, nw = nt >> 5;
+  unsigned incl = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) wsum[w] = incl;
+  group_sync(g, nt);
+  if (w == 0) {
+    unsigned x = lane < nw ? wsum[lane] : 0;
+    unsigned xi = x;
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned t = __shfl_up_sync(0xffffffffu, xi, o);
+      if (lane >= o) xi += t;
+    }
+    if (lane < nw) wsum[lane] = xi - x;
+    if (lane == nw - 1) *tot = xi;
+  }
+  group_sync(g, nt);
+  unsigned res = incl - v + wsum[w];
+  group_sync(g, nt);
+  return res;
+}
 
 template <int ND>
 __global__ void __launch_bounds__(kMidThreads) k_mid_build(
@@ -738,23 +778,22 @@ __global__ void __launch_bounds__(kMidThreads) k_mid_build(
     NodeOut<ND> out, int* err, int p0) {
   using L = MidLayout<ND>;
   extern __shared__ __align__(16) unsigned char smem[];
-  unsigned long long* key = (unsigned long long*)(smem + L::key);
-  int* dsti = (int*)(smem + L::dst);
-  unsigned* bin = (unsigned*)(smem + L::bins);
-  unsigned long long* cand = (unsigned long long*)(smem + L::bins);
+  unsigned long long* key_all = (unsigned long long*)(smem + L::key);
+  int* dst_all = (int*)(smem + L::dst);
   MNode<ND>* cur = (MNode<ND>*)(smem + L::nodes);
   MNode<ND>* nxt = cur + kMidNodes;
-  __shared__ unsigned wsum[32], tot;
-  __shared__ int n_cur, n_next, s_k, s_ncand;
-  __shared__ unsigned s_fill;
-  __shared__ unsigned long long s_prefix;
-  __shared__ unsigned long long box[4 * ND];  // left min, left max, right min, right max
+  __shared__ unsigned wsum[kMidGroups][32], tot[kMidGroups];
+  __shared__ int n_cur, n_next, s_k[kMidGroups], s_ncand[kMidGroups];
+  __shared__ unsigned s_fill[kMidGroups];
+  __shared__ unsigned long long s_prefix[kMidGroups];
+  // per group: left min, left max, right min, right max
+  __shared__ unsigned long long box[kMidGroups][4 * ND];
   const int tid = threadIdx.x, lane = tid & 31;
   const MRoot R = roots[blockIdx.x];
   int buf = R.buf;
 
-  // the subtree root's box
-  if (tid < 2 * ND) box[tid] = tid < ND ? ~0ull : 0ull;
+  // the subtree root's box (every thread)
+  if (tid < 2 * ND) box[0][tid] = tid < ND ? ~0ull : 0ull;
   __syncthreads();
   {
     const double* C = buf ? Cb : Ca;
@@ -769,8 +808,8 @@ __global__ void __launch_bounds__(kMidThreads) k_mid_build(
       mn = warp_min_u64(mn);
       mx = warp_max_u64(mx);
       if (lane == 0) {
-        atomicMin(&box[d], mn);
-        atomicMax(&box[ND + d], mx);
+        atomicMin(&box[0][d], mn);
+        atomicMax(&box[0][ND + d], mx);
       }
     }
   }
@@ -782,23 +821,34 @@ __global__ void __launch_bounds__(kMidThreads) k_mid_build(
     r.h = R.h;
     r.pad = 0;
     for (int d = 0; d < ND; d++) {
-      r.kmin[d] = box[d];
-      r.kmax[d] = box[ND + d];
+      r.kmin[d] = box[0][d];
+      r.kmax[d] = box[0][ND + d];
     }
     cur[0] = r;
     n_cur = 1;
+    n_next = 0;
   }
   __syncthreads();
-  for (int depth = 0; depth < 32 && n_cur > 0; depth++) {
+  for (int depth = 0; depth < 32; depth++) {
+    const int ncur = n_cur;  // read by every thread before thread 0 rewrites it
+    if (ncur <= 0) break;
+    if (ncur > kMidGroups) {  // cannot happen for subtrees of <= kMidMax particles
+      if (tid == 0) atomicExch(err, 3);
+      break;
+    }
+    const int G = ncur <= 1 ? 1 : (ncur <= 2 ? 2 : 4);
+    const int nt = kMidThreads / G, g = tid / nt, r = tid - g * nt;
     const double* C = buf ? Cb : Ca;
     const int* I = buf ? IDb : IDa;
     double* C2 = buf ? Ca : Cb;
     int* I2 = buf ? IDa : IDb;
-    const int ncur = n_cur;  // read by every thread before thread 0 rewrites it
-    if (tid == 0) n_next = 0;
-    for (int j = 0; j < ncur; j++) {
-      const MNode<ND> nd = cur[j];
+    if (g < ncur) {
+      const MNode<ND> nd = cur[g];
       const int S = nd.size, s0 = nd.start;
+      unsigned long long* key = key_all + (s0 - R.start);  // the node's slice: disjoint per node
+      int* dsti = dst_all + (s0 - R.start);
+      unsigned* bin = (unsigned*)(smem + L::bins) + g * kBins;
+      unsigned long long* cand = (unsigned long long*)bin;
       // DetermineSplitDim: the first strictly larger FP64 spread wins
       double lo[ND], hi[ND];
 #pragma unroll
@@ -817,7 +867,7 @@ __global__ void __launch_bounds__(kMidThreads) k_mid_build(
         }
       }
       const double* Cd = C + (int64_t)dim * cs + s0;
-      for (int i = tid; i < S; i += kMidThreads) key[i] = okey(Cd[i]);
+      for (int i = r; i < S; i += nt) key[i] = okey(Cd[i]);
       // the median key: rank kr = (S - 1) / 2 along dim
       const int kr = (S - 1) / 2;
       const unsigned long long kmin_dim = sel<ND>(nd.kmin, dim), kmax_dim = sel<ND>(nd.kmax, dim);
@@ -827,24 +877,24 @@ __global__ void __launch_bounds__(kMidThreads) k_mid_build(
                                                : (first_diff >= 63 ? 0ull : (~0ull << (first_diff + 1)));
       unsigned long long prefix = first_diff < 0 ? kmin_dim : (kmin_dim & mask);
       int k = kr, ncand = S;
-      __syncthreads();  // keys stored
+      group_sync(g, nt);  // keys stored
       for (int pass = 0; mask != ~0ull && pass < kPasses; pass++) {
         if (ncand <= kMidCollect) {
           // the class is small: gather its keys; the k-th smallest of them is the median key
-          if (tid == 0) s_fill = 0u;
-          __syncthreads();
-          for (int i = tid; i < S; i += kMidThreads) {
+          if (r == 0) s_fill[g] = 0u;
+          group_sync(g, nt);
+          for (int i = r; i < S; i += nt) {
             const unsigned long long kk = key[i];
             if ((kk & mask) == prefix) {
-              unsigned slot = atomicAdd(&s_fill, 1u);
+              unsigned slot = atomicAdd(&s_fill[g], 1u);
               if (slot < (unsigned)kMidCollect) cand[slot] = kk;
             }
           }
-          __syncthreads();
+          group_sync(g, nt);
           const int n = min(ncand, kMidCollect);
-          if (tid == 0 && s_fill != (unsigned)ncand) atomicExch(err, 5);
-          if (tid < n) {
-            const unsigned long long mine = cand[tid];
+          if (r == 0 && s_fill[g] != (unsigned)ncand) atomicExch(err, 5);
+          if (r < n) {
+            const unsigned long long mine = cand[r];
             int below = 0, equal = 0;
             for (int i = 0; i < n; i++) {
               const unsigned long long o = cand[i];
@@ -852,23 +902,23 @@ __global__ void __launch_bounds__(kMidThreads) k_mid_build(
               equal += o == mine;
             }
             const int kk = min(max(k, 0), n - 1);
-            if (below <= kk && kk < below + equal) s_prefix = mine;  // every holder: same value
+            if (below <= kk && kk < below + equal) s_prefix[g] = mine;  // every holder: same value
           }
-          __syncthreads();
-          prefix = s_prefix;
+          group_sync(g, nt);
+          prefix = s_prefix[g];
           mask = ~0ull;
-          __syncthreads();  // s_prefix and the gathered keys are read before any reuse
+          group_sync(g, nt);  // s_prefix and the gathered keys are read before any reuse
           break;
         }
         const int hi_bit = first_diff - 11 * pass;
         const int width = min(11, hi_bit + 1), shift = hi_bit - width + 1;
         const unsigned long long dmask = ((1ull << width) - 1ull) << shift;
-        for (int i = tid; i < kBins; i += kMidThreads) bin[i] = 0u;
-        __syncthreads();
+        for (int i = r; i < kBins; i += nt) bin[i] = 0u;
+        group_sync(g, nt);
         // whole warps per round (match_any needs every lane): lanes with the same digit
         // add once
-        for (int i0 = 0; i0 < S; i0 += kMidThreads) {
-          const int i = i0 + tid;
+        for (int i0 = 0; i0 < S; i0 += nt) {
+          const int i = i0 + r;
           int digit = -1;
           if (i < S) {
             const unsigned long long kk = key[i];
@@ -877,83 +927,121 @@ __global__ void __launch_bounds__(kMidThreads) k_mid_build(
           const unsigned peers = __match_any_sync(0xffffffffu, digit);
           if (digit >= 0 && lane == __ffs(peers) - 1) atomicAdd(&bin[digit], __popc(peers));
         }
-        __syncthreads();
+        group_sync(g, nt);
         // the digit whose bin holds rank k: each thread owns kPer consecutive bins
-        constexpr int kPer = kBins / kMidThreads;
-        unsigned cnt[kPer], sum = 0;
+        constexpr int kPerMax = kBins * kMidGroups / kMidThreads;
+        const int kPer = kBins / nt;
+        unsigned cnt[kPerMax], sum = 0;
 #pragma unroll
-        for (int q = 0; q < kPer; q++) {
-          cnt[q] = bin[tid * kPer + q];
+        for (int q = 0; q < kPerMax; q++) {
+          cnt[q] = q < kPer ? bin[r * kPer + q] : 0u;
           sum += cnt[q];
         }
-        unsigned before = block_excl_scan_t<kMidThreads>(sum, &tot, wsum);
+        unsigned before = group_excl_scan(sum, r, nt, g, &tot[g], wsum[g]);
         if (before <= (unsigned)k && (unsigned)k < before + sum) {
           int digit = -1;
 #pragma unroll
-          for (int q = 0; q < kPer; q++) {
-            if (digit < 0) {
+          for (int q = 0; q < kPerMax; q++) {
+            if (digit < 0 && q < kPer) {
               if ((unsigned)k < before + cnt[q]) {
-                digit = tid * kPer + q;
-                s_ncand = (int)cnt[q];
+                digit = r * kPer + q;
+                s_ncand[g] = (int)cnt[q];
               } else {
                 before += cnt[q];
               }
             }
           }
-          s_k = k - (int)before;
-          s_prefix = prefix | ((unsigned long long)digit << shift);
+          s_k[g] = k - (int)before;
+          s_prefix[g] = prefix | ((unsigned long long)digit << shift);
         }
-        __syncthreads();
-        k = s_k;
-        ncand = s_ncand;
-        prefix = s_prefix;
+        group_sync(g, nt);
+        k = s_k[g];
+        ncand = s_ncand[g];
+        prefix = s_prefix[g];
         mask |= dmask;
-        __syncthreads();  // the shared values are read before the next pass writes them
+        group_sync(g, nt);  // the shared values are read before the next pass writes them
       }
-      if (mask != ~0ull && tid == 0) atomicExch(err, 5);  // selection unfinished: report
+      if (mask != ~0ull && r == 0) atomicExch(err, 5);  // selection unfinished: report
       const unsigned long long piv = prefix;
-      // counts below / equal to the median key over contiguous runs, one per thread
-      const int E = (S + kMidThreads - 1) / kMidThreads;
-      const int r0 = min(tid * E, S), r1 = min(r0 + E, S);
-      unsigned a = 0, e = 0;
-      for (int i = r0; i < r1; i++) {
-        a += key[i] < piv;
-        e += key[i] == piv;
+      // the stable 3-way partition: warp w of the group takes WR rounds of 32 consecutive
+      // keys; ballots rank each key inside its round and class, one scan over the warps'
+      // (less, equal) counts orders the warps (counts packed in one word: both < 2^16)
+      const int nw = nt >> 5, w = r >> 5;
+      const int WR = (S + nt - 1) / nt;  // rounds per warp: at most kMidRounds
+      const int wbase = w * WR * 32;
+      unsigned cls = 0, nl = 0, ne = 0;
+#pragma unroll
+      for (int j = 0; j < kMidRounds; j++) {
+        if (j < WR) {
+          const int i = wbase + j * 32 + lane;
+          unsigned c = 3;
+          if (i < S) {
+            const unsigned long long kk = key[i];
+            c = kk < piv ? 0u : (kk == piv ? 1u : 2u);
+          }
+          cls |= c << (2 * j);
+          nl += __popc(__ballot_sync(0xffffffffu, c == 0));
+          ne += __popc(__ballot_sync(0xffffffffu, c == 1));
+        }
       }
-      // (less, equal) packed in one word: both counts stay below 2^16
-      const unsigned pre = block_excl_scan_t<kMidThreads>((a << 16) | e, &tot, wsum);
-      const int n_less = (int)(tot >> 16), total_eq = (int)(tot & 0xffffu);
+      if (lane == 0) wsum[g][w] = (nl << 16) | ne;
+      group_sync(g, nt);
+      if (w == 0) {
+        const unsigned v = lane < nw ? wsum[g][lane] : 0u;
+        unsigned incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+          const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += t;
+        }
+        if (lane < nw) wsum[g][lane] = incl - v;
+        if (lane == nw - 1) tot[g] = incl;
+      }
+      group_sync(g, nt);
+      const unsigned pre = wsum[g][w];
+      const int n_less = (int)(tot[g] >> 16), total_eq = (int)(tot[g] & 0xffffu);
       const int kleft = kr + 1, right0 = s0 + kleft;
       const int need_eq = kleft - n_less, excess = total_eq - need_eq;
-      if (tid == 0) out.write(R.nbase + nd.h, lo, hi, p0 + s0, S, dim, okey_inv(piv));
+      if (r == 0) out.write(R.nbase + nd.h, lo, hi, p0 + s0, S, dim, okey_inv(piv));
       // destinations: less, then the first need_eq equal keys on the left; the other equal
       // keys, then greater, on the right; each class in its current order
       unsigned rl = pre >> 16, re = pre & 0xffffu;
-      unsigned rg = (unsigned)r0 - rl - re;
-      for (int i = r0; i < r1; i++) {
-        const unsigned long long kk = key[i];
-        int dst;
-        if (kk < piv) {
-          dst = s0 + (int)(rl++);
-        } else if (kk == piv) {
-          const int q = (int)(re++);
-          dst = q < need_eq ? s0 + n_less + q : right0 + (q - need_eq);
-        } else {
-          dst = right0 + excess + (int)(rg++);
+      unsigned rg = (unsigned)min(wbase, S) - rl - re;  // greater keys before this warp
+      const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+      for (int j = 0; j < kMidRounds; j++) {
+        if (j < WR) {
+          const int i = wbase + j * 32 + lane;
+          const unsigned c = (cls >> (2 * j)) & 3u;
+          const unsigned bL = __ballot_sync(0xffffffffu, c == 0), bE = __ballot_sync(0xffffffffu, c == 1),
+                         bG = __ballot_sync(0xffffffffu, c == 2);
+          if (c != 3) {
+            int dst;
+            if (c == 0) {
+              dst = s0 + (int)(rl + __popc(bL & lt));
+            } else if (c == 1) {
+              const int q = (int)(re + __popc(bE & lt));
+              dst = q < need_eq ? s0 + n_less + q : right0 + (q - need_eq);
+            } else {
+              dst = right0 + excess + (int)(rg + __popc(bG & lt));
+            }
+            if (dst < s0 || dst >= s0 + S) {  // selection inconsistent: report, keep in bounds
+              atomicExch(err, 2);
+              dst = s0 + i;
+            }
+            dsti[i] = dst;
+          }
+          rl += __popc(bL);
+          re += __popc(bE);
+          rg += __popc(bG);
         }
-        if (dst < s0 || dst >= s0 + S) {  // selection inconsistent: report, keep in bounds
-          atomicExch(err, 2);
-          dst = s0 + i;
-        }
-        dsti[i] = dst;
       }
-      if (tid < 4 * ND) box[tid] = (tid % (2 * ND)) < ND ? ~0ull : 0ull;
-      __syncthreads();
+      if (r < 4 * ND) box[g][r] = (r % (2 * ND)) < ND ? ~0ull : 0ull;
+      group_sync(g, nt);
       // move every coordinate and id; the children's boxes on the way
 #pragma unroll
       for (int d = 0; d < ND; d++) {
         unsigned long long mnl = ~0ull, mxl = 0ull, mnr = ~0ull, mxr = 0ull;
-        for (int i = tid; i < S; i += kMidThreads) {
+        for (int i = r; i < S; i += nt) {
           const double v = C[d * cs + s0 + i];
           const int t = dsti[i];
           C2[d * cs + t] = v;
@@ -971,19 +1059,20 @@ __global__ void __launch_bounds__(kMidThreads) k_mid_build(
         mnr = warp_min_u64(mnr);
         mxr = warp_max_u64(mxr);
         if (lane == 0) {
-          atomicMin(&box[d], mnl);
-          atomicMax(&box[ND + d], mxl);
-          atomicMin(&box[2 * ND + d], mnr);
-          atomicMax(&box[3 * ND + d], mxr);
+          atomicMin(&box[g][d], mnl);
+          atomicMax(&box[g][ND + d], mxl);
+          atomicMin(&box[g][2 * ND + d], mnr);
+          atomicMax(&box[g][3 * ND + d], mxr);
         }
       }
-      for (int i = tid; i < S; i += kMidThreads) I2[dsti[i]] = I[s0 + i];
-      __syncthreads();
-      if (tid == 0) {
+      for (int i = r; i < S; i += nt) I2[dsti[i]] = I[s0 + i];
+      group_sync(g, nt);
+      if (r == 0) {
         for (int side = 0; side < 2; side++) {
           const int cst = side ? right0 : s0, csz = side ? S - kleft : kleft;
           if (csz <= kLocalMax) continue;  // phase 2 finishes it
-          if (n_next >= kMidNodes) {
+          const int slot = atomicAdd(&n_next, 1);
+          if (slot >= kMidNodes) {
             atomicExch(err, 3);
             continue;
           }
@@ -993,15 +1082,18 @@ __global__ void __launch_bounds__(kMidThreads) k_mid_build(
           c.h = 2 * nd.h + 1 + side;
           c.pad = 0;
           for (int d = 0; d < ND; d++) {
-            c.kmin[d] = box[2 * ND * side + d];
-            c.kmax[d] = box[2 * ND * side + ND + d];
+            c.kmin[d] = box[g][2 * ND * side + d];
+            c.kmax[d] = box[g][2 * ND * side + ND + d];
           }
-          nxt[n_next++] = c;
+          nxt[slot] = c;
         }
       }
-      __syncthreads();  // the next node reuses the keys, destinations and boxes
     }
-    if (tid == 0) n_cur = n_next;
+    __syncthreads();  // every group is done with this level
+    if (tid == 0) {
+      n_cur = min(n_next, kMidNodes);
+      n_next = 0;
+    }
     MNode<ND>* t = cur;
     cur = nxt;
     nxt = t;
@@ -1104,26 +1196,57 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_build(
     }
   }
   __syncthreads();
-  // ND segments of P sorted at once; every segment ascending by (key, local index)
+  // ND segments of P sorted at once; every segment ascending by (key, local index). A
+  // bitonic network: the steps with partner distance jj >= 32 exchange through shared
+  // memory (one thread per pair, a barrier per step); the steps with jj <= 16 pair lanes
+  // of one warp, so each thread takes its elements e = row * kLocalThreads + tid one row
+  // at a time through all of them in registers (shuffles, no barrier).
+  const int rows = (total + kLocalThreads - 1) / kLocalThreads;
   for (int kk = 2; kk <= P; kk <<= 1) {
-    for (int jj = kk >> 1; jj > 0; jj >>= 1) {
-      for (int t = threadIdx.x; t < total; t += kLocalThreads) {
-        int u = t ^ jj;
-        if (u > t) {
-          bool up = ((t & (P - 1)) & kk) == 0;
-          unsigned long long a = skey[t], c = skey[u];
-          unsigned short ia = sidx[t], ic = sidx[u];
-          bool gt = (a > c) || (a == c && ia > ic);
-          if (gt == up) {
-            skey[t] = c;
-            skey[u] = a;
-            sidx[t] = ic;
-            sidx[u] = ia;
-          }
+    for (int jj = kk >> 1; jj >= 32; jj >>= 1) {
+      for (int q = threadIdx.x; q < total / 2; q += kLocalThreads) {
+        const int t = ((q & ~(jj - 1)) << 1) | (q & (jj - 1)), u = t + jj;
+        const bool up = ((t & (P - 1)) & kk) == 0;
+        const unsigned long long a = skey[t], c = skey[u];
+        const unsigned short ia = sidx[t], ic = sidx[u];
+        const bool gt = (a > c) || (a == c && ia > ic);
+        if (gt == up) {
+          skey[t] = c;
+          skey[u] = a;
+          sidx[t] = ic;
+          sidx[u] = ia;
         }
       }
       __syncthreads();
     }
+    // the register steps: every kk up to 32 at once, later only jj = 16 .. 1
+    const int kk_last = kk < 32 ? min(32, P) : kk;
+    for (int row = 0; row < rows; row++) {
+      const int e = row * kLocalThreads + threadIdx.x;
+      const bool have = e < total;
+      unsigned long long a = have ? skey[e] : ~0ull;
+      unsigned ia = have ? sidx[e] : 0xffffu;
+      for (int k2 = kk; k2 <= kk_last; k2 <<= 1) {
+        for (int jj = min(k2 >> 1, 16); jj > 0; jj >>= 1) {
+          const unsigned long long c = __shfl_xor_sync(0xffffffffu, a, jj);
+          const unsigned ic = __shfl_xor_sync(0xffffffffu, ia, jj);
+          const bool lower = (e & jj) == 0;
+          const bool up = ((e & (P - 1)) & k2) == 0;
+          // the lower element of a pair keeps the smaller (up) or larger (down) one
+          const bool other_less = (c < a) || (c == a && ic < ia);
+          if (other_less == (lower == up)) {
+            a = c;
+            ia = ic;
+          }
+        }
+      }
+      if (have) {
+        skey[e] = a;
+        sidx[e] = (unsigned short)ia;
+      }
+    }
+    __syncthreads();
+    kk = kk_last;
   }
   unsigned short* cur = lst;
   unsigned short* nxt = lst + NL * K;
