@@ -1182,11 +1182,14 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_build(
     id[e] = I[R.start + e];
   }
   __syncthreads();
-  int P = 1;
-  while (P < S) P <<= 1;
+  int P = 1, lgP = 0;
+  while (P < S) {
+    P <<= 1;
+    lgP++;
+  }
   const int total = ND * P;
   for (int t = threadIdx.x; t < total; t += kLocalThreads) {
-    int d = t / P, r = t - d * P;
+    int d = t >> lgP, r = t & (P - 1);
     if (r < S) {
       skey[t] = okey(cc[d * K + r]);
       sidx[t] = (unsigned short)r;
@@ -1250,14 +1253,16 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_build(
   }
   unsigned short* cur = lst;
   unsigned short* nxt = lst + NL * K;
-  for (int t = threadIdx.x; t < ND * S; t += kLocalThreads) {
-    int d = t / S, i = t - d * S;
-    unsigned short q = sidx[d * P + i];
-    if (q >= S) {  // a padding slot inside the sorted range: report, keep in bounds
-      atomicExch(err, 3);
-      q = (unsigned short)i;
+#pragma unroll
+  for (int d = 0; d < ND; d++) {
+    for (int i = threadIdx.x; i < S; i += kLocalThreads) {
+      unsigned short q = sidx[d * P + i];
+      if (q >= S) {  // a padding slot inside the sorted range: report, keep in bounds
+        atomicExch(err, 3);
+        q = (unsigned short)i;
+      }
+      cur[d * K + i] = q;
     }
-    cur[d * K + i] = q;
   }
   __syncthreads();  // the sort keys' region is reused from here on
   for (int i = threadIdx.x; i < S; i += kLocalThreads) {
@@ -1333,12 +1338,11 @@ __global__ void __launch_bounds__(kLocalThreads) k_local_build(
     __syncthreads();
     if (n_next == 0 || n_next > kLevelCap) break;
     // B: which particles go left, read off the list of their node's split dimension
-    for (int t = threadIdx.x; t < ND * S; t += kLocalThreads) {
-      int d = t / S, i = t - d * S;
-      int j = node_at[i];
+    for (int i = threadIdx.x; i < S; i += kLocalThreads) {
+      const int j = node_at[i];
       if (j >= 0) {
-        LNode nd = lv[j];
-        if (nd.dim == d) left[cur[d * K + i]] = (i - nd.start) < nd.kl;
+        const LNode nd = lv[j];
+        if (nd.dim >= 0) left[cur[nd.dim * K + i]] = (i - nd.start) < nd.kl;
       }
     }
     __syncthreads();
