@@ -228,8 +228,11 @@ __global__ void __launch_bounds__(32 * kWpb, 4) k_link(FofArgs a) {
       }
       __syncwarp();
       sp -= m;
-      unsigned todo = __ballot_sync(FULL, keep);
-      unsigned expand = 0;
+      // a kept node that is neither compact nor a leaf is expanded at once: the lanes'
+      // own balls are tested at its leaves
+      const bool inner = keep && !cpt && r.count > tv.b;
+      unsigned expand = __ballot_sync(FULL, inner);
+      unsigned todo = __ballot_sync(FULL, keep && !inner);
       while (todo) {
         int j = __ffs(todo) - 1;
         todo &= todo - 1;
@@ -568,8 +571,11 @@ __global__ void __launch_bounds__(32 * kWpb) k_crit6_warp(FofArgs a) {
       }
       __syncwarp();
       sp -= m;
-      unsigned todo = __ballot_sync(FULL, keep);
-      unsigned expand = 0;
+      // a kept inner node is expanded at once: the lanes' own queries are tested at its
+      // leaves
+      const bool inner = keep && nd.split_dim >= 0;
+      unsigned expand = __ballot_sync(FULL, inner);
+      unsigned todo = __ballot_sync(FULL, keep && !inner);
       while (todo) {
         const int jn = __ffs(todo) - 1;
         todo &= todo - 1;
