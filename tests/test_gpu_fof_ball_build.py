@@ -41,8 +41,12 @@ def test_build_same_nodes_and_leaves_as_reference(gpu, name):
     np.testing.assert_array_equal(leaf_labels(t), g["leaf_start_ids"])
 
 
+# the sizes cover each build tier and its edges: one per-CTA subtree (<= 1024), a
+# mid-tier subtree split by one CTA (1025-8192: 1025, 3001, 8192), global levels above
+# it (8193, 16385, 2^20), and b = 2 (deep per-CTA subtrees)
 @pytest.mark.parametrize("n,b", [(1, 16), (17, 16), (1000, 16), (1025, 16), (3001, 7),
-                                  (1 << 20, 16), (300000, 2)])
+                                  (8192, 16), (8193, 16), (16385, 5), (1 << 20, 16),
+                                  (300000, 2)])
 def test_build_leaf_sets_vs_oracle(gpu, port_built, n, b):
     pos, mass = syn.clustered_box(n, 100.0, seed=n % 97)
     o = oracle.OracleTree(pos, None, mass, b, 0, 0, 1000, None, backend="port", nthreads=8)
