@@ -63,6 +63,7 @@ struct GNodeT {
 constexpr int kPasses = 6;
 constexpr int kBins = 2048;
 constexpr int kCollect = kThreads;  // a class this small is gathered and ranked by one block
+static_assert(kCollect % kThreads == 0, "whole keys per thread");
 
 struct Chunk {
   int g;      // gnode index within the level
@@ -370,25 +371,38 @@ __global__ void __launch_bounds__(kThreads) k_radix(const Chunk* __restrict__ ch
   const unsigned long long base_prefix = pass == 0 ? (kmin_dim & common) : s.prefix;
   const unsigned long long base_mask = pass == 0 ? common : s.mask;
   if (collect) {
-    // the k-th smallest of the gathered keys is the median key: thread t holds key t and
-    // counts the keys below it and equal to it
+    // the k-th smallest of the gathered keys is the median key: thread t holds keys t,
+    // t + kThreads, ... and counts the keys below and equal to each
+    constexpr int kPerT = kCollect / kThreads;
     int n = min(s.ncand, kCollect);
     if (threadIdx.x == 0 && __ldcg(&g[c.g].nfill) != (unsigned)s.ncand) atomicExch(err, 5);
-    unsigned long long mine = ~0ull;
-    if ((int)threadIdx.x < n) mine = __ldcg(&cand[s.start + threadIdx.x]);
-    sk[threadIdx.x] = mine;
+    unsigned long long mine[kPerT];
+#pragma unroll
+    for (int q = 0; q < kPerT; q++) {
+      const int i = (int)threadIdx.x + q * kThreads;
+      mine[q] = i < n ? __ldcg(&cand[s.start + i]) : ~0ull;
+      sk[i] = mine[q];
+    }
     __syncthreads();
-    int below = 0, equal = 0;
+    int below[kPerT], equal[kPerT];
+#pragma unroll
+    for (int q = 0; q < kPerT; q++) below[q] = equal[q] = 0;
     for (int i = 0; i < n; i++) {
-      unsigned long long o = sk[i];
-      below += o < mine;
-      equal += o == mine;
+      const unsigned long long o = sk[i];
+#pragma unroll
+      for (int q = 0; q < kPerT; q++) {
+        below[q] += o < mine[q];
+        equal[q] += o == mine[q];
+      }
     }
     int kr = min(max(s.k, 0), n - 1);
-    if ((int)threadIdx.x < n && below <= kr && kr < below + equal) {
-      // every holder of the k-th key writes the same value
-      g[c.g].prefix = mine;
-      g[c.g].mask = ~0ull;
+#pragma unroll
+    for (int q = 0; q < kPerT; q++) {
+      if ((int)threadIdx.x + q * kThreads < n && below[q] <= kr && kr < below[q] + equal[q]) {
+        // every holder of the k-th key writes the same value
+        g[c.g].prefix = mine[q];
+        g[c.g].mask = ~0ull;
+      }
     }
     if (threadIdx.x == 0) g[c.g].nfill = 0u;
     return;
