@@ -305,6 +305,23 @@ __device__ void ph_coop(const TreeView& tv, PhWarp<KMAX>& w, int lane, bool acti
     e32[k] = fmaxf(tv.eps6[k], __fmul_ru(__double2float_ru(fabs(x[k])), 1.2e-7f));
   }
   float thr = thresh_hi_bits(dkey(top));
+  // A first screen of each pair in round to nearest: with dx = fl(q - c) per coordinate
+  // and dc = fl(sum w32 dx^2) (relative error below 2^-21), the weighted distance in the
+  // exact coordinates is at least (sqrt(dc / (1 + 2^-21)) / (1 + 2^-24) - e0)^2, where
+  // e0 = |sqrt(w32) 2 e32| bounds the coordinates' FP32 rounding; so dc >= thr_far =
+  // (sqrt(thr) + e0)^2 (1 + 2^-20), every operation rounded up, proves it is >= thr.
+  float e0 = 0.f;
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    const float t = __fmul_ru(2.f, e32[k]);
+    e0 = __fadd_ru(e0, __fmul_ru(__fmul_ru(w32[k], t), t));
+  }
+  e0 = __fsqrt_ru(e0);
+  auto far_of = [&](float t) {
+    const float s = __fadd_ru(__fsqrt_ru(t), e0);
+    return __fmul_ru(__fmul_ru(s, s), 1.0f + 1.0f / 1048576.0f);
+  };
+  float thr_far = far_of(thr);
   const NodeS* N = tv.nodes6 + tv.nbase;
   const NodeF6* F = tv.nodef6 + tv.nbase;
   double m[6] = {1, 1, 1, 1, 1, 1};
@@ -336,6 +353,15 @@ __device__ void ph_coop(const TreeView& tv, PhWarp<KMAX>& w, int lane, bool acti
             if (ti == skip) continue;
             const float4 a = w.sp[j], b = w.sv[j];
             const float c[6] = {a.x, a.y, a.z, b.x, b.y, b.z};
+            {
+              float dc = 0.f;
+#pragma unroll
+              for (int k = 0; k < 6; k++) {
+                const float d = q32[k] - c[k];
+                dc = fmaf(w32[k] * d, d, dc);
+              }
+              if (dc >= thr_far) continue;
+            }
             if (pair_lb6f(q32, c, w32, e32) >= thr) continue;
             const P4 p = tv.pos[ti];
             const V4 v = tv.vel[ti];
@@ -344,6 +370,7 @@ __device__ void ph_coop(const TreeView& tv, PhWarp<KMAX>& w, int lane, bool acti
               ph_replace_top<KMAX, 32>(w.H, lane, K, d2, ti);
               top = w.H.d[0][lane];
               thr = thresh_hi_bits(dkey(top));
+              thr_far = far_of(thr);
             }
           }
         }
