@@ -152,7 +152,8 @@ __device__ __forceinline__ bool crit_cmp(int cmp, const double* p, const double 
 // step pops up to 32 nodes from the warp's stack, lane i loads node i, drops it when it
 // lies farther than ll from the box around all of the warp's query points, and for a
 // compact node chases its union-find root, so the dependent loads of up to 32 nodes
-// overlap. The surviving nodes are then tested against every lane's own query.
+// overlap. Surviving inner nodes that are not compact are expanded at once; surviving
+// leaves and compact nodes are then tested against every lane's own query.
 //
 // CRIT3D: FOFCriterion with FOF3d inside its search region, run as FOF with
 // ll^2 = params[6]; the FP32 decisions are the same (their 2^-20 margins cover the
