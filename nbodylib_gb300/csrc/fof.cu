@@ -552,7 +552,8 @@ __global__ void __launch_bounds__(32 * kWpb) k_crit6_warp(FofArgs a) {
     __syncwarp();
     // frontier-parallel: each step pops up to 32 nodes, lane i loads node i and drops it
     // when the warp's query box cannot reach it, so the dependent node loads overlap; the
-    // surviving nodes are then tested against every lane's own query
+    // surviving inner nodes are expanded at once, the surviving leaves tested against
+    // every lane's own query
     for (int guard = 0; sp > 0 && guard < (1 << 26); guard++) {
       // above kCritBatchLimit entries pop one node at a time: a depth-first descent from
       // there adds at most the tree depth, so the stack never exceeds kCritStack
